@@ -1,0 +1,305 @@
+"""Benchmark: Mrays/s of the GB300 projection engine on the voxel-grid workload.
+
+Workload (one step = one pass of the hot path over one batch): the 256^3 FP32
+grid of 64 seeded Gaussians rendered from 180 views (azimuth 0, 2, ..., 358
+degrees, polar 90) at 1024x1024 with the uniform-step integrator, ds = half a
+voxel (2/256/2), R = 4, fov = 40 -- 188.7 M rays per step.
+
+value     : device throughput, volume resident in HBM, output to a device
+            buffer, L2 flushed (256 MiB write) before every timed step, each
+            step timed with CUDA events on the launching stream.
+e2e       : the same metric through the reference ABI call
+            RenderVolumeProjectionsCUDA with pinned host buffers (volume
+            upload and image download inside the timed region).
+roofline  : the render kernel against the FP32 FMA peak measured in this run
+            by a CUDA-core SGEMM (TF32 off); the algorithmic work is the
+            exact count of lattice samples the kernel evaluates (a counter
+            pass) times 58 FLOPs per trilinear sample.
+cpu_baseline / --impl reference: the FP64 CPU restatement of the reference
+            path (oracle/), on all host cores, on a seeded ray subset.
+
+Multi-GPU: the path has no exchange step; N processes render disjoint view
+subsets (view k on rank k mod N) with no collective ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_PER_SAMPLE = 58  # 8 common (position + accumulate) + 50 trilinear
+METRIC = "Mrays/s on 1 GB300 (uniform-step integrator, voxel grid 256^3, 180 views x 1024^2)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--views", type=int, default=180)
+    p.add_argument("--res", type=int, default=1024)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region (the recipe's query)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = float(s[2])
+                for k, n in enumerate(names):
+                    if s[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def fp32_peak_tflops(torch):
+    """CUDA-core FP32 throughput via SGEMM with TF32 disabled (best of 5)."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    for _ in range(2):
+        torch.mm(a, b)
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_baseline(workload, seconds, threads=None):
+    """FP64 oracle on a seeded subset of the workload's rays, all host cores."""
+    from oracle import oracle as O
+    vol = workload.volume
+    cams21 = None
+    threads = threads or os.cpu_count() or 1
+    from xray_projection_render_gb300 import engine  # camera rows only (host code)
+    cams21 = engine.xray_camera_params(workload.angles, workload.R, workload.fov)
+    rng = np.random.default_rng(1234)
+
+    def run(n):
+        rays = np.stack([rng.integers(0, len(workload.angles), n), rng.integers(0, workload.res, n),
+                         rng.integers(0, workload.res, n)], 1).astype(np.int32)
+        t = time.perf_counter()
+        O.render_volume_abi(vol, cams21, workload.res, np.float32(workload.ds), rays=rays,
+                            nthreads=threads)
+        return time.perf_counter() - t
+
+    n = 2000
+    dt = run(n)
+    n2 = int(max(2000, min(5_000_000, n * seconds / max(dt, 1e-3))))
+    dt2 = run(n2)
+    return {"value": n2 / dt2 / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{n2} seeded random rays of the {len(workload.angles)}x{workload.res}^2 "
+                      f"voxel workload ({dt2:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from xray_projection_render_gb300 import workloads as W
+    w = W.voxel_blobs(args.res, args.views)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(w, max(2.0, args.cpu_seconds / max(1, args.steps)))
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.median(vals))
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": w.name, "views": len(w.angles), "res": w.res, "ds": w.ds},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import __graft_entry__ as G
+    import xray_projection_render_gb300 as X
+    from xray_projection_render_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    G.build()
+    w = W.voxel_blobs(args.res, args.views)
+    my_angles = w.angles[rank::world]
+    n_my = len(my_angles)
+    res = w.res
+    img = res * res
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    vol_dev = torch.from_numpy(w.volume).to(dev)
+    scene = X.Scene(w.obj, None, [vol_dev])
+    out = torch.empty((n_my, res, res), device=dev, dtype=torch.float32)
+    flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)  # 256 MiB > L2
+
+    def step():
+        X.render(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, out=out,
+                 stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # exact sample count of one step (counter pass, untimed)
+    _, samples, fp64 = X.render(scene, my_angles[:max(1, min(8, n_my))], resolution=res, ds=w.ds,
+                                R=w.R, fov=w.fov, stats=True)
+    frac = min(8, n_my) / n_my
+    samples_step = samples / frac
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    t_step = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([t_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    rays_total = len(w.angles) * img
+    value = rays_total / t_step / 1e6
+
+    # end to end through the reference ABI with pinned host buffers
+    cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
+    vol_host = torch.from_numpy(w.volume).pin_memory()
+    out_host = torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
+    X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)  # warm
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
+        e2e_times.append(time.perf_counter() - t0)
+    t_e2e = float(np.mean(e2e_times))
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e_value = rays_total / t_e2e / 1e6
+
+    peaks = measured_peaks()
+    fp32_peak = fp32_peak_tflops(torch)
+    achieved = samples_step * FLOPS_PER_SAMPLE / t_step / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Gaussian-blob grid)",
+        "config": {"workload": w.name, "views": len(w.angles), "res": res, "ds": w.ds,
+                   "grid": [256, 256, 256], "integrator": "simple", "R": w.R, "fov": w.fov,
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "parallelism": f"views k mod {world}"},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s",
+                "h2d_bytes_per_step": int(w.volume.nbytes + cams21.nbytes),
+                "d2h_bytes_per_step": int(n_my * img * 4),
+                "path": "RenderVolumeProjectionsCUDA, pinned host buffers"},
+        "gpu_launches": args.steps,  # one render launch per step (all views)
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                     "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
+                     "samples_per_step": samples_step, "flops_per_sample": FLOPS_PER_SAMPLE,
+                     "fp64_fallback_fraction": fp64 / max(samples, 1),
+                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    scene.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

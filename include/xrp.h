@@ -1,0 +1,185 @@
+/*
+ * xrp.h -- C ABI of libcuda_render.so, the GB300 (sm_103a) projection engine.
+ *
+ * The library is a drop-in for the dlopen'd native library of
+ * igrega348/xray_projection_render: the Go loader (cuda_backend.go:27-43)
+ * resolves exactly three symbols, declared first below with the signatures of
+ * the reference header (cuda_backend.h).  The remaining entry points are
+ * additions that give the same loader access to every object type,
+ * deformation and integrator of the reference's CPU path.
+ *
+ * Conventions shared by every entry point:
+ *   - return 0 on success and a positive code on failure; the codes of the
+ *     reference functions keep their meaning (1 null pointer, 2 bad sizes,
+ *     3-8 device allocation / copy / launch failures), and xrp_last_error()
+ *     returns a message for the calling thread;
+ *   - calls are synchronous unless they take a stream; host buffers belong to
+ *     the caller; the library never frees caller memory;
+ *   - transmittance images are float32, laid out [view][i][j] with i the
+ *     horizontal and j the vertical pixel index, exactly as the reference's
+ *     img[i][j] (main.go:460-470) and out_images (cuda_backend.h:96-97).
+ */
+#ifndef XRP_H
+#define XRP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define XRP_API __attribute__((visibility("default")))
+#else
+#define XRP_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* Reference ABI (cuda_backend.h), exported verbatim                         */
+/* ------------------------------------------------------------------------- */
+
+/* cuda_backend.h:22-27 */
+typedef struct {
+    float p0[3];
+    float p1[3];
+    float radius;
+    float rho;
+} CylinderParams;
+
+/* cuda_backend.h:78-83: eye, row-major camera-to-world matrix, fov, R. */
+typedef struct {
+    float eye[3];
+    float view[16];
+    float fov_y;
+    float R;
+} XRayCameraParams;
+
+/*
+ * Replaces RenderVolumeProjectionsCUDA (cuda_backend.h:101-112,
+ * cuda_backend.cu:82-203).  Renders num_cameras projections of a voxel grid
+ * stored [z][x][y] (idx = k*nx*ny + i*ny + j).  Unlike the reference GPU
+ * kernel, the result follows the reference CPU semantics exactly
+ * (VoxelGrid.Density with the (N-1) lattice, objects.go:789-855, and
+ * integrate_along_ray, main.go:144-154) evaluated on these FP32 inputs.
+ * Codes: 1 null pointer; 2 bad sizes or ds <= 0 / not finite; 3 device
+ * allocation; 4 volume upload; 5 table upload; 6 output allocation;
+ * 7 kernel failure; 8 copy back.
+ */
+XRP_API int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
+                                const XRayCameraParams* cameras, int num_cameras, int image_res,
+                                float ds, float flat_field, float* out_images);
+
+/*
+ * Replaces AssembleVoxelGridCUDA (cuda_backend.h:33-39, cuda_backend.cu:208-292):
+ * brute-force cylinder voxelizer, out[k*res*res + i*res + j].
+ */
+XRP_API int AssembleVoxelGridCUDA(const CylinderParams* cylinders, int num_cylinders, int res,
+                          float density_multiplier, float* out_volume);
+
+/*
+ * Replaces AssembleVoxelGridSpatialCUDA (cuda_backend.h:58-68,
+ * cuda_backend.cu:297-417): the same voxelizer with CSR cell lists.
+ */
+XRP_API int AssembleVoxelGridSpatialCUDA(const CylinderParams* cylinders, int num_cylinders, int res,
+                                 float density_multiplier, int grid_dim, const int* cell_offsets,
+                                 const int* cyl_indices, int num_cyl_indices, float* out_volume);
+
+/* ------------------------------------------------------------------------- */
+/* Additions                                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* Message for the last failure on the calling thread ("" if none).  No
+ * counterpart in the reference library; the Go shim keeps its own buffer
+ * (cuda_backend.go:22-25). */
+XRP_API const char* xrp_last_error(void);
+
+/* Library version, 100*major + minor. */
+XRP_API int xrp_version(void);
+
+/* One camera, FP64, as computeCameraFromAngles returns it (main.go:226-239):
+ * eye and the column-major (mathgl layout) camera-to-world matrix. */
+typedef struct {
+    double eye[3];
+    double camera[16];
+    double fov_deg;
+} xrp_camera;
+
+/* computeCameraFromAngles for n (azimuthal, polar) pairs in degrees
+ * (main.go:226-239; the angle lists of main.go:242-257, 782-809). */
+XRP_API int xrp_cameras_from_angles(const double* az_polar_deg, int n, double R, double fov_deg,
+                            xrp_camera* out);
+
+enum { XRP_INTEGRATE_SIMPLE = 0, XRP_INTEGRATE_HIERARCHICAL = 1 };
+enum { XRP_FLAG_STATS = 1 };
+
+/* Per-call options: the globals and flags of the reference CLI
+ * (main.go:37-41, 683-707, 725-729). */
+typedef struct {
+    int resolution;            /* image side in pixels */
+    int integration;           /* XRP_INTEGRATE_* (main.go:811-819) */
+    double ds;                 /* step (> 0); DS for the hierarchical integrator */
+    double R;                  /* camera distance; samples span [R-1.74, R+1.74] */
+    double flat_field;         /* added to the optical depth (main.go:146) */
+    double density_multiplier; /* main.go:139 */
+    int flags;                 /* XRP_FLAG_* */
+    int reserved;
+} xrp_render_opts;
+
+typedef struct xrp_scene xrp_scene;
+
+/* A caller-provided voxel grid for {"type":"voxel_grid","volume":k} entries:
+ * FP32 values [z][x][y]; `data` is a host pointer, or a device pointer when
+ * `on_device` is 1 (then it must stay valid while the scene lives). */
+typedef struct {
+    const float* data;
+    int nx, ny, nz;
+    int on_device;
+} xrp_volume_desc;
+
+/*
+ * Loads a scene from the reference's JSON object schema (objects.go:658-689:
+ * sphere, cube, box, cylinder, parallelepiped, gyroid, object_collection,
+ * tessellated_obj_coll, voxel_grid from a .raw path) and an optional
+ * deformation map (deformations.go:308-343; NULL or "" for none).  The object
+ * tree is flattened once and kept on the current device until
+ * xrp_scene_destroy.  Codes: 1 null pointer, 2 schema error (see
+ * xrp_last_error), 3 device allocation, 4 upload.
+ */
+XRP_API int xrp_scene_create(const char* object_json, const char* deformation_json,
+                     const xrp_volume_desc* volumes, int num_volumes, xrp_scene** out);
+XRP_API void xrp_scene_destroy(xrp_scene* scene);
+
+/* Support box of the scene (where density may be non-zero), world units. */
+XRP_API int xrp_scene_support(const xrp_scene* scene, double lo[3], double hi[3]);
+
+/*
+ * Renders `num_views` cameras into host memory `out` (num_views*res*res
+ * float32).  Same results as the reference CPU path (main.go:429-471) for the
+ * same inputs; runs on the calling thread's current device and returns when
+ * the images are in `out`.
+ */
+XRP_API int xrp_render(xrp_scene* scene, const xrp_camera* views, int num_views, const xrp_render_opts* opts,
+               float* out);
+
+/*
+ * As xrp_render, but `out_device` is device memory and the work is queued on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream); returns
+ * after queuing.  The scene and the cameras must not change until the stream
+ * has passed this call.
+ */
+XRP_API int xrp_render_device(xrp_scene* scene, const xrp_camera* views, int num_views,
+                      const xrp_render_opts* opts, float* out_device, void* stream);
+
+/* Counters of the last call on this thread that set XRP_FLAG_STATS:
+ * samples evaluated and samples re-evaluated in FP64. */
+XRP_API int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples);
+
+/* Frees the device buffers the library caches between calls. */
+XRP_API void xrp_release_cache(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XRP_H */

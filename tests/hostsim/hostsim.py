@@ -1,0 +1,76 @@
+"""Loader for the CPU build of the engine's per-pixel code (test harness only).
+
+The engine's device code (xray_projection_render_gb300/csrc/xrp_device.h) is
+host+device; compiled here with g++ it lets the tests check the guard-band
+decisions, the flattened scene and the lattices against the FP64 oracle on a
+machine without a GPU.  The product never loads this library.
+"""
+import ctypes
+import json
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+CSRC = os.path.join(ROOT, "xray_projection_render_gb300", "csrc")
+LIB = os.path.join(HERE, "_build", "libxrp_hostsim.so")
+_lib = None
+
+
+def build():
+    srcs = [os.path.join(HERE, "xrp_hostsim.cpp"), os.path.join(CSRC, "xrp_scene.cpp")]
+    deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    tmp = LIB + f".tmp{os.getpid()}"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+                    "-fno-fast-math", "-pthread", "-I", os.path.join(ROOT, "include"), *srcs,
+                    "-o", tmp], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(build())
+        P, I, D, L_ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_long
+        L.hs_render.restype = I
+        L.hs_render.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, I, I, I, P, I, I, I, D, D, D,
+                                D, P, P, I, P, L_, I, ctypes.c_char_p, I]
+        _lib = L
+    return _lib
+
+
+def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integration="simple",
+           flat_field=0.0, density_multiplier=1.0, rays=None, nthreads=None, force_general=False):
+    """cams: array (n, 20) = eye(3), column-major camera(16), fov."""
+    cams = np.ascontiguousarray(cams, dtype=np.float64).reshape(-1, 20)
+    n = cams.shape[0]
+    vol = None
+    nx = ny = nz = 0
+    if volume is not None:
+        vol = np.ascontiguousarray(volume, dtype=np.float32)
+        nz, nx, ny = vol.shape
+    if rays is not None:
+        rays = np.ascontiguousarray(rays, dtype=np.int32).reshape(-1, 3)
+        out = np.zeros(rays.shape[0], dtype=np.float32)
+    else:
+        out = np.zeros((n, res, res), dtype=np.float32)
+    stats = np.zeros(2, dtype=np.uint64)
+    err = ctypes.create_string_buffer(512)
+    rc = lib().hs_render(json.dumps(obj).encode(), json.dumps(deformation).encode()
+                         if deformation else None,
+                         vol.ctypes.data if vol is not None else None, nx, ny, nz,
+                         cams.ctypes.data, n, res, 1 if integration == "hierarchical" else 0,
+                         ds, R, flat_field, density_multiplier, out.ctypes.data, stats.ctypes.data,
+                         nthreads or os.cpu_count() or 1,
+                         rays.ctypes.data if rays is not None else None,
+                         rays.shape[0] if rays is not None else 0, 1 if force_general else 0,
+                         err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return out, stats

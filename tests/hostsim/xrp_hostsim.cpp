@@ -1,0 +1,107 @@
+// xrp_hostsim.cpp -- TEST HARNESS ONLY: runs the engine's per-pixel code
+// (xrp_device.h) on CPU threads so that its guard-band logic, flattening and
+// lattices can be checked against the FP64 oracle without a GPU.  The product
+// never loads this library; on the GPU the same code runs in xrp_engine.cu.
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../../xray_projection_render_gb300/csrc/xrp_device.h"
+#include "../../xray_projection_render_gb300/csrc/xrp_scene.h"
+
+using namespace xrp;
+
+extern "C" __attribute__((visibility("default"))) int hs_render(
+    const char* obj_json, const char* def_json, const float* vol, int nx, int ny, int nz,
+    const double* cams, int ncams, int res, int integration, double ds, double R, double ff,
+    double dm, float* out, unsigned long long* stats, int nthreads, const int* rays, long nrays,
+    int force_general, char* err, int errlen) {
+    try {
+        std::vector<HVolume> ext;
+        if (vol) {
+            HVolume v;
+            v.nx = nx;
+            v.ny = ny;
+            v.nz = nz;
+            v.data.assign(vol, vol + (size_t)nx * ny * nz);
+            ext.push_back(v);
+        }
+        HostScene hs = load_scene(obj_json, def_json, ext);
+        std::vector<ViewDev> views(ncams);
+        double fov_max = 0;
+        for (int c = 0; c < ncams; c++) {
+            const double* p = cams + 20 * c;
+            view_from_camera(p, p + 3, p[19], views[c]);
+            fov_max = std::max(fov_max, std::fabs(p[19]));
+        }
+        HostPrepared hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max);
+        for (size_t k = 0; k < hp.vols.size(); k++) {
+            hp.vols[k].data = hs.vols[k].data.data();
+            hp.vols[k].data64 = hs.vols[k].data64.empty() ? nullptr : hs.vols[k].data64.data();
+        }
+        SceneDev S = hp.S;
+        S.nodes = hp.fs.nodes.data();
+        S.nodes64 = hp.fs.nodes64.data();
+        S.child = hp.fs.child.data();
+        S.cells = hp.fs.cells.data();
+        S.items = hp.fs.items.data();
+        S.defs = hp.fs.defs.data();
+        S.vols = hp.vols.data();
+        Lattice L = hp.hl.hdr;
+        L.s64 = hp.hl.s64.data();
+        L.t32 = hp.hl.t32.data();
+        L.fstart = hp.hl.fstart.data();
+        L.f64 = hp.hl.f64.data();
+        L.ft32 = hp.hl.ft32.data();
+        RenderParams P = hp.P;
+        P.nviews = ncams;
+        P.xs = hp.xs.data();
+        bool vf = hp.volume_fast && !force_general;
+        long total = rays ? nrays : (long)ncams * res * res;
+        std::vector<unsigned long long> s0(nthreads, 0), s1(nthreads, 0);
+        auto work = [&](int t) {
+            for (long q = t; q < total; q += nthreads) {
+                int v, i, j;
+                if (rays) {
+                    v = rays[3 * q];
+                    i = rays[3 * q + 1];
+                    j = rays[3 * q + 2];
+                } else {
+                    v = (int)(q / ((long)res * res));
+                    i = (int)((q / res) % res);
+                    j = (int)(q % res);
+                }
+                RayStats st{0, 0};
+                float val;
+                bool hier = integration == 1;
+                if (hier)
+                    val = vf ? render_pixel<true, true>(S, L, P, views[v], i, j, st)
+                             : render_pixel<true, false>(S, L, P, views[v], i, j, st);
+                else
+                    val = vf ? render_pixel<false, true>(S, L, P, views[v], i, j, st)
+                             : render_pixel<false, false>(S, L, P, views[v], i, j, st);
+                out[q] = val;
+                s0[t] += st.samples;
+                s1[t] += st.fallbacks;
+            }
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nthreads; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto& x : th) x.join();
+        if (stats) {
+            stats[0] = stats[1] = 0;
+            for (int t = 0; t < nthreads; t++) {
+                stats[0] += s0[t];
+                stats[1] += s1[t];
+            }
+        }
+        return 0;
+    } catch (const std::exception& ex) {
+        if (err && errlen > 0) {
+            strncpy(err, ex.what(), errlen - 1);
+            err[errlen - 1] = 0;
+        }
+        return 2;
+    }
+}

@@ -1,0 +1,14 @@
+"""GB300-native (sm_103a) engine for the per-pixel X-ray projection line
+integral of igrega348/xray_projection_render.
+
+The engine is the C-ABI library ``libcuda_render.so`` (include/xrp.h), a
+drop-in for the reference's dlopen'd GPU library; this package holds its
+CUDA/C++ sources (``csrc/``), its build recipe (``build.py``), a ctypes
+front end (``engine.py``) and the seeded synthetic workloads
+(``workloads.py``).
+"""
+from .engine import (Scene, assemble_voxel_grid, camera_arrays, cameras_from_angles,
+                     release_cache, render, render_volume_projections, xray_camera_params)
+
+__all__ = ["Scene", "render", "render_volume_projections", "assemble_voxel_grid",
+           "cameras_from_angles", "camera_arrays", "xray_camera_params", "release_cache"]

@@ -1,0 +1,90 @@
+"""Build recipe for libcuda_render.so (sm_103a) -- no cmake, two translation units.
+
+    python -m xray_projection_render_gb300.build
+
+compiles ``csrc/xrp_scene.cpp`` with g++ and ``csrc/xrp_engine.cu`` with nvcc for
+``sm_103a`` in parallel, then links ``libcuda_render.so`` next to this file (the
+name the reference's Go loader looks for, cuda_backend.go:103-114).  Host
+floating point is built with contraction off so the FP64 camera and scene
+arithmetic rounds every operation, as the reference does.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libcuda_render.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
+            if f.endswith((".cu", ".cpp", ".h"))] + [os.path.join(INCLUDE, "xrp.h")]
+
+
+def _stale(target):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in _sources() + [__file__])
+
+
+def _run(cmd, verbose):
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout, r.stderr, flush=True)
+    return r
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    """Compile the engine for sm_103a and return the path of the shared library."""
+    if not force and not ptxas_info and not _stale(LIB):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    common_host = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fvisibility=hidden"]
+    o_scene = os.path.join(BUILD, "xrp_scene.o")
+    o_engine = os.path.join(BUILD, "xrp_engine.o")
+    cmd_scene = ["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, "-c",
+                 os.path.join(CSRC, "xrp_scene.cpp"), "-o", o_scene]
+    cmd_engine = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler",
+                  ",".join(common_host), "-I", INCLUDE, "-c", os.path.join(CSRC, "xrp_engine.cu"),
+                  "-o", o_engine]
+    if ptxas_info:
+        cmd_engine.insert(1, "-Xptxas=-v")
+    with ThreadPoolExecutor(2) as ex:
+        futs = [ex.submit(_run, cmd_scene, verbose), ex.submit(_run, cmd_engine, verbose)]
+        results = [f.result() for f in futs]
+    tmp = LIB + f".tmp{os.getpid()}"
+    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, o_engine, o_scene, "-lpthread"],
+         verbose)
+    os.replace(tmp, LIB)
+    if ptxas_info:
+        return results[1].stderr
+    return LIB
+
+
+if __name__ == "__main__":
+    info = "--ptxas" in sys.argv
+    out = build(force=True, verbose="-v" in sys.argv, ptxas_info=info)
+    print(out)

@@ -1,0 +1,922 @@
+// xrp_device.h -- scene image and per-sample / per-ray evaluation, shared by
+// the CUDA kernels and (for logic tests only) a host build.
+//
+// Two evaluators live here:
+//   * an FP32 evaluator with guard bands: every discontinuous predicate of the
+//     reference (strict `<` on a sphere, inclusive bounds of a unit cell, the
+//     floor of a tessellation fold, ...) is decided in FP32 only when the FP32
+//     margin is farther from the decision boundary than a precomputed error
+//     bound; otherwise it reports "uncertain" (NaN);
+//   * an FP64 evaluator that repeats the reference's arithmetic operation by
+//     operation (no contraction: __dmul_rn/__dadd_rn on the device), used for
+//     the uncertain samples only.
+// The reference semantics restated here are objects/objects.go:63-72 (sphere),
+// 171-179 (box), 247-255 (parallelepiped), 334-350 (cylinder), 422-438
+// (collection), 458-464 (unit cell), 568-582 (tessellation), 789-855 (voxel
+// grid), 1014-1032 (gyroid); deformations/deformations.go:29-38, 87-92,
+// 136-141, 173-175, 210-222, 269-274; main.go:123-199 (density, deform and
+// both integrators).
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define XRP_HD __host__ __device__ __forceinline__
+#define XRP_HDN static __host__ __device__ __noinline__
+#else
+#define XRP_HD inline
+#define XRP_HDN static
+#endif
+
+namespace xrp {
+
+// ---------------------------------------------------------------------------
+// exact FP64 operations (one rounding each, never fused)
+// ---------------------------------------------------------------------------
+#if defined(__CUDA_ARCH__)
+XRP_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+XRP_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
+XRP_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+XRP_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+XRP_HD double dsqrt(double a) { return __dsqrt_rn(a); }
+XRP_HD float f_exp(float x) { return __expf(x); }
+XRP_HD float f_rcp(float x) { return __frcp_rn(x); }
+#else
+XRP_HD double dadd(double a, double b) { return a + b; }
+XRP_HD double dsub(double a, double b) { return a - b; }
+XRP_HD double dmul(double a, double b) { return a * b; }
+XRP_HD double ddiv(double a, double b) { return a / b; }
+XRP_HD double dsqrt(double a) { return sqrt(a); }
+XRP_HD float f_exp(float x) { return expf(x); }
+XRP_HD float f_rcp(float x) { return 1.0f / x; }
+#endif
+
+XRP_HD float xnan() { return __builtin_nanf(""); }
+XRP_HD int32_t f2i(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_int(f);
+#else
+    int32_t i;
+    __builtin_memcpy(&i, &f, 4);
+    return i;
+#endif
+}
+XRP_HD bool isunc(float r) { return r != r; }
+
+// sin and cos of one argument: Cody-Waite reduction to [-pi, pi] with a
+// two-term 2*pi, then the SFU approximations (device) or libm (host).  The
+// error of the reduction and of the approximations is folded into the gyroid
+// guard band on the host side.
+XRP_HD void f_sincos(float x, float* s, float* c) {
+    const float inv2pi = 0.159154943091895f;
+    const float twopi_hi = 6.28318548202514648f;      // float(2*pi)
+    const float twopi_lo = -1.7484555314695172e-07f;  // 2*pi - twopi_hi
+    float k = rintf(x * inv2pi);
+    float r = fmaf(-k, twopi_hi, x);
+    r = fmaf(-k, twopi_lo, r);
+#if defined(__CUDA_ARCH__)
+    __sincosf(r, s, c);
+#else
+    *s = sinf(r);
+    *c = cosf(r);
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// scene image
+// ---------------------------------------------------------------------------
+enum NodeType : int32_t {
+    N_SPHERE = 1,
+    N_BOX = 2,
+    N_CYL = 3,
+    N_PPD = 4,
+    N_GYROID = 5,
+    N_COLL = 6,
+    N_TESS = 7,
+    N_VOXEL = 8,
+};
+
+enum CollFlags : int32_t {
+    C_GREEDY = 1,     // GreedyDensEval
+    C_EXACT_SUM = 2,  // every partial sum of child densities is exact in FP32
+    C_ACCEL = 4,      // per-cell candidate lists are present
+    C_CLIP = 8,       // clip the sum to [0, 1] (every ObjectCollection)
+};
+
+// Leaf parameter slots (Node.f).  RHO and BAND slots are shared by leaves.
+enum : int { F_RHO = 27, F_BAND = 26, F_BAND2 = 25 };
+
+struct Node {
+    int32_t type;
+    int32_t a;      // COLL: first slot in the child list; TESS: unit-cell collection node; VOXEL: volume id
+    int32_t b;      // COLL: number of children
+    int32_t flags;  // COLL: CollFlags | (accel grid dim << 16) | (homogeneous leaf type << 8)
+    float f[28];
+};
+static_assert(sizeof(Node) == 128, "Node must stay 128 bytes");
+
+struct Node64 {
+    double d[16];
+};
+
+struct Volume {
+    const float* data;     // [z][x][y], FP32
+    const double* data64;  // exact values when FP32 cannot hold them, else null
+    int32_t nx, ny, nz;
+    int32_t pad;
+    float scale[3];        // (N-1)/2 per axis
+    float band_w;          // world-space guard band for the inclusive [-1,1] test
+};
+
+enum DefType : int32_t { D_GAUSSIAN = 1, D_LINEAR, D_RIGID, D_SIGMOID, D_AFFINE };
+
+struct DefStep {
+    int32_t type;
+    int32_t axis;  // sigmoid
+    int32_t pad[2];
+    float f[12];
+    double d[12];
+};
+
+// Everything a kernel needs about one scene (passed by value).
+struct SceneDev {
+    const Node* nodes;
+    const Node64* nodes64;
+    const int32_t* child;   // child node ids of collections
+    const int32_t* cells;   // accel: per collection, (G^3 + 1) offsets into items
+    const int32_t* items;   // accel: child slots (positions within the collection)
+    const Volume* vols;
+    const DefStep* defs;
+    int32_t root;
+    int32_t ndefs;
+    int32_t hier_zero_guard;  // 1: flag near-zero voxel values (hierarchical zero test)
+    int32_t pad;
+    float sup_lo[3], sup_hi[3];  // dilated support box (FP32, world)
+};
+
+// One view (camera) of a batch, prepared on the host.
+struct ViewDev {
+    double eye[3];
+    double m[16];       // camera-to-world, column-major (mathgl layout)
+    double inv_w;       // 1/m[15] when the last row is (0,0,0,w); else 0
+    double f;           // focal length 1/tan(fov/2)
+    int32_t general_w;  // 1: divide by the per-pixel w
+    int32_t pad[3];
+};
+
+// Sample lattice of one integrator run (same for every ray of a batch).
+struct Lattice {
+    const double* s64;    // simple: s_k; hierarchical: coarse right ends r_k
+    const float* t32;     // float(s_k - s_c)
+    const int32_t* fstart;  // hierarchical: fine sample range of coarse k
+    const double* f64;    // hierarchical: fine positions
+    const float* ft32;    // hierarchical: float(fine - s_c)
+    int32_t K;            // number of (coarse) samples
+    int32_t hierarchical;
+    double s_c;           // reference point of the FP32 offsets
+    double smin;
+    double ds;            // simple: ds; hierarchical: DS
+    double ds_fine;       // hierarchical: DS/10
+    float ds32, dsf32;    // float(ds), float(ds_fine)
+    float t_first;        // float(s_0 - s_c)
+    float inv_ds;         // 1/ds (FP32, for clipping)
+};
+
+struct RenderParams {
+    int32_t res;
+    int32_t nviews;
+    float flat_field;
+    float density_multiplier;
+    const double* xs;     // pixel coordinate table i/(res/2)-1, length res
+};
+
+// ---------------------------------------------------------------------------
+// FP32 guarded evaluation
+// ---------------------------------------------------------------------------
+// Returns the density (pre-multiplier) or NaN when a predicate is too close
+// to its decision boundary for FP32 to decide.
+
+XRP_HD float sphere32(const float* f, float x, float y, float z) {
+    float dx = x - f[0], dy = y - f[1], dz = z - f[2];
+    float m = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - f[3];
+    if (m < -f[F_BAND]) return f[F_RHO];
+    if (m > f[F_BAND]) return 0.0f;
+    return xnan();
+}
+
+XRP_HD float box32(const float* f, float x, float y, float z) {
+    float mx = f[3] - fabsf(x - f[0]);
+    float my = f[4] - fabsf(y - f[1]);
+    float mz = f[5] - fabsf(z - f[2]);
+    float b = f[F_BAND];
+    float mn = fminf(mx, fminf(my, mz));
+    if (mn > b) return f[F_RHO];
+    if (mn < -b) return 0.0f;
+    return xnan();
+}
+
+XRP_HD float cyl32(const float* f, float x, float y, float z) {
+    float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+    float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
+    float bc = f[F_BAND2];
+    if (c < -bc || c > 1.0f + bc) return 0.0f;
+    float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
+    float m = fmaf(pz, pz, fmaf(py, py, px * px)) - f[7];
+    float bd = f[F_BAND];
+    if (m > bd) return 0.0f;
+    if (m < -bd && c > bc && c < 1.0f - bc) return f[F_RHO];
+    return xnan();
+}
+
+XRP_HD float ppd32(const float* f, float x, float y, float z) {
+    float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+    float qx = fmaf(f[5], wz, fmaf(f[4], wy, f[3] * wx));
+    float qy = fmaf(f[8], wz, fmaf(f[7], wy, f[6] * wx));
+    float qz = fmaf(f[11], wz, fmaf(f[10], wy, f[9] * wx));
+    float b = f[F_BAND];
+    // margin to the strict interval (0, 1) on each axis
+    float mx = fminf(qx, 1.0f - qx), my = fminf(qy, 1.0f - qy), mz = fminf(qz, 1.0f - qz);
+    float mn = fminf(mx, fminf(my, mz));
+    if (mn > b) return f[F_RHO];
+    if (mn < -b) return 0.0f;
+    return xnan();
+}
+
+XRP_HD float gyroid32(const float* f, float x, float y, float z) {
+    float X = (x - f[0]) * f[3], Y = (y - f[1]) * f[3], Z = (z - f[2]) * f[3];
+    float sx, cx, sy, cy, sz, cz;
+    f_sincos(X, &sx, &cx);
+    f_sincos(Y, &sy, &cy);
+    f_sincos(Z, &sz, &cz);
+    float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
+    float m = f[4] - fabsf(g);
+    if (m > f[F_BAND]) return f[F_RHO];
+    if (m < -f[F_BAND]) return 0.0f;
+    return xnan();
+}
+
+XRP_HD float voxel32(const Volume& V, float band_zero, float x, float y, float z, int zero_guard) {
+    float b = V.band_w;
+    float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+    float mx = fmaxf(ax, fmaxf(ay, az));
+    if (mx > 1.0f + b) return 0.0f;
+    if (!(mx < 1.0f - b)) return xnan();  // on the inclusive boundary, or NaN
+    float ux = (x + 1.0f) * V.scale[0];
+    float uy = (y + 1.0f) * V.scale[1];
+    float uz = (z + 1.0f) * V.scale[2];
+    float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    float wx = ux - fx, wy = uy - fy, wz = uz - fz;
+    x0 = x0 < 0 ? 0 : (x0 > V.nx - 1 ? V.nx - 1 : x0);
+    y0 = y0 < 0 ? 0 : (y0 > V.ny - 1 ? V.ny - 1 : y0);
+    z0 = z0 < 0 ? 0 : (z0 > V.nz - 1 ? V.nz - 1 : z0);
+    int x1 = x0 + 1 > V.nx - 1 ? V.nx - 1 : x0 + 1;
+    int y1 = y0 + 1 > V.ny - 1 ? V.ny - 1 : y0 + 1;
+    int z1 = z0 + 1 > V.nz - 1 ? V.nz - 1 : z0 + 1;
+    long NXY = (long)V.nx * V.ny, NY = V.ny;
+    const float* r = V.data;
+    float v000 = r[z0 * NXY + x0 * NY + y0];
+    float v001 = r[z1 * NXY + x0 * NY + y0];
+    float v010 = r[z0 * NXY + x0 * NY + y1];
+    float v011 = r[z1 * NXY + x0 * NY + y1];
+    float v100 = r[z0 * NXY + x1 * NY + y0];
+    float v101 = r[z1 * NXY + x1 * NY + y0];
+    float v110 = r[z0 * NXY + x1 * NY + y1];
+    float v111 = r[z1 * NXY + x1 * NY + y1];
+    float v00 = fmaf(wz, v001 - v000, v000);
+    float v01 = fmaf(wz, v011 - v010, v010);
+    float v10 = fmaf(wz, v101 - v100, v100);
+    float v11 = fmaf(wz, v111 - v110, v110);
+    float v0 = fmaf(wy, v01 - v00, v00);
+    float v1 = fmaf(wy, v11 - v10, v10);
+    float v = fmaf(wx, v1 - v0, v0);
+    if (zero_guard) {
+        // the hierarchical integrator tests density == 0: decide that only
+        // when FP32 and FP64 cannot disagree
+        float amax = fmaxf(fmaxf(fmaxf(fabsf(v000), fabsf(v001)), fmaxf(fabsf(v010), fabsf(v011))),
+                           fmaxf(fmaxf(fabsf(v100), fabsf(v101)), fmaxf(fabsf(v110), fabsf(v111))));
+        if (amax > 0.0f && fabsf(v) <= band_zero * amax) return xnan();
+    }
+    return v;
+}
+
+XRP_HD float leaf32(const Node& n, float x, float y, float z) {
+    switch (n.type) {
+    case N_SPHERE: return sphere32(n.f, x, y, z);
+    case N_BOX: return box32(n.f, x, y, z);
+    case N_CYL: return cyl32(n.f, x, y, z);
+    case N_PPD: return ppd32(n.f, x, y, z);
+    case N_GYROID: return gyroid32(n.f, x, y, z);
+    default: return xnan();
+    }
+}
+
+template <int D>
+XRP_HD float coll32(const SceneDev& S, const Node& c, float x, float y, float z);
+
+// A collection child: leaf, voxel grid or (nested) tessellation.
+template <int D>
+XRP_HD float item32(const SceneDev& S, int id, float x, float y, float z) {
+    const Node& n = S.nodes[id];
+    if (n.type <= N_GYROID) return leaf32(n, x, y, z);
+    if (n.type == N_VOXEL) return voxel32(S.vols[n.a], n.f[0], x, y, z, S.hier_zero_guard);
+    if (n.type == N_TESS) {
+        if constexpr (D > 0) {
+            const float* f = n.f;
+            // outer inclusive bounds (objects.go:570)
+            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
+                             fminf(z - f[4], f[5] - z));
+            if (mo < -f[6]) return 0.0f;
+            if (!(mo > f[6])) return xnan();
+            // fold into the unit cell (objects.go:574-579)
+            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
+            float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
+            float bq = f[23];
+            float fr = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)), fminf(qy - ny, 1.0f - (qy - ny))),
+                             fminf(qz - nz, 1.0f - (qz - nz)));
+            if (!(fr > bq)) return xnan();
+            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
+            // unit-cell inclusive bounds (objects.go:460)
+            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
+                             fminf(fz - f[11], f[12] - fz));
+            if (mu < -f[13]) return 0.0f;
+            if (!(mu > f[13])) return xnan();
+            return coll32<D - 1>(S, S.nodes[n.a], fx, fy, fz);
+        } else {
+            return xnan();
+        }
+    }
+    return xnan();
+}
+
+// ObjectCollection.Density (objects.go:422-438) in FP32.
+template <int D>
+XRP_HD float coll32(const SceneDev& S, const Node& c, float x, float y, float z) {
+    const int32_t* kids = S.child + c.a;
+    int cnt = c.b;
+    const int32_t* list = nullptr;
+    if (c.flags & C_ACCEL) {
+        int G = (c.flags >> 16) & 0xff;
+        int ix = (int)floorf((x - c.f[0]) * c.f[3]);
+        int iy = (int)floorf((y - c.f[1]) * c.f[4]);
+        int iz = (int)floorf((z - c.f[2]) * c.f[5]);
+        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
+        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
+        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
+        int cell_base = f2i(c.f[6]);
+        const int32_t* off = S.cells + cell_base + (iz * G + iy) * G + ix;
+        int s0 = off[0], s1 = off[1];
+        list = S.items + s0;
+        cnt = s1 - s0;
+    }
+    const bool greedy = (c.flags & C_GREEDY) != 0;
+    float sum = 0.0f, sabs = 0.0f;
+    const int homo = (c.flags >> 8) & 0xff;
+    for (int k = 0; k < cnt; k++) {
+        int slot = list ? list[k] : k;
+        const Node& n = S.nodes[kids[slot]];
+        float r;
+        if (homo == N_CYL)
+            r = cyl32(n.f, x, y, z);
+        else if (homo == N_SPHERE)
+            r = sphere32(n.f, x, y, z);
+        else
+            r = item32<D>(S, kids[slot], x, y, z);
+        if (isunc(r)) return r;
+        if (greedy && r > 0.0f) return r;
+        sum += r;
+        sabs += fabsf(r);
+    }
+    if (!(c.flags & C_EXACT_SUM) && sabs > 0.0f && fabsf(sum) <= c.f[7] * sabs) return xnan();
+    if (c.flags & C_CLIP) sum = fminf(fmaxf(sum, 0.0f), 1.0f);
+    return sum;
+}
+
+// deform() (main.go:123-133) in FP32.
+XRP_HD void deform32(const SceneDev& S, float& x, float& y, float& z) {
+    for (int i = 0; i < S.ndefs; i++) {
+        const DefStep& d = S.defs[i];
+        const float* a = d.f;
+        switch (d.type) {
+        case D_GAUSSIAN: {
+            float x0 = x - a[6], y0 = y - a[7], z0 = z - a[8];
+            float r2 = fmaf(z0, z0, fmaf(y0, y0, x0 * x0));
+            float dx = a[0] * f_exp(-r2 * a[3]);
+            float dy = a[1] * f_exp(-r2 * a[4]);
+            float dz = a[2] * f_exp(-r2 * a[5]);
+            x += dx; y += dy; z += dz;
+            break;
+        }
+        case D_LINEAR: {
+            float nx = fmaf(a[4], z, fmaf(a[5], y, fmaf(a[0], x, x)));
+            float ny = fmaf(a[3], z, fmaf(a[1], y, fmaf(a[5], x, y)));
+            float nz = fmaf(a[2], z, fmaf(a[3], y, fmaf(a[4], x, z)));
+            x = nx; y = ny; z = nz;
+            break;
+        }
+        case D_RIGID: x += a[0]; y += a[1]; z += a[2]; break;
+        case D_SIGMOID: {
+            float* p = d.axis == 0 ? &x : (d.axis == 1 ? &y : &z);
+            float e = f_exp(-(*p - a[1]) * a[2]);
+            *p += a[0] * f_rcp(1.0f + e);
+            break;
+        }
+        case D_AFFINE: {
+            float nx = fmaf(a[2], z, fmaf(a[1], y, a[0] * x));
+            float ny = fmaf(a[5], z, fmaf(a[4], y, a[3] * x));
+            float nz = fmaf(a[8], z, fmaf(a[7], y, a[6] * x));
+            x = nx; y = ny; z = nz;
+            break;
+        }
+        default: break;
+        }
+    }
+}
+
+constexpr int kMaxDepth = 3;  // nested tessellations supported by the evaluators
+
+XRP_HD float density32(const SceneDev& S, float x, float y, float z) {
+    if (S.ndefs) deform32(S, x, y, z);
+    const Node& r = S.nodes[S.root];
+    if (r.type <= N_GYROID) return leaf32(r, x, y, z);
+    if (r.type == N_COLL) return coll32<kMaxDepth>(S, r, x, y, z);
+    return item32<kMaxDepth>(S, S.root, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 exact evaluation (reference arithmetic, operation by operation)
+// ---------------------------------------------------------------------------
+
+XRP_HD double sphere64(const double* d, double x, double y, double z) {
+    x = dsub(x, d[0]);
+    y = dsub(y, d[1]);
+    z = dsub(z, d[2]);
+    double r_2 = dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z));
+    if (r_2 < dmul(d[3], d[3])) return d[4];
+    return 0.0;
+}
+
+XRP_HD double box64(const double* d, double x, double y, double z) {
+    x = fabs(dsub(x, d[0]));
+    y = fabs(dsub(y, d[1]));
+    z = fabs(dsub(z, d[2]));
+    if (x < dmul(0.5, d[3]) && y < dmul(0.5, d[4]) && z < dmul(0.5, d[5])) return d[6];
+    return 0.0;
+}
+
+XRP_HD double ppd64(const double* d, double x, double y, double z) {
+    double wx = dsub(x, d[0]), wy = dsub(y, d[1]), wz = dsub(z, d[2]);
+    const double* m = &d[3];  // column-major
+    double qx = dadd(dadd(dmul(m[0], wx), dmul(m[3], wy)), dmul(m[6], wz));
+    double qy = dadd(dadd(dmul(m[1], wx), dmul(m[4], wy)), dmul(m[7], wz));
+    double qz = dadd(dadd(dmul(m[2], wx), dmul(m[5], wy)), dmul(m[8], wz));
+    if (qx > 0.0 && qx < 1.0 && qy > 0.0 && qy < 1.0 && qz > 0.0 && qz < 1.0) return d[12];
+    return 0.0;
+}
+
+XRP_HD double cyl64(const double* d, double x, double y, double z) {
+    double vx = dsub(d[3], d[0]), vy = dsub(d[4], d[1]), vz = dsub(d[5], d[2]);
+    double wx = dsub(x, d[0]), wy = dsub(y, d[1]), wz = dsub(z, d[2]);
+    double wv = dadd(dadd(dmul(wx, vx), dmul(wy, vy)), dmul(wz, vz));
+    double vv = dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz));
+    double c = ddiv(wv, vv);
+    if (c < 0.0 || c > 1.0) return 0.0;
+    double dx = dsub(wx, dmul(vx, c)), dy = dsub(wy, dmul(vy, c)), dz = dsub(wz, dmul(vz, c));
+    double dd = dsqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)));
+    if (dd < d[6]) return d[7];
+    return 0.0;
+}
+
+XRP_HD double gyroid64(const double* d, double x, double y, double z) {
+    x = ddiv(dsub(x, d[0]), d[3]);
+    y = ddiv(dsub(y, d[1]), d[3]);
+    z = ddiv(dsub(z, d[2]), d[3]);
+    double v = dadd(dadd(dmul(sin(x), cos(y)), dmul(sin(y), cos(z))), dmul(sin(z), cos(x)));
+    if (fabs(v) < d[4]) return d[5];
+    return 0.0;
+}
+
+XRP_HD double voxel64(const Volume& V, double x, double y, double z) {
+    if (x < -1 || x > 1 || y < -1 || y > 1 || z < -1 || z > 1) return 0.0;
+    x = ddiv(dadd(x, 1.0), 2.0);
+    y = ddiv(dadd(y, 1.0), 2.0);
+    z = ddiv(dadd(z, 1.0), 2.0);
+    x = dmul(x, (double)(V.nx - 1));
+    y = dmul(y, (double)(V.ny - 1));
+    z = dmul(z, (double)(V.nz - 1));
+    int x0 = (int)floor(x), y0 = (int)floor(y), z0 = (int)floor(z);
+    int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+    if (x0 < 0) x0 = 0;
+    if (y0 < 0) y0 = 0;
+    if (z0 < 0) z0 = 0;
+    if (x1 >= V.nx) x1 = V.nx - 1;
+    if (y1 >= V.ny) y1 = V.ny - 1;
+    if (z1 >= V.nz) z1 = V.nz - 1;
+    // indices stay in range for inputs inside [-1,1]; clamp the upper side
+    // too so that no input can address outside the grid
+    if (x0 > V.nx - 1) x0 = V.nx - 1;
+    if (y0 > V.ny - 1) y0 = V.ny - 1;
+    if (z0 > V.nz - 1) z0 = V.nz - 1;
+    double wx = dsub(x, (double)x0), wy = dsub(y, (double)y0), wz = dsub(z, (double)z0);
+    long NXY = (long)V.nx * V.ny, NY = V.ny;
+    long i000 = z0 * NXY + x0 * NY + y0, i001 = z1 * NXY + x0 * NY + y0;
+    long i010 = z0 * NXY + x0 * NY + y1, i011 = z1 * NXY + x0 * NY + y1;
+    long i100 = z0 * NXY + x1 * NY + y0, i101 = z1 * NXY + x1 * NY + y0;
+    long i110 = z0 * NXY + x1 * NY + y1, i111 = z1 * NXY + x1 * NY + y1;
+    double v000, v001, v010, v011, v100, v101, v110, v111;
+    if (V.data64) {
+        const double* r = V.data64;
+        v000 = r[i000]; v001 = r[i001]; v010 = r[i010]; v011 = r[i011];
+        v100 = r[i100]; v101 = r[i101]; v110 = r[i110]; v111 = r[i111];
+    } else {
+        const float* r = V.data;
+        v000 = r[i000]; v001 = r[i001]; v010 = r[i010]; v011 = r[i011];
+        v100 = r[i100]; v101 = r[i101]; v110 = r[i110]; v111 = r[i111];
+    }
+    double v00 = dadd(dmul(v000, dsub(1, wz)), dmul(v001, wz));
+    double v01 = dadd(dmul(v010, dsub(1, wz)), dmul(v011, wz));
+    double v10 = dadd(dmul(v100, dsub(1, wz)), dmul(v101, wz));
+    double v11 = dadd(dmul(v110, dsub(1, wz)), dmul(v111, wz));
+    double v0 = dadd(dmul(v00, dsub(1, wy)), dmul(v01, wy));
+    double v1 = dadd(dmul(v10, dsub(1, wy)), dmul(v11, wy));
+    return dadd(dmul(v0, dsub(1, wx)), dmul(v1, wx));
+}
+
+XRP_HD double leaf64(const SceneDev& S, int id, double x, double y, double z) {
+    const double* d = S.nodes64[id].d;
+    switch (S.nodes[id].type) {
+    case N_SPHERE: return sphere64(d, x, y, z);
+    case N_BOX: return box64(d, x, y, z);
+    case N_CYL: return cyl64(d, x, y, z);
+    case N_PPD: return ppd64(d, x, y, z);
+    case N_GYROID: return gyroid64(d, x, y, z);
+    default: return 0.0;
+    }
+}
+
+template <int D>
+XRP_HD double coll64(const SceneDev& S, int id, double x, double y, double z);
+
+template <int D>
+XRP_HD double item64(const SceneDev& S, int id, double x, double y, double z) {
+    const Node& n = S.nodes[id];
+    if (n.type <= N_GYROID) return leaf64(S, id, x, y, z);
+    if (n.type == N_VOXEL) return voxel64(S.vols[n.a], x, y, z);
+    if (n.type == N_TESS) {
+        if constexpr (D > 0) {
+            const double* t = S.nodes64[id].d;
+            if (x < t[0] || x > t[1] || y < t[2] || y > t[3] || z < t[4] || z > t[5]) return 0.0;
+            const double* u = &t[6];
+            double dx = dsub(u[1], u[0]);
+            x = dsub(x, dmul(dx, floor(ddiv(dsub(x, u[0]), dx))));
+            double dy = dsub(u[3], u[2]);
+            y = dsub(y, dmul(dy, floor(ddiv(dsub(y, u[2]), dy))));
+            double dz = dsub(u[5], u[4]);
+            z = dsub(z, dmul(dz, floor(ddiv(dsub(z, u[4]), dz))));
+            if (x < u[0] || x > u[1] || y < u[2] || y > u[3] || z < u[4] || z > u[5]) return 0.0;
+            return coll64<D - 1>(S, n.a, x, y, z);
+        }
+    }
+    return 0.0;
+}
+
+template <int D>
+XRP_HD double coll64(const SceneDev& S, int id, double x, double y, double z) {
+    const Node& c = S.nodes[id];
+    const int32_t* kids = S.child + c.a;
+    const bool greedy = (c.flags & C_GREEDY) != 0;
+    double density = 0.0;
+    for (int k = 0; k < c.b; k++) {
+        double rho = item64<D>(S, kids[k], x, y, z);
+        if (greedy && rho > 0.0) return rho;
+        density = dadd(density, rho);
+    }
+    if (c.flags & C_CLIP) {
+        if (density < 0.0)
+            density = 0.0;
+        else if (density > 1.0)
+            density = 1.0;
+    }
+    return density;
+}
+
+XRP_HD void deform64(const SceneDev& S, double& x, double& y, double& z) {
+    for (int i = 0; i < S.ndefs; i++) {
+        const DefStep& dd = S.defs[i];
+        const double* a = dd.d;
+        switch (dd.type) {
+        case D_GAUSSIAN: {
+            double x0 = dsub(x, a[6]), y0 = dsub(y, a[7]), z0 = dsub(z, a[8]);
+            double r2 = dadd(dadd(dmul(x0, x0), dmul(y0, y0)), dmul(z0, z0));
+            double dx = dmul(a[0], exp(ddiv(-r2, dmul(dmul(2.0, a[3]), a[3]))));
+            double dy = dmul(a[1], exp(ddiv(-r2, dmul(dmul(2.0, a[4]), a[4]))));
+            double dz = dmul(a[2], exp(ddiv(-r2, dmul(dmul(2.0, a[5]), a[5]))));
+            x = dadd(x, dx); y = dadd(y, dy); z = dadd(z, dz);
+            break;
+        }
+        case D_LINEAR: {
+            double nx = dadd(dadd(dadd(x, dmul(a[0], x)), dmul(a[5], y)), dmul(a[4], z));
+            double ny = dadd(dadd(dadd(y, dmul(a[5], x)), dmul(a[1], y)), dmul(a[3], z));
+            double nz = dadd(dadd(dadd(z, dmul(a[4], x)), dmul(a[3], y)), dmul(a[2], z));
+            x = nx; y = ny; z = nz;
+            break;
+        }
+        case D_RIGID: x = dadd(x, a[0]); y = dadd(y, a[1]); z = dadd(z, a[2]); break;
+        case D_SIGMOID: {
+            double* p = dd.axis == 0 ? &x : (dd.axis == 1 ? &y : &z);
+            double e = exp(ddiv(-dsub(*p, a[1]), a[2]));
+            *p = dadd(*p, ddiv(a[0], dadd(1.0, e)));
+            break;
+        }
+        case D_AFFINE: {
+            double nx = dadd(dadd(dmul(a[0], x), dmul(a[1], y)), dmul(a[2], z));
+            double ny = dadd(dadd(dmul(a[3], x), dmul(a[4], y)), dmul(a[5], z));
+            double nz = dadd(dadd(dmul(a[6], x), dmul(a[7], y)), dmul(a[8], z));
+            x = nx; y = ny; z = nz;
+            break;
+        }
+        default: break;
+        }
+    }
+}
+
+// density() without the multiplier (main.go:137-140).
+XRP_HDN double density64(const SceneDev& S, double x, double y, double z) {
+    if (S.ndefs) deform64(S, x, y, z);
+    if (S.nodes[S.root].type == N_COLL) return coll64<kMaxDepth>(S, S.root, x, y, z);
+    return item64<kMaxDepth>(S, S.root, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// per-ray setup and the two integrators
+// ---------------------------------------------------------------------------
+
+struct Ray {
+    double o[3];   // eye
+    double d[3];   // normalised direction, bit-identical to the reference
+    float pc[3];   // float(o + d*s_c)
+    float d32[3];  // float(d)
+};
+
+// main.go:457-465 and the Normalize() at main.go:145 / 160.
+XRP_HD void setup_ray(const ViewDev& V, const RenderParams& P, int i, int j, double s_c, Ray& r) {
+    double v0 = P.xs[i], v1 = P.xs[j], v2 = -V.f;
+    const double* m = V.m;
+    double t0 = dadd(dadd(dadd(dmul(m[0], v0), dmul(m[4], v1)), dmul(m[8], v2)), dmul(m[12], 1.0));
+    double t1 = dadd(dadd(dadd(dmul(m[1], v0), dmul(m[5], v1)), dmul(m[9], v2)), dmul(m[13], 1.0));
+    double t2 = dadd(dadd(dadd(dmul(m[2], v0), dmul(m[6], v1)), dmul(m[10], v2)), dmul(m[14], 1.0));
+    double iw = V.inv_w;
+    if (V.general_w) {
+        double t3 = dadd(dadd(dadd(dmul(m[3], v0), dmul(m[7], v1)), dmul(m[11], v2)), dmul(m[15], 1.0));
+        iw = ddiv(1.0, t3);
+    }
+    double dx = dsub(dmul(t0, iw), V.eye[0]);
+    double dy = dsub(dmul(t1, iw), V.eye[1]);
+    double dz = dsub(dmul(t2, iw), V.eye[2]);
+    double l = ddiv(1.0, dsqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz))));
+    r.d[0] = dmul(dx, l);
+    r.d[1] = dmul(dy, l);
+    r.d[2] = dmul(dz, l);
+    r.o[0] = V.eye[0];
+    r.o[1] = V.eye[1];
+    r.o[2] = V.eye[2];
+    for (int a = 0; a < 3; a++) {
+        r.pc[a] = (float)fma(r.d[a], s_c, r.o[a]);
+        r.d32[a] = (float)r.d[a];
+    }
+}
+
+// FP64 position of sample s exactly as the reference forms it (main.go:148-150).
+XRP_HD double sample64(const SceneDev& S, const Ray& r, double s) {
+    double x = dadd(r.o[0], dmul(r.d[0], s));
+    double y = dadd(r.o[1], dmul(r.d[1], s));
+    double z = dadd(r.o[2], dmul(r.d[2], s));
+    return density64(S, x, y, z);
+}
+
+// Parameter interval [t0, t1] (offsets from s_c) where the ray is inside the
+// dilated support box; t0 > t1 when it misses.
+XRP_HD void clip_ray(const float* lo, const float* hi, const Ray& r, float& t0, float& t1) {
+    t0 = -3.0e38f;
+    t1 = 3.0e38f;
+    for (int a = 0; a < 3; a++) {
+        float dd = r.d32[a];
+        float p = r.pc[a];
+        if (dd != 0.0f) {
+            float inv = 1.0f / dd;
+            float ta = (lo[a] - p) * inv, tb = (hi[a] - p) * inv;
+            t0 = fmaxf(t0, fminf(ta, tb));
+            t1 = fminf(t1, fmaxf(ta, tb));
+        } else if (p < lo[a] || p > hi[a]) {
+            t0 = 1.0f;
+            t1 = -1.0f;
+        }
+    }
+}
+
+struct KahanF {
+    float s = 0.0f, c = 0.0f;
+    XRP_HD void add(float v) {
+        float y = v - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// Index range [k0, k1] of lattice samples that may lie inside the support.
+XRP_HD bool sample_range(const Lattice& L, float t0, float t1, int K, int& k0, int& k1) {
+    if (!(t0 <= t1)) return false;
+    float a = (t0 - L.t_first) * L.inv_ds;
+    float b = (t1 - L.t_first) * L.inv_ds;
+    a = fmaxf(a, -4.0f);
+    b = fminf(b, (float)K + 4.0f);
+    k0 = (int)floorf(a) - 2;
+    k1 = (int)ceilf(b) + 2;
+    if (k0 < 0) k0 = 0;
+    if (k1 > K - 1) k1 = K - 1;
+    return k0 <= k1;
+}
+
+struct RayStats {
+    uint32_t samples;
+    uint32_t fallbacks;
+};
+
+// Samplers: density at lattice offset t (FP32, NaN when uncertain) and the
+// exact FP64 density at reference position s.
+struct SceneSampler {
+    const SceneDev& S;
+    const Ray& r;
+    XRP_HD float f32(float t) const {
+        float x = fmaf(r.d32[0], t, r.pc[0]);
+        float y = fmaf(r.d32[1], t, r.pc[1]);
+        float z = fmaf(r.d32[2], t, r.pc[2]);
+        return density32(S, x, y, z);
+    }
+    XRP_HD double f64(double s) const { return sample64(S, r, s); }
+};
+
+// A scene whose root is a voxel grid (no deformation): samples are formed
+// directly in grid coordinates u = (p + 1) * (N - 1) / 2.
+struct VolRay {
+    float uc[3];  // float((p_c + 1) * scale)
+    float du[3];  // float(d * scale)
+};
+
+XRP_HD void setup_volray(const Volume& V, const Ray& r, double s_c, VolRay& vr) {
+    for (int a = 0; a < 3; a++) {
+        double sc = (double)V.scale[a];
+        vr.uc[a] = (float)((fma(r.d[a], s_c, r.o[a]) + 1.0) * sc);
+        vr.du[a] = (float)(r.d[a] * sc);
+    }
+}
+
+// VoxelGrid.Density in grid coordinates; all dimensions >= 2.
+XRP_HD float vol32(const Volume& V, const float* inv_scale, float band_zero, int zero_guard,
+                   float ux, float uy, float uz) {
+    float nx1 = (float)(V.nx - 1), ny1 = (float)(V.ny - 1), nz1 = (float)(V.nz - 1);
+    // world-space margin to the inclusive [-1, 1] bounds
+    float mx = fminf(ux, nx1 - ux) * inv_scale[0];
+    float my = fminf(uy, ny1 - uy) * inv_scale[1];
+    float mz = fminf(uz, nz1 - uz) * inv_scale[2];
+    float m = fminf(mx, fminf(my, mz));
+    float b = V.band_w;
+    if (m < -b) return 0.0f;
+    if (!(m > b)) return xnan();
+    float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+    int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    float wx = ux - fx, wy = uy - fy, wz = uz - fz;
+    x0 = x0 > V.nx - 2 ? V.nx - 2 : x0;
+    y0 = y0 > V.ny - 2 ? V.ny - 2 : y0;
+    z0 = z0 > V.nz - 2 ? V.nz - 2 : z0;
+    x0 = x0 < 0 ? 0 : x0;
+    y0 = y0 < 0 ? 0 : y0;
+    z0 = z0 < 0 ? 0 : z0;
+    long NY = V.ny, NXY = (long)V.nx * V.ny;
+    const float* p0 = V.data + z0 * NXY + x0 * NY + y0;
+    const float* p1 = p0 + NXY;
+#if defined(__CUDA_ARCH__)
+    float v000 = __ldg(p0), v010 = __ldg(p0 + 1), v100 = __ldg(p0 + NY), v110 = __ldg(p0 + NY + 1);
+    float v001 = __ldg(p1), v011 = __ldg(p1 + 1), v101 = __ldg(p1 + NY), v111 = __ldg(p1 + NY + 1);
+#else
+    float v000 = p0[0], v010 = p0[1], v100 = p0[NY], v110 = p0[NY + 1];
+    float v001 = p1[0], v011 = p1[1], v101 = p1[NY], v111 = p1[NY + 1];
+#endif
+    float v00 = fmaf(wz, v001 - v000, v000);
+    float v01 = fmaf(wz, v011 - v010, v010);
+    float v10 = fmaf(wz, v101 - v100, v100);
+    float v11 = fmaf(wz, v111 - v110, v110);
+    float v0 = fmaf(wy, v01 - v00, v00);
+    float v1 = fmaf(wy, v11 - v10, v10);
+    float v = fmaf(wx, v1 - v0, v0);
+    if (zero_guard) {
+        float amax = fmaxf(fmaxf(fmaxf(fabsf(v000), fabsf(v001)), fmaxf(fabsf(v010), fabsf(v011))),
+                           fmaxf(fmaxf(fabsf(v100), fabsf(v101)), fmaxf(fabsf(v110), fabsf(v111))));
+        if (amax > 0.0f && fabsf(v) <= band_zero * amax) return xnan();
+    }
+    return v;
+}
+
+struct VolumeSampler {
+    const SceneDev& S;
+    const Volume& V;
+    const Ray& r;
+    const VolRay& vr;
+    float inv_scale[3];
+    float band_zero;
+    XRP_HD float f32(float t) const {
+        return vol32(V, inv_scale, band_zero, S.hier_zero_guard, fmaf(vr.du[0], t, vr.uc[0]),
+                     fmaf(vr.du[1], t, vr.uc[1]), fmaf(vr.du[2], t, vr.uc[2]));
+    }
+    XRP_HD double f64(double s) const { return sample64(S, r, s); }
+};
+
+// integrate_along_ray (main.go:144-154): returns the sum of densities over
+// the lattice samples (pre-multiplier, pre-ds).
+template <class Sampler>
+XRP_HD float march_simple(const Lattice& L, const float* lo, const float* hi, const Ray& r,
+                          const Sampler& smp, RayStats& st) {
+    float t0, t1;
+    clip_ray(lo, hi, r, t0, t1);
+    int k0, k1;
+    KahanF acc;
+    if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
+    for (int k = k0; k <= k1; k++) {
+        float rho = smp.f32(L.t32[k]);
+        if (isunc(rho)) {
+            rho = (float)smp.f64(L.s64[k]);
+            st.fallbacks++;
+        }
+        acc.add(rho);
+    }
+    st.samples += (uint32_t)(k1 - k0 + 1);
+    return acc.s;
+}
+
+// integrate_hierarchical (main.go:159-199): returns sum(w*rho) with w in
+// {DS, DS/10} (pre-multiplier).
+template <class Sampler>
+XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, const Ray& r,
+                        const Sampler& smp, RayStats& st) {
+    float t0, t1;
+    clip_ray(lo, hi, r, t0, t1);
+    int k0, k1;
+    KahanF acc;
+    if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
+    bool prev_zero = true;  // coarse samples before k0 are outside the support
+    for (int k = k0; k <= k1; k++) {
+        float rho = smp.f32(L.t32[k]);
+        if (isunc(rho)) {
+            rho = (float)smp.f64(L.s64[k]);
+            st.fallbacks++;
+        }
+        st.samples++;
+        bool zero = (rho == 0.0f);
+        if (zero != prev_zero) {
+            int f0 = L.fstart[k], f1 = L.fstart[k + 1];
+            for (int m = f0; m < f1; m++) {
+                float rf = smp.f32(L.ft32[m]);
+                if (isunc(rf)) {
+                    rf = (float)smp.f64(L.f64[m]);
+                    st.fallbacks++;
+                }
+                acc.add(rf * L.dsf32);
+            }
+            st.samples += (uint32_t)(f1 - f0);
+            acc.add(rho * L.dsf32);
+        } else {
+            acc.add(rho * L.ds32);
+        }
+        prev_zero = zero;
+    }
+    return acc.s;
+}
+
+// One pixel: optical depth T = flat_field + multiplier * (sum), as
+// transmittance exp(-T) (main.go:146, 153, 175, 198).
+template <bool HIER, bool VOLUME>
+XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P,
+                          const ViewDev& V, int i, int j, RayStats& st) {
+    Ray r;
+    setup_ray(V, P, i, j, L.s_c, r);
+    float acc;
+    if constexpr (VOLUME) {
+        const Volume& vol = S.vols[0];
+        VolRay vr;
+        setup_volray(vol, r, L.s_c, vr);
+        VolumeSampler smp{S, vol, r, vr, {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
+                          S.nodes[S.root].f[0]};
+        acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
+                   : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+    } else {
+        SceneSampler smp{S, r};
+        acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
+                   : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+    }
+    float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+    float T = fmaf(w, acc, P.flat_field);
+    return expf(-T);
+}
+
+}  // namespace xrp

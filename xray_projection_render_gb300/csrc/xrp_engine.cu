@@ -1,0 +1,708 @@
+// xrp_engine.cu -- CUDA kernels and the C ABI of libcuda_render.so.
+//
+// One thread marches one pixel's ray over the reference's FP64 sample lattice
+// with the FP32 guarded evaluator of xrp_device.h; a block covers a 16x16
+// pixel tile (each warp an 8x4 sub-tile, so neighbouring rays of a warp stay
+// spatially coherent for the voxel gathers and the primitive candidate
+// lists).  Views are processed in chunks so that the copy of one chunk's
+// images to the host overlaps the rendering of the next.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/xrp.h"
+#include "xrp_device.h"
+#include "xrp_scene.h"
+
+using namespace xrp;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string t_err;
+static thread_local uint64_t t_stats[2] = {0, 0};
+
+static int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return code;
+}
+
+static int cuda_fail(int code, const char* what, cudaError_t e) {
+    return fail(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+template <bool HIER, bool VOLUME>
+__global__ void __launch_bounds__(256)
+    k_render(SceneDev S, Lattice L, RenderParams P, const ViewDev* __restrict__ views, int view0,
+             int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats) {
+    const int res = P.res;
+    const int tpr = (res + 15) >> 4;
+    const int tpv = tpr * tpr;
+    const int b = blockIdx.x;
+    const int v = b / tpv;
+    const int t = b - v * tpv;
+    const int ti = t / tpr, tj = t - ti * tpr;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = (ti << 4) + ((warp >> 1) << 2) + (lane >> 3);
+    const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
+    RayStats st{0, 0};
+    if (v < nviews && i < res && j < res) {
+        float val = render_pixel<HIER, VOLUME>(S, L, P, views[view0 + v], i, j, st);
+        out[((size_t)v * res + i) * res + j] = val;
+    }
+    if (stats) {  // every lane reaches this point
+        unsigned s = __reduce_add_sync(0xffffffffu, st.samples);
+        unsigned f = __reduce_add_sync(0xffffffffu, st.fallbacks);
+        if (lane == 0) {
+            atomicAdd(&stats[0], (unsigned long long)s);
+            if (f) atomicAdd(&stats[1], (unsigned long long)f);
+        }
+    }
+}
+
+// Reference voxelizer semantics (cuda_backend.cu:208-252): one voxel per
+// thread, cylinders staged in shared memory.
+__global__ void __launch_bounds__(256)
+    k_voxelize(const CylinderParams* __restrict__ cyl, int ncyl, int res, float dm,
+               const int* __restrict__ cell_off, const int* __restrict__ cell_idx, int grid_dim,
+               int use_smem, float* __restrict__ out) {
+    extern __shared__ CylinderParams s_cyl[];
+    const bool spatial = cell_off != nullptr;
+    if (use_smem) {
+        for (int k = threadIdx.x; k < ncyl; k += blockDim.x) s_cyl[k] = cyl[k];
+        __syncthreads();
+    }
+    long total = (long)res * res * res;
+    for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long)gridDim.x * blockDim.x) {
+        int k = (int)(idx / ((long)res * res));
+        int i = (int)((idx / res) % res);
+        int j = (int)(idx % res);
+        float rf = (float)res;
+        float x = (float)i / rf * 2.0f - 1.0f;
+        float y = (float)j / rf * 2.0f - 1.0f;
+        float z = (float)k / rf * 2.0f - 1.0f;
+        int c0 = 0, c1 = ncyl;
+        if (spatial) {
+            float cs = 2.0f / (float)grid_dim;
+            int cx = (int)((x + 1.0f) / cs), cy = (int)((y + 1.0f) / cs), cz = (int)((z + 1.0f) / cs);
+            cx = min(max(cx, 0), grid_dim - 1);
+            cy = min(max(cy, 0), grid_dim - 1);
+            cz = min(max(cz, 0), grid_dim - 1);
+            int cell = (cz * grid_dim + cy) * grid_dim + cx;
+            c0 = cell_off[cell];
+            c1 = cell_off[cell + 1];
+        }
+        float dens = 0.0f;
+        for (int q = c0; q < c1; q++) {
+            const CylinderParams c = spatial ? cyl[cell_idx[q]] : (use_smem ? s_cyl[q] : cyl[q]);
+            float vx = c.p1[0] - c.p0[0], vy = c.p1[1] - c.p0[1], vz = c.p1[2] - c.p0[2];
+            float wx = x - c.p0[0], wy = y - c.p0[1], wz = z - c.p0[2];
+            float vv = vx * vx + vy * vy + vz * vz;
+            if (vv == 0.0f) continue;
+            float tt = (wx * vx + wy * vy + wz * vz) / vv;
+            if (tt < 0.0f || tt > 1.0f) continue;
+            float dx = wx - vx * tt, dy = wy - vy * tt, dz = wz - vz * tt;
+            if (dx * dx + dy * dy + dz * dz < c.radius * c.radius) dens += c.rho;
+        }
+        dens *= dm;
+        dens = fminf(fmaxf(dens, 0.0f), 1.0f);
+        out[idx] = dens;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-device engine state
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Engine {
+    int device = -1;
+    cudaStream_t compute = nullptr, copy = nullptr;
+    cudaMemPool_t pool = nullptr;
+    std::mutex mtx;
+    unsigned long long* stats = nullptr;  // 2 counters
+    bool ok = false;
+    std::string init_error;
+};
+
+std::mutex g_engines_mtx;
+std::map<int, std::unique_ptr<Engine>> g_engines;
+
+Engine* engine_for_current(int* code) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *code = cuda_fail(3, "cudaGetDevice", e);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> g(g_engines_mtx);
+    auto it = g_engines.find(dev);
+    if (it != g_engines.end()) return it->second.get();
+    auto E = std::make_unique<Engine>();
+    E->device = dev;
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    if ((e = cudaStreamCreateWithFlags(&E->compute, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&E->copy, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMemPoolCreate(&E->pool, &props)) != cudaSuccess ||
+        (e = cudaMalloc(&E->stats, 2 * sizeof(unsigned long long))) != cudaSuccess) {
+        *code = cuda_fail(3, "engine initialisation", e);
+        return nullptr;
+    }
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(E->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    E->ok = true;
+    Engine* raw = E.get();
+    g_engines[dev] = std::move(E);
+    return raw;
+}
+
+// Stream-ordered allocation from the engine pool, freed on the same stream.
+struct PoolBuf {
+    void* p = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t alloc(Engine* E, size_t n, cudaStream_t st) {
+        s = st;
+        return cudaMallocFromPoolAsync(&p, n ? n : 16, E->pool, st);
+    }
+    ~PoolBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
+// Packs small tables into one upload.
+struct Tables {
+    std::vector<unsigned char> host;
+    size_t add(const void* src, size_t n, size_t align = 16) {
+        size_t off = (host.size() + align - 1) / align * align;
+        host.resize(off + n);
+        if (n) memcpy(host.data() + off, src, n);
+        return off;
+    }
+    template <class T>
+    size_t add(const std::vector<T>& v) {
+        return add(v.data(), v.size() * sizeof(T));
+    }
+};
+
+struct Prepared {
+    SceneDev S;
+    Lattice L;
+    RenderParams P;
+    const ViewDev* views = nullptr;
+    bool volume_fast = false;
+    bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
+};
+
+// Everything a render needs on the device except the volume data.
+int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol_dev,
+            const std::vector<const double*>& vol64_dev, const std::vector<ViewDev>& views,
+            int res, int integration, double ds, double R, double ff, double dm, double fov_max,
+            cudaStream_t st, PoolBuf& tab, Prepared& out) {
+    HostPrepared hp;
+    try {
+        hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max);
+    } catch (const std::exception& ex) {
+        return fail(2, "%s", ex.what());
+    }
+    for (size_t k = 0; k < hp.vols.size(); k++) {
+        hp.vols[k].data = vol_dev[k];
+        hp.vols[k].data64 = vol64_dev[k];
+    }
+    const FlatScene& fs = hp.fs;
+    const HostLattice& hl = hp.hl;
+    Tables T;
+    size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
+    size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
+    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs);
+    size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
+    size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
+    cudaError_t e = tab.alloc(E, T.host.size(), st);
+    if (e != cudaSuccess) return cuda_fail(3, "table allocation", e);
+    e = cudaMemcpyAsync(tab.p, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(5, "table upload", e);
+    unsigned char* base = (unsigned char*)tab.p;
+    out.S = hp.S;
+    SceneDev& S = out.S;
+    S.nodes = (const Node*)(base + o_nodes);
+    S.nodes64 = (const Node64*)(base + o_n64);
+    S.child = (const int32_t*)(base + o_child);
+    S.cells = (const int32_t*)(base + o_cells);
+    S.items = (const int32_t*)(base + o_items);
+    S.defs = (const DefStep*)(base + o_defs);
+    S.vols = (const Volume*)(base + o_vols);
+    out.L = hl.hdr;
+    Lattice& L = out.L;
+    L.s64 = (const double*)(base + o_s64);
+    L.t32 = (const float*)(base + o_t32);
+    L.fstart = (const int32_t*)(base + o_fs);
+    L.f64 = (const double*)(base + o_f64);
+    L.ft32 = (const float*)(base + o_ft32);
+    out.P = hp.P;
+    out.P.nviews = (int)views.size();
+    out.P.xs = (const double*)(base + o_xs);
+    out.views = (const ViewDev*)(base + o_views);
+    out.volume_fast = hp.volume_fast;
+    out.empty = hl.hdr.K <= 0;
+    return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launch
+// ---------------------------------------------------------------------------
+
+static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integration, float* dout,
+                          unsigned long long* stats, cudaStream_t st) {
+    const ViewDev* dviews = pr.views;
+    const int res = pr.P.res;
+    const int tpr = (res + 15) / 16;
+    long blocks = (long)nviews * tpr * tpr;
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
+    dim3 grid((unsigned)blocks), block(256);
+    bool hier = integration == XRP_INTEGRATE_HIERARCHICAL;
+    if (pr.volume_fast) {
+        if (hier)
+            k_render<true, true><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        else
+            k_render<false, true><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+    } else {
+        if (hier)
+            k_render<true, false><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        else
+            k_render<false, false><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+    }
+    return cudaGetLastError();
+}
+
+// Renders `views` into `out` (device or host memory).  Host output goes
+// through two device chunk buffers so the copy of chunk c overlaps the
+// rendering of chunk c+1.
+static int render_views(Engine* E, const HostScene& hs, const std::vector<const float*>& vdev,
+                        const std::vector<const double*>& v64, const std::vector<ViewDev>& views,
+                        const xrp_render_opts& o, double fov_max, float* out, bool out_host,
+                        cudaStream_t st, cudaStream_t st_copy, bool want_stats) {
+    const int res = o.resolution;
+    const int nviews = (int)views.size();
+    PoolBuf tab;
+    Prepared pr;
+    int rc = prepare(E, hs, vdev, v64, views, res, o.integration, o.ds, o.R, o.flat_field,
+                     o.density_multiplier, fov_max, st, tab, pr);
+    if (rc) return rc;
+    unsigned long long* stats = nullptr;
+    cudaError_t e;
+    if (want_stats) {
+        if ((e = cudaMemsetAsync(E->stats, 0, 2 * sizeof(unsigned long long), st)) != cudaSuccess)
+            return cuda_fail(7, "stats reset", e);
+        stats = E->stats;
+    }
+    const size_t img = (size_t)res * res;
+    const int tpv = ((res + 15) / 16) * ((res + 15) / 16);
+    const int max_views_per_launch = std::max(1, (int)(0x7fffffffL / tpv));
+    if (!out_host) {
+        for (int v0 = 0; v0 < nviews; v0 += max_views_per_launch) {
+            int n = std::min(max_views_per_launch, nviews - v0);
+            if ((e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st)) != cudaSuccess)
+                return cuda_fail(7, "kernel launch", e);
+        }
+    } else {
+        size_t chunk = std::max<size_t>(1, std::min<size_t>((size_t)nviews, ((size_t)64 << 20) / (img * 4)));
+        chunk = std::min<size_t>(chunk, (size_t)max_views_per_launch);
+        int nchunks = (int)((nviews + chunk - 1) / chunk);
+        PoolBuf buf[2];
+        for (int b = 0; b < std::min(2, nchunks); b++)
+            if ((e = buf[b].alloc(E, chunk * img * sizeof(float), st)) != cudaSuccess)
+                return cuda_fail(6, "image buffer allocation", e);
+        cudaEvent_t kev[2], cev[2];
+        for (int b = 0; b < 2; b++) {
+            cudaEventCreateWithFlags(&kev[b], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&cev[b], cudaEventDisableTiming);
+        }
+        auto launch_chunk = [&](int c) -> cudaError_t {
+            int b = c & 1;
+            if (c >= 2) cudaStreamWaitEvent(st, cev[b], 0);
+            int v0 = (int)(c * chunk);
+            int n = (int)std::min(chunk, (size_t)(nviews - v0));
+            cudaError_t le = launch(pr, v0, n, o.integration, (float*)buf[b].p, stats, st);
+            cudaEventRecord(kev[b], st);
+            return le;
+        };
+        int code = 0;
+        if ((e = launch_chunk(0)) != cudaSuccess) code = cuda_fail(7, "kernel launch", e);
+        for (int c = 0; c < nchunks && !code; c++) {
+            if (c + 1 < nchunks && (e = launch_chunk(c + 1)) != cudaSuccess) {
+                code = cuda_fail(7, "kernel launch", e);
+                break;
+            }
+            int b = c & 1;
+            int v0 = (int)(c * chunk);
+            size_t n = std::min(chunk, (size_t)(nviews - v0));
+            cudaStreamWaitEvent(st_copy, kev[b], 0);
+            e = cudaMemcpyAsync(out + (size_t)v0 * img, buf[b].p, n * img * sizeof(float),
+                                cudaMemcpyDeviceToHost, st_copy);
+            if (e != cudaSuccess) {
+                code = cuda_fail(8, "image copy", e);
+                break;
+            }
+            cudaEventRecord(cev[b], st_copy);
+        }
+        cudaError_t e1 = cudaStreamSynchronize(st_copy);
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        for (int b = 0; b < 2; b++) {
+            cudaEventDestroy(kev[b]);
+            cudaEventDestroy(cev[b]);
+        }
+        if (code) return code;
+        if (e2 != cudaSuccess) return cuda_fail(7, "kernel execution", e2);
+        if (e1 != cudaSuccess) return cuda_fail(8, "image copy", e1);
+    }
+    if (want_stats) {
+        unsigned long long h[2] = {0, 0};
+        if ((e = cudaMemcpyAsync(h, E->stats, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return cuda_fail(7, "stats read", e);
+        t_stats[0] = h[0];
+        t_stats[1] = h[1];
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// scenes
+// ---------------------------------------------------------------------------
+
+struct xrp_scene {
+    HostScene hs;
+    std::vector<void*> owned;  // device allocations (cudaMalloc)
+    std::vector<const float*> vdev;
+    std::vector<const double*> v64;
+    int device = -1;
+    double sup_lo[3], sup_hi[3];
+};
+
+static void scene_free(xrp_scene* s) {
+    if (!s) return;
+    for (void* p : s->owned) cudaFree(p);
+    delete s;
+}
+
+static bool opts_ok(const xrp_render_opts* o, std::string& why) {
+    if (!o) { why = "null options"; return false; }
+    if (o->resolution <= 0) { why = "resolution must be > 0"; return false; }
+    if (!(o->ds > 0) || !std::isfinite(o->ds)) { why = "ds must be > 0 and finite"; return false; }
+    if (!std::isfinite(o->R)) { why = "R must be finite"; return false; }
+    if (o->integration != XRP_INTEGRATE_SIMPLE && o->integration != XRP_INTEGRATE_HIERARCHICAL) {
+        why = "unknown integration method";
+        return false;
+    }
+    double samples = 3.48 / o->ds;
+    if (samples > 5.0e7) { why = "ds too small (more than 5e7 samples per ray)"; return false; }
+    return true;
+}
+
+static std::vector<ViewDev> views_from(const xrp_camera* cams, int n, double* fov_max) {
+    std::vector<ViewDev> v(n);
+    *fov_max = 0;
+    for (int k = 0; k < n; k++) {
+        view_from_camera(cams[k].eye, cams[k].camera, cams[k].fov_deg, v[k]);
+        *fov_max = std::max(*fov_max, std::fabs(cams[k].fov_deg));
+    }
+    return v;
+}
+
+extern "C" {
+
+const char* xrp_last_error(void) { return t_err.c_str(); }
+
+int xrp_version(void) { return 100; }
+
+int xrp_cameras_from_angles(const double* az_polar, int n, double R, double fov_deg, xrp_camera* out) {
+    if (!az_polar || !out) return fail(1, "null pointer");
+    if (n < 0) return fail(2, "negative count");
+    for (int k = 0; k < n; k++) {
+        camera_from_angles(az_polar[2 * k], az_polar[2 * k + 1], R, out[k].eye, out[k].camera);
+        out[k].fov_deg = fov_deg;
+    }
+    return 0;
+}
+
+int xrp_scene_create(const char* object_json, const char* deformation_json,
+                     const xrp_volume_desc* volumes, int num_volumes, xrp_scene** out) {
+    if (!object_json || !out) return fail(1, "null pointer");
+    if (num_volumes < 0 || (num_volumes > 0 && !volumes)) return fail(1, "bad volume list");
+    *out = nullptr;
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    std::unique_ptr<xrp_scene, void (*)(xrp_scene*)> s(new xrp_scene(), scene_free);
+    s->device = E->device;
+    std::vector<HVolume> ext(num_volumes);
+    for (int k = 0; k < num_volumes; k++) {
+        const xrp_volume_desc& d = volumes[k];
+        if (!d.data) return fail(1, "volume %d: null data", k);
+        if (d.nx <= 0 || d.ny <= 0 || d.nz <= 0) return fail(2, "volume %d: bad sizes", k);
+        ext[k].nx = d.nx;
+        ext[k].ny = d.ny;
+        ext[k].nz = d.nz;
+        if (d.on_device) {
+            ext[k].ext = d.data;
+        } else {
+            size_t n = (size_t)d.nx * d.ny * d.nz;
+            ext[k].data.assign(d.data, d.data + n);
+        }
+    }
+    try {
+        s->hs = load_scene(object_json, deformation_json, ext);
+        RenderGeometry g;
+        FlatScene fs = flatten(s->hs, g, false);  // validates depth and types
+        for (int a = 0; a < 3; a++) {
+            s->sup_lo[a] = fs.sup_lo[a];
+            s->sup_hi[a] = fs.sup_hi[a];
+        }
+    } catch (const std::exception& ex) {
+        return fail(2, "%s", ex.what());
+    }
+    for (auto& v : s->hs.vols) {
+        size_t n = (size_t)v.nx * v.ny * v.nz;
+        if (v.ext) {
+            s->vdev.push_back(v.ext);
+        } else {
+            void* p = nullptr;
+            cudaError_t e = cudaMalloc(&p, n * sizeof(float));
+            if (e != cudaSuccess) return cuda_fail(3, "volume allocation", e);
+            s->owned.push_back(p);
+            if ((e = cudaMemcpy(p, v.data.data(), n * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+                return cuda_fail(4, "volume upload", e);
+            s->vdev.push_back((const float*)p);
+            std::vector<float>().swap(v.data);
+        }
+        if (!v.data64.empty()) {
+            void* p = nullptr;
+            cudaError_t e = cudaMalloc(&p, n * sizeof(double));
+            if (e != cudaSuccess) return cuda_fail(3, "volume allocation", e);
+            s->owned.push_back(p);
+            if ((e = cudaMemcpy(p, v.data64.data(), n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+                return cuda_fail(4, "volume upload", e);
+            s->v64.push_back((const double*)p);
+            std::vector<double>().swap(v.data64);
+        } else {
+            s->v64.push_back(nullptr);
+        }
+    }
+    *out = s.release();
+    return 0;
+}
+
+void xrp_scene_destroy(xrp_scene* scene) { scene_free(scene); }
+
+int xrp_scene_support(const xrp_scene* s, double lo[3], double hi[3]) {
+    if (!s || !lo || !hi) return fail(1, "null pointer");
+    for (int a = 0; a < 3; a++) {
+        lo[a] = s->sup_lo[a];
+        hi[a] = s->sup_hi[a];
+    }
+    return 0;
+}
+
+int xrp_render(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_render_opts* o, float* out) {
+    if (!s || !views || !o || !out) return fail(1, "null pointer");
+    std::string why;
+    if (nviews <= 0) return fail(2, "num_views must be > 0");
+    if (!opts_ok(o, why)) return fail(2, "%s", why.c_str());
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
+    double fov_max;
+    std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
+    std::lock_guard<std::mutex> g(E->mtx);
+    return render_views(E, s->hs, s->vdev, s->v64, v, *o, fov_max, out, true, E->compute, E->copy,
+                        (o->flags & XRP_FLAG_STATS) != 0);
+}
+
+int xrp_render_device(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_render_opts* o,
+                      float* out_device, void* stream) {
+    if (!s || !views || !o || !out_device) return fail(1, "null pointer");
+    std::string why;
+    if (nviews <= 0) return fail(2, "num_views must be > 0");
+    if (!opts_ok(o, why)) return fail(2, "%s", why.c_str());
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
+    double fov_max;
+    std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
+    // stats use the engine's shared counters and need a synchronisation
+    return render_views(E, s->hs, s->vdev, s->v64, v, *o, fov_max, out_device, false,
+                        (cudaStream_t)stream, (cudaStream_t)stream, false);
+}
+
+int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples) {
+    if (samples) *samples = t_stats[0];
+    if (fp64_samples) *fp64_samples = t_stats[1];
+    return 0;
+}
+
+void xrp_release_cache(void) {
+    std::lock_guard<std::mutex> g(g_engines_mtx);
+    for (auto& kv : g_engines) {
+        std::lock_guard<std::mutex> g2(kv.second->mtx);
+        cudaStreamSynchronize(kv.second->compute);
+        cudaStreamSynchronize(kv.second->copy);
+        cudaMemPoolTrimTo(kv.second->pool, 0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reference ABI
+// ---------------------------------------------------------------------------
+
+int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
+                                const XRayCameraParams* cams, int ncams, int res, float ds,
+                                float flat_field, float* out_images) {
+    if (!volume || !cams || !out_images) return fail(1, "null pointer");
+    if (nx <= 0 || ny <= 0 || nz <= 0 || res <= 0 || ncams <= 0) return fail(2, "bad sizes");
+    if (!(ds > 0.0f) || !std::isfinite(ds)) return fail(2, "ds must be > 0 and finite");
+    if ((double)3.48 / (double)ds > 5.0e7) return fail(2, "ds too small");
+    size_t nvox = (size_t)nx * ny * nz;
+    if (nvox / nx / ny != (size_t)nz) return fail(2, "volume too large");
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    std::lock_guard<std::mutex> g(E->mtx);
+    cudaStream_t st = E->compute;
+    PoolBuf dvol;
+    cudaError_t e = dvol.alloc(E, nvox * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_fail(3, "volume allocation", e);
+    if ((e = cudaMemcpyAsync(dvol.p, volume, nvox * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(4, "volume upload", e);
+    HostScene hs = volume_scene((const float*)dvol.p, nx, ny, nz);
+    std::vector<const float*> vdev{(const float*)dvol.p};
+    std::vector<const double*> v64{nullptr};
+    size_t img = (size_t)res * res;
+    // cameras that share R share one sample lattice (main.go:465)
+    int c0 = 0;
+    while (c0 < ncams) {
+        int c1 = c0 + 1;
+        while (c1 < ncams && cams[c1].R == cams[c0].R) c1++;
+        std::vector<ViewDev> views(c1 - c0);
+        double fov_max = 0;
+        for (int c = c0; c < c1; c++) {
+            double eye[3], m[16];
+            for (int a = 0; a < 3; a++) eye[a] = (double)cams[c].eye[a];
+            for (int r = 0; r < 4; r++)
+                for (int k = 0; k < 4; k++) m[k * 4 + r] = (double)cams[c].view[r * 4 + k];
+            view_from_camera(eye, m, (double)cams[c].fov_y, views[c - c0]);
+            fov_max = std::max(fov_max, std::fabs((double)cams[c].fov_y));
+        }
+        xrp_render_opts o;
+        memset(&o, 0, sizeof(o));
+        o.resolution = res;
+        o.integration = XRP_INTEGRATE_SIMPLE;
+        o.ds = (double)ds;
+        o.R = (double)cams[c0].R;
+        o.flat_field = (double)flat_field;
+        o.density_multiplier = 1.0;
+        int rc = render_views(E, hs, vdev, v64, views, o, fov_max, out_images + (size_t)c0 * img, true,
+                              st, E->copy, false);
+        if (rc) return rc;
+        c0 = c1;
+    }
+    return 0;
+}
+
+static int voxelize(const CylinderParams* cyl, int ncyl, int res, float dm, int grid_dim,
+                    const int* off, const int* idx, int nidx, float* out, bool spatial) {
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return spatial ? 3 : 2;
+    std::lock_guard<std::mutex> g(E->mtx);
+    cudaStream_t st = E->compute;
+    size_t nvox = (size_t)res * res * res;
+    PoolBuf dcyl, dout, doff, didx;
+    cudaError_t e;
+    int c_alloc = spatial ? 3 : 2, c_copy = spatial ? 4 : 3, c_valloc = spatial ? 3 : 4;
+    if ((e = dcyl.alloc(E, (size_t)ncyl * sizeof(CylinderParams), st)) != cudaSuccess)
+        return cuda_fail(c_alloc, "cylinder allocation", e);
+    if ((e = cudaMemcpyAsync(dcyl.p, cyl, (size_t)ncyl * sizeof(CylinderParams), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(c_copy, "cylinder upload", e);
+    if ((e = dout.alloc(E, nvox * sizeof(float), st)) != cudaSuccess)
+        return cuda_fail(c_valloc, "volume allocation", e);
+    if (spatial) {
+        size_t ncell = (size_t)grid_dim * grid_dim * grid_dim + 1;
+        if ((e = doff.alloc(E, ncell * sizeof(int), st)) != cudaSuccess ||
+            (e = didx.alloc(E, (size_t)std::max(nidx, 1) * sizeof(int), st)) != cudaSuccess)
+            return cuda_fail(3, "cell list allocation", e);
+        if ((e = cudaMemcpyAsync(doff.p, off, ncell * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (nidx > 0 && (e = cudaMemcpyAsync(didx.p, idx, (size_t)nidx * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess))
+            return cuda_fail(4, "cell list upload", e);
+    }
+    int use_smem = (!spatial && (size_t)ncyl * sizeof(CylinderParams) <= 48 * 1024) ? 1 : 0;
+    size_t smem = use_smem ? (size_t)ncyl * sizeof(CylinderParams) : 0;
+    long blocks = (long)((nvox + 255) / 256);
+    blocks = std::min<long>(blocks, 152L * 64);
+    k_voxelize<<<(unsigned)std::max<long>(blocks, 1), 256, smem, st>>>(
+        (const CylinderParams*)dcyl.p, ncyl, res, dm, spatial ? (const int*)doff.p : nullptr,
+        spatial ? (const int*)didx.p : nullptr, grid_dim, use_smem, (float*)dout.p);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return cuda_fail(5, "voxelizer kernel", e);
+    if ((e = cudaMemcpyAsync(out, dout.p, nvox * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return cuda_fail(6, "volume copy", e);
+    return 0;
+}
+
+int AssembleVoxelGridCUDA(const CylinderParams* cylinders, int num_cylinders, int res,
+                          float density_multiplier, float* out_volume) {
+    if (!cylinders || !out_volume || num_cylinders <= 0 || res <= 0) return fail(1, "bad arguments");
+    return voxelize(cylinders, num_cylinders, res, density_multiplier, 0, nullptr, nullptr, 0,
+                    out_volume, false);
+}
+
+int AssembleVoxelGridSpatialCUDA(const CylinderParams* cylinders, int num_cylinders, int res,
+                                 float density_multiplier, int grid_dim, const int* cell_offsets,
+                                 const int* cyl_indices, int num_cyl_indices, float* out_volume) {
+    if (!cylinders || !out_volume || !cell_offsets || !cyl_indices) return fail(1, "null pointer");
+    if (num_cylinders <= 0 || res <= 0 || grid_dim <= 0 || num_cyl_indices < 0) return fail(2, "bad sizes");
+    // the device reads cyl_indices[cell_offsets[c] .. cell_offsets[c+1]) and
+    // cylinders[cyl_indices[q]]: check the lists before any device access
+    long ncell = (long)grid_dim * grid_dim * grid_dim;
+    if (grid_dim > 1024) return fail(2, "grid_dim too large");
+    for (long c = 0; c < ncell; c++)
+        if (cell_offsets[c] < 0 || cell_offsets[c] > cell_offsets[c + 1]) return fail(2, "bad cell offsets");
+    if (cell_offsets[ncell] > num_cyl_indices) return fail(2, "cell offsets exceed the index list");
+    for (int q = 0; q < num_cyl_indices; q++)
+        if (cyl_indices[q] < 0 || cyl_indices[q] >= num_cylinders) return fail(2, "bad cylinder index");
+    return voxelize(cylinders, num_cylinders, res, density_multiplier, grid_dim, cell_offsets,
+                    cyl_indices, num_cyl_indices, out_volume, true);
+}
+
+}  // extern "C"

@@ -1,0 +1,193 @@
+"""Python front end of the GB300 projection engine (libcuda_render.so).
+
+Mirrors the reference's render interface (main.go:310-471 / api.go:40-64):
+an object map in the reference JSON/YAML schema, an optional deformation
+map, camera angles and the CLI options (resolution, ds, R, fov, flat_field,
+density_multiplier, integration).  Every call goes through the C ABI of
+include/xrp.h; the images are float32 transmittance [view][i][j].
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+
+import numpy as np
+
+from . import _lib
+from ._lib import XrpCamera, XrpRenderOpts, XrpVolumeDesc, check
+
+
+def _json(x) -> bytes | None:
+    if x is None:
+        return None
+    if isinstance(x, (bytes, bytearray)):
+        return bytes(x)
+    if isinstance(x, str):
+        return x.encode()
+    return json.dumps(x).encode()
+
+
+def _is_torch_cuda(t) -> bool:
+    return type(t).__module__.startswith("torch") and getattr(t, "is_cuda", False)
+
+
+class Scene:
+    """A scene resident on the current CUDA device (xrp_scene_create).
+
+    ``volumes`` lists the grids referenced by ``{"type": "voxel_grid",
+    "volume": k}`` entries: float32 numpy arrays [z][x][y] (copied to the
+    device) or CUDA tensors (used in place; keep them alive)."""
+
+    def __init__(self, obj, deformation=None, volumes=()):
+        L = _lib.load()
+        self._keep = []
+        descs = (XrpVolumeDesc * max(1, len(volumes)))()
+        for k, v in enumerate(volumes):
+            if _is_torch_cuda(v):
+                if v.dtype.__repr__() != "torch.float32" or not v.is_contiguous():
+                    raise ValueError("device volumes must be contiguous float32")
+                nz, nx, ny = v.shape
+                descs[k] = XrpVolumeDesc(v.data_ptr(), nx, ny, nz, 1)
+            else:
+                a = np.ascontiguousarray(v, dtype=np.float32)
+                nz, nx, ny = a.shape
+                descs[k] = XrpVolumeDesc(a.ctypes.data, nx, ny, nz, 0)
+            self._keep.append(v)
+        h = ctypes.c_void_p()
+        check(L.xrp_scene_create(_json(obj), _json(deformation), descs, len(volumes),
+                                 ctypes.byref(h)), "xrp_scene_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def support(self):
+        lo = (ctypes.c_double * 3)()
+        hi = (ctypes.c_double * 3)()
+        check(_lib.load().xrp_scene_support(self._h, lo, hi), "xrp_scene_support")
+        return list(lo), list(hi)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().xrp_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def cameras_from_angles(angles, R=4.0, fov=40.0):
+    """computeCameraFromAngles (main.go:226-239) for a list of (azimuthal,
+    polar) degrees, as an array of XrpCamera."""
+    a = np.ascontiguousarray(np.asarray(angles, dtype=np.float64).reshape(-1, 2))
+    cams = (XrpCamera * max(1, a.shape[0]))()
+    check(_lib.load().xrp_cameras_from_angles(a.ctypes.data, a.shape[0], float(R), float(fov),
+                                              cams), "xrp_cameras_from_angles")
+    return cams, a.shape[0]
+
+
+def camera_arrays(angles, R=4.0, fov=40.0):
+    """(eyes [n,3], column-major cameras [n,16]) from the engine's camera code."""
+    cams, n = cameras_from_angles(angles, R, fov)
+    eyes = np.array([list(cams[k].eye) for k in range(n)])
+    mats = np.array([list(cams[k].camera) for k in range(n)])
+    return eyes, mats
+
+
+def _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats):
+    if integration not in ("simple", "hierarchical"):
+        raise ValueError(f"Unknown integration method: {integration}")
+    return XrpRenderOpts(int(resolution),
+                         _lib.XRP_INTEGRATE_HIERARCHICAL if integration == "hierarchical"
+                         else _lib.XRP_INTEGRATE_SIMPLE,
+                         float(ds), float(R), float(flat_field), float(density_multiplier),
+                         _lib.XRP_FLAG_STATS if stats else 0, 0)
+
+
+def render(scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, flat_field=0.0,
+           density_multiplier=1.0, integration="simple", out=None, stream=None, stats=False):
+    """Render the views given by ``angles`` ((azimuthal, polar) degrees).
+
+    Host path (default): returns a float32 numpy array [views, res, res];
+    ``out`` may be a preallocated (ideally pinned) host array.  Device path:
+    pass ``out`` as a contiguous float32 CUDA tensor; the work is queued on
+    ``stream`` (default: torch's current stream) and the call returns at once.
+    With ``stats`` (host path) returns (images, samples, fp64_samples)."""
+    L = _lib.load()
+    cams, n = cameras_from_angles(angles, R, fov)
+    o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats)
+    if out is not None and _is_torch_cuda(out):
+        import torch
+        if out.dtype != torch.float32 or not out.is_contiguous() or out.numel() < n * resolution ** 2:
+            raise ValueError("out must be a contiguous float32 CUDA tensor of views*res*res")
+        st = stream if stream is not None else torch.cuda.current_stream(out.device)
+        check(L.xrp_render_device(scene.handle, cams, n, ctypes.byref(o),
+                                  ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(st.cuda_stream)),
+              "xrp_render_device")
+        return out
+    if out is None:
+        out = np.empty((n, resolution, resolution), dtype=np.float32)
+    ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+    check(L.xrp_render(scene.handle, cams, n, ctypes.byref(o), ctypes.c_void_p(ptr)), "xrp_render")
+    if stats:
+        s = ctypes.c_uint64()
+        f = ctypes.c_uint64()
+        L.xrp_last_stats(ctypes.byref(s), ctypes.byref(f))
+        return out, s.value, f.value
+    return out
+
+
+def xray_camera_params(angles, R=4.0, fov=40.0) -> np.ndarray:
+    """The float32 XRayCameraParams rows the reference Go glue builds
+    (cuda_path.go:61-77): eye, row-major camera-to-world, fov, R; shape [n,21]."""
+    eyes, mats = camera_arrays(angles, R, fov)
+    rows = np.zeros((len(eyes), 21), dtype=np.float32)
+    rows[:, 0:3] = eyes
+    rows[:, 3:19] = mats.reshape(-1, 4, 4).transpose(0, 2, 1).reshape(-1, 16)
+    rows[:, 19] = fov
+    rows[:, 20] = R
+    return rows
+
+
+def render_volume_projections(volume, cams21, image_res, ds, flat_field=0.0, out=None):
+    """RenderVolumeProjectionsCUDA (cuda_backend.h:101-112) on host buffers:
+    ``volume`` float32 [nz][nx][ny], ``cams21`` float32 [n,21]."""
+    L = _lib.load()
+    vol = np.ascontiguousarray(volume, dtype=np.float32)
+    nz, nx, ny = vol.shape
+    c = np.ascontiguousarray(cams21, dtype=np.float32).reshape(-1, 21)
+    n = c.shape[0]
+    if out is None:
+        out = np.empty((n, image_res, image_res), dtype=np.float32)
+    ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+    check(L.RenderVolumeProjectionsCUDA(vol.ctypes.data, nx, ny, nz, c.ctypes.data, n,
+                                        int(image_res), ctypes.c_float(ds),
+                                        ctypes.c_float(flat_field), ctypes.c_void_p(ptr)),
+          "RenderVolumeProjectionsCUDA")
+    return out
+
+
+def assemble_voxel_grid(cylinders, res, density_multiplier=1.0):
+    """AssembleVoxelGridCUDA (cuda_backend.h:33-39); cylinders: float32 [n, 8]
+    rows (p0, p1, radius, rho).  Returns float32 [res, res, res] ([k][i][j])."""
+    L = _lib.load()
+    c = np.ascontiguousarray(cylinders, dtype=np.float32).reshape(-1, 8)
+    out = np.empty((res, res, res), dtype=np.float32)
+    check(L.AssembleVoxelGridCUDA(c.ctypes.data, c.shape[0], int(res),
+                                  ctypes.c_float(density_multiplier), out.ctypes.data),
+          "AssembleVoxelGridCUDA")
+    return out
+
+
+def release_cache():
+    _lib.load().xrp_release_cache()
