@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--res", type=int, default=1024)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer ABI timing")
+    p.add_argument("--volume-path", default="gather", choices=["gather", "loads"],
+                   help="voxel reads: texture gathers (default) or per-tap loads")
     return p.parse_args()
 
 
@@ -142,19 +145,17 @@ def fp32_peak_tflops(torch):
 def cpu_baseline(workload, seconds, threads=None):
     """FP64 oracle on a seeded subset of the workload's rays, all host cores."""
     from oracle import oracle as O
-    vol = workload.volume
-    cams21 = None
     threads = threads or os.cpu_count() or 1
     from xray_projection_render_gb300 import engine  # camera rows only (host code)
     cams21 = engine.xray_camera_params(workload.angles, workload.R, workload.fov)
+    scene = O.VolumeABIScene(workload.volume)
     rng = np.random.default_rng(1234)
 
     def run(n):
         rays = np.stack([rng.integers(0, len(workload.angles), n), rng.integers(0, workload.res, n),
                          rng.integers(0, workload.res, n)], 1).astype(np.int32)
         t = time.perf_counter()
-        O.render_volume_abi(vol, cams21, workload.res, np.float32(workload.ds), rays=rays,
-                            nthreads=threads)
+        scene.render_rays(cams21, workload.res, np.float32(workload.ds), rays, nthreads=threads)
         return time.perf_counter() - t
 
     n = 2000
@@ -218,14 +219,14 @@ def main():
 
     def step():
         X.render(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, out=out,
-                 stream=stream)
+                 stream=stream, volume_path=args.volume_path)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     # exact sample count of one step (counter pass, untimed)
     _, samples, fp64 = X.render(scene, my_angles[:max(1, min(8, n_my))], resolution=res, ds=w.ds,
-                                R=w.R, fov=w.fov, stats=True)
+                                R=w.R, fov=w.fov, stats=True, volume_path=args.volume_path)
     frac = min(8, n_my) / n_my
     samples_step = samples / frac
     if world > 1:
@@ -251,11 +252,14 @@ def main():
 
     # end to end through the reference ABI with pinned host buffers
     cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
-    vol_host = torch.from_numpy(w.volume).pin_memory()
-    out_host = torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
-    X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)  # warm
-    e2e_times = []
-    for _ in range(max(1, min(args.steps, 3))):
+    if args.no_e2e:
+        e2e_times = [float("nan")]
+    else:
+        e2e_times = []
+        vol_host = torch.from_numpy(w.volume).pin_memory()
+        out_host = torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
+        X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)  # warm
+    for _ in range(0 if args.no_e2e else max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
@@ -278,6 +282,7 @@ def main():
         "config": {"workload": w.name, "views": len(w.angles), "res": res, "ds": w.ds,
                    "grid": [256, 256, 256], "integrator": "simple", "R": w.R, "fov": w.fov,
                    "l2": "flushed before every timed step (256 MiB write)",
+                   "volume_path": args.volume_path,
                    "parallelism": f"views k mod {world}"},
         "e2e": {"value": e2e_value, "unit": "Mrays/s",
                 "h2d_bytes_per_step": int(w.volume.nbytes + cams21.nbytes),

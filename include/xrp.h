@@ -111,7 +111,10 @@ XRP_API int xrp_cameras_from_angles(const double* az_polar_deg, int n, double R,
                             xrp_camera* out);
 
 enum { XRP_INTEGRATE_SIMPLE = 0, XRP_INTEGRATE_HIERARCHICAL = 1 };
-enum { XRP_FLAG_STATS = 1 };
+enum {
+    XRP_FLAG_STATS = 1,        /* count evaluated and FP64-re-evaluated samples */
+    XRP_FLAG_VOLUME_LOADS = 2  /* voxel-grid roots: per-tap loads instead of texture gathers */
+};
 
 /* Per-call options: the globals and flags of the reference CLI
  * (main.go:37-41, 683-707, 725-729). */

@@ -83,6 +83,8 @@ def lib():
                 "orc_render": (I, [I, I, D, D, I, D, D, D, I, P, P, I, P, L_, P, P, I]),
                 "orc_render_volume_abi": (I, [P, I, I, I, P, I, I, ctypes.c_float,
                                               ctypes.c_float, P, P, P, L_, I]),
+                "orc_render_f32cams": (I, [I, P, I, I, ctypes.c_float, ctypes.c_float, P, P, P,
+                                           L_, I]),
                 "orc_sample_table": (L_, [D, D, D, P, L_]),
                 "orc_min_feature_size": (D, [I]),
             }
@@ -370,6 +372,31 @@ def render_volume_abi(volume, cams21, res, ds, flat_field=0.0, *, rays=None, nth
     if rc != 0:
         raise ValueError(f"oracle volume render failed with code {rc}")
     return (out, outT) if return_T else out
+
+
+class VolumeABIScene:
+    """A voxel grid loaded once for repeated RenderVolumeProjectionsCUDA-
+    semantics renders (the CPU-baseline timing loop)."""
+
+    def __init__(self, volume):
+        self.vol = np.ascontiguousarray(volume, dtype=np.float32)
+        nz, nx, ny = self.vol.shape
+        L = lib()
+        L.orc_reset()
+        self.root = L.orc_voxel_f32(_ptr(self.vol), nx, ny, nz)
+        if self.root < 0:
+            raise MemoryError("oracle voxel allocation failed")
+
+    def render_rays(self, cams21, res, ds, rays, flat_field=0.0, nthreads=None):
+        c = np.ascontiguousarray(cams21, dtype=np.float32).reshape(-1, 21)
+        rays = np.ascontiguousarray(rays, dtype=np.int32).reshape(-1, 3)
+        out = np.zeros(rays.shape[0])
+        rc = lib().orc_render_f32cams(self.root, _ptr(c), c.shape[0], int(res), ctypes.c_float(ds),
+                                      ctypes.c_float(flat_field), _ptr(out), None, _ptr(rays),
+                                      rays.shape[0], int(nthreads or default_threads()))
+        if rc != 0:
+            raise ValueError(f"oracle volume render failed with code {rc}")
+        return out
 
 
 def sample_table(smin, smax, ds):

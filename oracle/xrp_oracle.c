@@ -819,12 +819,23 @@ ORC_EXPORT int orc_render(int root, int deform, double dm, double ff, int hierar
  * (cuda_backend.h:78-112): FP32 eye, row-major FP32 camera-to-world matrix,
  * FP32 fov, R, ds and flat field, widened to FP64, and the simple integrator
  * over VoxelGrid.Density. */
+ORC_EXPORT int orc_render_f32cams(int vox, const float* cams21, int ncams, int res, float ds,
+                                  float ff, double* out, double* out_T, const int* rays, long nrays,
+                                  int nthreads);
+
 ORC_EXPORT int orc_render_volume_abi(const float* volume, int nx, int ny, int nz,
                                      const float* cams21, int ncams, int res, float ds, float ff,
                                      double* out, double* out_T, const int* rays, long nrays,
                                      int nthreads) {
     int vox = orc_voxel_f32(volume, nx, ny, nz);
     if (vox < 0) return 3;
+    return orc_render_f32cams(vox, cams21, ncams, res, ds, ff, out, out_T, rays, nrays, nthreads);
+}
+
+/* The same with an already built root node (voxel grid). */
+ORC_EXPORT int orc_render_f32cams(int vox, const float* cams21, int ncams, int res, float ds,
+                                  float ff, double* out, double* out_T, const int* rays, long nrays,
+                                  int nthreads) {
     double* eyes = (double*)malloc((size_t)ncams * 3 * sizeof(double));
     double* cams = (double*)malloc((size_t)ncams * 16 * sizeof(double));
     if (!eyes || !cams) { free(eyes); free(cams); return 3; }

@@ -78,10 +78,23 @@ def test_gyroid_sigmoid_reduced(X, integration):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-def test_voxel_scene_reduced(X, integration):
+@pytest.mark.parametrize("path", ["gather", "loads"])
+def test_voxel_scene_reduced(X, integration, path):
     w = W().reduced(W().voxel_blobs(n=64), 128, 6)
-    got, ref = _render_both(X, w, integration)
+    got, ref = _render_both(X, w, integration, volume_path=path)
     _compare(got, ref)
+
+
+def test_voxel_gather_and_loads_agree_non_cubic(X):
+    # non-cubic grid: catches any axis or component-order mix-up in the gathers
+    vol = W().gaussian_blob_volume(40, 12, seed=9)[:24, :40, :31].copy()  # nz=24, nx=40, ny=31
+    angles = [(0.0, 90.0), (63.0, 50.0), (250.0, 130.0)]
+    with X.Scene({"type": "voxel_grid", "volume": 0}, None, [vol]) as s:
+        a = X.render(s, angles, resolution=80, ds=0.01)
+        b = X.render(s, angles, resolution=80, ds=0.01, volume_path="loads")
+    ref = O.render(O.Scene({"type": "voxel_grid", "_voxels": vol}), angles, 80, 0.01)
+    _compare(a, ref)
+    _compare(b, ref)
 
 
 def test_batched_random_scenes(X):

@@ -41,6 +41,7 @@ class XrpVolumeDesc(ctypes.Structure):
 XRP_INTEGRATE_SIMPLE = 0
 XRP_INTEGRATE_HIERARCHICAL = 1
 XRP_FLAG_STATS = 1
+XRP_FLAG_VOLUME_LOADS = 2
 
 # Every symbol include/xrp.h declares, with (restype, argtypes).
 SIGNATURES = {

@@ -51,10 +51,93 @@ static int cuda_fail(int code, const char* what, cudaError_t e) {
 // kernels
 // ---------------------------------------------------------------------------
 
-template <bool HIER, bool VOLUME>
-__global__ void __launch_bounds__(256)
+// Gather of the 2x2 texels around (u, v) from layer `layer` of a 2D layered
+// texture (hand-written tld4; CUDA C++ exposes gather for plain 2D only).
+// With u, v at the centre of a texel quad the footprint is exact; the four
+// values come back unfiltered, in the order (u0,v1), (u1,v1), (u1,v0), (u0,v0).
+__device__ __forceinline__ float4 gather_a2d(cudaTextureObject_t tex, int layer, float u, float v) {
+    float4 r;
+    asm volatile("tld4.r.a2d.v4.f32.f32 {%0, %1, %2, %3}, [%4, {%5, %6, %7, %7}];"
+                 : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+                 : "l"(tex), "r"(layer), "f"(u), "f"(v));
+    return r;
+}
+
+// Voxel-grid sampler reading the 8 taps with two gathers: the grid is a
+// layered texture with one layer per z slice, width ny (j) and height nx (i),
+// point-sampled and clamped to the edge (so x1 = min(x0+1, N-1) as in
+// objects.go:822-830).  Bounds, weights and interpolation are those of vol32.
+struct VolumeTexSampler {
+    const SceneDev& S;
+    const Volume& V;
+    const Ray& r;
+    const VolRay& vr;
+    float inv_scale[3];
+    float band_zero;
+    cudaTextureObject_t tex;
+    __device__ __forceinline__ float f32(float t) const {
+        float ux = fmaf(vr.du[0], t, vr.uc[0]);
+        float uy = fmaf(vr.du[1], t, vr.uc[1]);
+        float uz = fmaf(vr.du[2], t, vr.uc[2]);
+        float nx1 = (float)(V.nx - 1), ny1 = (float)(V.ny - 1), nz1 = (float)(V.nz - 1);
+        float mx = fminf(ux, nx1 - ux) * inv_scale[0];
+        float my = fminf(uy, ny1 - uy) * inv_scale[1];
+        float mz = fminf(uz, nz1 - uz) * inv_scale[2];
+        float m = fminf(mx, fminf(my, mz));
+        float b = V.band_w;
+        if (m < -b) return 0.0f;
+        if (!(m > b)) return xnan();
+        float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+        int x0 = min(max((int)fx, 0), V.nx - 2);
+        int y0 = min(max((int)fy, 0), V.ny - 2);
+        int z0 = min(max((int)fz, 0), V.nz - 2);
+        float wx = ux - (float)x0, wy = uy - (float)y0, wz = uz - (float)z0;
+        float4 g0 = gather_a2d(tex, z0, (float)y0 + 1.0f, (float)x0 + 1.0f);
+        float4 g1 = gather_a2d(tex, z0 + 1, (float)y0 + 1.0f, (float)x0 + 1.0f);
+        float v000 = g0.w, v010 = g0.z, v100 = g0.x, v110 = g0.y;
+        float v001 = g1.w, v011 = g1.z, v101 = g1.x, v111 = g1.y;
+        float v00 = fmaf(wz, v001 - v000, v000);
+        float v01 = fmaf(wz, v011 - v010, v010);
+        float v10 = fmaf(wz, v101 - v100, v100);
+        float v11 = fmaf(wz, v111 - v110, v110);
+        float v0 = fmaf(wy, v01 - v00, v00);
+        float v1 = fmaf(wy, v11 - v10, v10);
+        float v = fmaf(wx, v1 - v0, v0);
+        if (S.hier_zero_guard) {
+            float amax = fmaxf(fmaxf(fmaxf(fabsf(v000), fabsf(v001)), fmaxf(fabsf(v010), fabsf(v011))),
+                               fmaxf(fmaxf(fabsf(v100), fabsf(v101)), fmaxf(fabsf(v110), fabsf(v111))));
+            if (amax > 0.0f && fabsf(v) <= band_zero * amax) return xnan();
+        }
+        return v;
+    }
+    __device__ __forceinline__ double f64(double s) const { return sample64(S, r, s); }
+};
+
+template <bool HIER>
+__device__ __forceinline__ float render_pixel_tex(const SceneDev& S, const Lattice& L,
+                                                  const RenderParams& P, const ViewDev& V, int i,
+                                                  int j, cudaTextureObject_t tex, RayStats& st) {
+    Ray r;
+    setup_ray(V, P, i, j, L.s_c, r);
+    const Volume& vol = S.vols[0];
+    VolRay vr;
+    setup_volray(vol, r, L.s_c, vr);
+    VolumeTexSampler smp{S, vol, r, vr,
+                         {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
+                         S.nodes[S.root].f[0], tex};
+    float acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
+                     : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+    float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+    return expf(-fmaf(w, acc, P.flat_field));
+}
+
+// MODE: 0 general scene, 1 voxel grid through loads, 2 voxel grid through
+// texture gathers.
+template <bool HIER, int MODE>
+__global__ void __launch_bounds__(256, MODE == 0 ? 1 : 4)
     k_render(SceneDev S, Lattice L, RenderParams P, const ViewDev* __restrict__ views, int view0,
-             int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats) {
+             int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats,
+             cudaTextureObject_t tex) {
     const int res = P.res;
     const int tpr = (res + 15) >> 4;
     const int tpv = tpr * tpr;
@@ -67,7 +150,11 @@ __global__ void __launch_bounds__(256)
     const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
     RayStats st{0, 0};
     if (v < nviews && i < res && j < res) {
-        float val = render_pixel<HIER, VOLUME>(S, L, P, views[view0 + v], i, j, st);
+        float val;
+        if constexpr (MODE == 2)
+            val = render_pixel_tex<HIER>(S, L, P, views[view0 + v], i, j, tex, st);
+        else
+            val = render_pixel<HIER, MODE == 1>(S, L, P, views[view0 + v], i, j, st);
         out[((size_t)v * res + i) * res + j] = val;
     }
     if (stats) {  // every lane reaches this point
@@ -196,6 +283,59 @@ struct PoolBuf {
     }
 };
 
+// A voxel grid as a 2D layered texture (layer = z slice, width ny, height
+// nx), point-sampled with clamp-to-edge addressing, for the gather sampler.
+struct LayeredTex {
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    ~LayeredTex() { release(); }
+    void release() {
+        if (tex) cudaDestroyTextureObject(tex);
+        if (arr) cudaFreeArray(arr);
+        tex = 0;
+        arr = nullptr;
+    }
+    // Returns cudaSuccess and leaves tex == 0 when the grid does not fit the
+    // layered-texture limits (the load path is used then).
+    cudaError_t create(const float* data, int nx, int ny, int nz, cudaStream_t st) {
+        release();
+        int dev = 0, mw = 0, mh = 0, ml = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&mw, cudaDevAttrMaxTexture2DLayeredWidth, dev);
+        cudaDeviceGetAttribute(&mh, cudaDevAttrMaxTexture2DLayeredHeight, dev);
+        cudaDeviceGetAttribute(&ml, cudaDevAttrMaxTexture2DLayeredLayers, dev);
+        if (ny > mw || nx > mh || nz > ml || nx < 2 || ny < 2 || nz < 2) return cudaSuccess;
+        cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+        cudaError_t e = cudaMalloc3DArray(&arr, &fd, make_cudaExtent(ny, nx, nz), cudaArrayLayered);
+        if (e != cudaSuccess) { arr = nullptr; return e; }
+        cudaMemcpy3DParms cp;
+        memset(&cp, 0, sizeof(cp));
+        cp.srcPtr = make_cudaPitchedPtr((void*)data, (size_t)ny * sizeof(float), ny, nx);
+        cp.dstArray = arr;
+        cp.extent = make_cudaExtent(ny, nx, nz);
+        cp.kind = cudaMemcpyDefault;
+        if ((e = cudaMemcpy3DAsync(&cp, st)) != cudaSuccess) return e;
+        cudaResourceDesc rd;
+        memset(&rd, 0, sizeof(rd));
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = arr;
+        cudaTextureDesc td;
+        memset(&td, 0, sizeof(td));
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        return cudaCreateTextureObject(&tex, &rd, &td, nullptr);
+    }
+};
+
+// Gathers are the default for voxel-grid roots; XRP_VOLUME_PATH=loads selects
+// the per-tap load path (both give the same results).
+static bool volume_gathers_enabled() {
+    const char* e = getenv("XRP_VOLUME_PATH");
+    return !(e && strcmp(e, "loads") == 0);
+}
+
 // Packs small tables into one upload.
 struct Tables {
     std::vector<unsigned char> host;
@@ -217,6 +357,7 @@ struct Prepared {
     RenderParams P;
     const ViewDev* views = nullptr;
     bool volume_fast = false;
+    cudaTextureObject_t tex = 0;  // layered texture of the root grid (0: use loads)
     bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
 };
 
@@ -224,7 +365,7 @@ struct Prepared {
 int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol_dev,
             const std::vector<const double*>& vol64_dev, const std::vector<ViewDev>& views,
             int res, int integration, double ds, double R, double ff, double dm, double fov_max,
-            cudaStream_t st, PoolBuf& tab, Prepared& out) {
+            cudaStream_t st, PoolBuf& tab, Prepared& out, cudaTextureObject_t tex) {
     HostPrepared hp;
     try {
         hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max);
@@ -269,6 +410,7 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     out.P.xs = (const double*)(base + o_xs);
     out.views = (const ViewDev*)(base + o_views);
     out.volume_fast = hp.volume_fast;
+    out.tex = hp.volume_fast ? tex : 0;
     out.empty = hl.hdr.K <= 0;
     return 0;
 }
@@ -289,17 +431,19 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
     if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
     dim3 grid((unsigned)blocks), block(256);
     bool hier = integration == XRP_INTEGRATE_HIERARCHICAL;
-    if (pr.volume_fast) {
-        if (hier)
-            k_render<true, true><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
-        else
-            k_render<false, true><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+    int mode = pr.volume_fast ? (pr.tex ? 2 : 1) : 0;
+#define XRP_LAUNCH(H, M) \
+    k_render<H, M><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats, pr.tex)
+    if (hier) {
+        if (mode == 2) XRP_LAUNCH(true, 2);
+        else if (mode == 1) XRP_LAUNCH(true, 1);
+        else XRP_LAUNCH(true, 0);
     } else {
-        if (hier)
-            k_render<true, false><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
-        else
-            k_render<false, false><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        if (mode == 2) XRP_LAUNCH(false, 2);
+        else if (mode == 1) XRP_LAUNCH(false, 1);
+        else XRP_LAUNCH(false, 0);
     }
+#undef XRP_LAUNCH
     return cudaGetLastError();
 }
 
@@ -309,13 +453,15 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
 static int render_views(Engine* E, const HostScene& hs, const std::vector<const float*>& vdev,
                         const std::vector<const double*>& v64, const std::vector<ViewDev>& views,
                         const xrp_render_opts& o, double fov_max, float* out, bool out_host,
-                        cudaStream_t st, cudaStream_t st_copy, bool want_stats) {
+                        cudaStream_t st, cudaStream_t st_copy, bool want_stats,
+                        cudaTextureObject_t tex) {
     const int res = o.resolution;
     const int nviews = (int)views.size();
     PoolBuf tab;
     Prepared pr;
     int rc = prepare(E, hs, vdev, v64, views, res, o.integration, o.ds, o.R, o.flat_field,
-                     o.density_multiplier, fov_max, st, tab, pr);
+                     o.density_multiplier, fov_max, st, tab, pr,
+                     (o.flags & XRP_FLAG_VOLUME_LOADS) ? 0 : tex);
     if (rc) return rc;
     unsigned long long* stats = nullptr;
     cudaError_t e;
@@ -406,12 +552,29 @@ struct xrp_scene {
     std::vector<const double*> v64;
     int device = -1;
     double sup_lo[3], sup_hi[3];
+    std::unique_ptr<LayeredTex> tex;  // root voxel grid as a layered texture
+    bool tex_tried = false;
 };
 
 static void scene_free(xrp_scene* s) {
     if (!s) return;
     for (void* p : s->owned) cudaFree(p);
     delete s;
+}
+
+// Builds the layered texture of a voxel-grid root once per scene.
+static int scene_texture(xrp_scene* s, cudaStream_t st) {
+    if (s->tex_tried) return 0;
+    s->tex_tried = true;
+    const HNode& r = s->hs.nodes[s->hs.root];
+    if (r.type != N_VOXEL || !s->hs.defs.empty() || !volume_gathers_enabled()) return 0;
+    const HVolume& v = s->hs.vols[r.vol];
+    auto t = std::make_unique<LayeredTex>();
+    cudaError_t e = t->create(s->vdev[r.vol], v.nx, v.ny, v.nz, st);
+    if (e != cudaSuccess) return cuda_fail(3, "volume texture", e);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(4, "volume texture copy", e);
+    if (t->tex) s->tex = std::move(t);
+    return 0;
 }
 
 static bool opts_ok(const xrp_render_opts* o, std::string& why) {
@@ -544,8 +707,10 @@ int xrp_render(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_rend
     double fov_max;
     std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
     std::lock_guard<std::mutex> g(E->mtx);
+    int rc = scene_texture(s, E->compute);
+    if (rc) return rc;
     return render_views(E, s->hs, s->vdev, s->v64, v, *o, fov_max, out, true, E->compute, E->copy,
-                        (o->flags & XRP_FLAG_STATS) != 0);
+                        (o->flags & XRP_FLAG_STATS) != 0, s->tex ? s->tex->tex : 0);
 }
 
 int xrp_render_device(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_render_opts* o,
@@ -560,9 +725,12 @@ int xrp_render_device(xrp_scene* s, const xrp_camera* views, int nviews, const x
     if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
     double fov_max;
     std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
+    int rc = scene_texture(s, (cudaStream_t)stream);
+    if (rc) return rc;
     // stats use the engine's shared counters and need a synchronisation
     return render_views(E, s->hs, s->vdev, s->v64, v, *o, fov_max, out_device, false,
-                        (cudaStream_t)stream, (cudaStream_t)stream, false);
+                        (cudaStream_t)stream, (cudaStream_t)stream, false,
+                        s->tex ? s->tex->tex : 0);
 }
 
 int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples) {
@@ -600,8 +768,15 @@ int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
     std::lock_guard<std::mutex> g(E->mtx);
     cudaStream_t st = E->compute;
     PoolBuf dvol;
-    cudaError_t e = dvol.alloc(E, nvox * sizeof(float), st);
-    if (e != cudaSuccess) return cuda_fail(3, "volume allocation", e);
+    LayeredTex tex;
+    cudaError_t e;
+    if (volume_gathers_enabled()) {
+        // the gather path reads the grid from the texture only; the FP64
+        // re-evaluation of uncertain samples reads the linear copy below
+        if ((e = tex.create(volume, nx, ny, nz, st)) != cudaSuccess) return cuda_fail(3, "volume texture", e);
+    }
+    if ((e = dvol.alloc(E, nvox * sizeof(float), st)) != cudaSuccess)
+        return cuda_fail(3, "volume allocation", e);
     if ((e = cudaMemcpyAsync(dvol.p, volume, nvox * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return cuda_fail(4, "volume upload", e);
     HostScene hs = volume_scene((const float*)dvol.p, nx, ny, nz);
@@ -632,7 +807,7 @@ int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
         o.flat_field = (double)flat_field;
         o.density_multiplier = 1.0;
         int rc = render_views(E, hs, vdev, v64, views, o, fov_max, out_images + (size_t)c0 * img, true,
-                              st, E->copy, false);
+                              st, E->copy, false, tex.tex);
         if (rc) return rc;
         c0 = c1;
     }

@@ -104,28 +104,36 @@ def camera_arrays(angles, R=4.0, fov=40.0):
     return eyes, mats
 
 
-def _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats):
+def _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats,
+          volume_path="gather"):
     if integration not in ("simple", "hierarchical"):
         raise ValueError(f"Unknown integration method: {integration}")
+    if volume_path not in ("gather", "loads"):
+        raise ValueError(f"Unknown volume path: {volume_path}")
+    flags = (_lib.XRP_FLAG_STATS if stats else 0) | \
+        (_lib.XRP_FLAG_VOLUME_LOADS if volume_path == "loads" else 0)
     return XrpRenderOpts(int(resolution),
                          _lib.XRP_INTEGRATE_HIERARCHICAL if integration == "hierarchical"
                          else _lib.XRP_INTEGRATE_SIMPLE,
                          float(ds), float(R), float(flat_field), float(density_multiplier),
-                         _lib.XRP_FLAG_STATS if stats else 0, 0)
+                         flags, 0)
 
 
 def render(scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, flat_field=0.0,
-           density_multiplier=1.0, integration="simple", out=None, stream=None, stats=False):
+           density_multiplier=1.0, integration="simple", out=None, stream=None, stats=False,
+           volume_path="gather"):
     """Render the views given by ``angles`` ((azimuthal, polar) degrees).
 
     Host path (default): returns a float32 numpy array [views, res, res];
     ``out`` may be a preallocated (ideally pinned) host array.  Device path:
     pass ``out`` as a contiguous float32 CUDA tensor; the work is queued on
     ``stream`` (default: torch's current stream) and the call returns at once.
-    With ``stats`` (host path) returns (images, samples, fp64_samples)."""
+    With ``stats`` (host path) returns (images, samples, fp64_samples).
+    ``volume_path`` picks how a voxel-grid root is read: texture gathers
+    (default) or per-tap loads; both give the same results."""
     L = _lib.load()
     cams, n = cameras_from_angles(angles, R, fov)
-    o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats)
+    o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats, volume_path)
     if out is not None and _is_torch_cuda(out):
         import torch
         if out.dtype != torch.float32 or not out.is_contiguous() or out.numel() < n * resolution ** 2:
