@@ -160,7 +160,7 @@ def cpu_baseline(workload, seconds, threads=None):
 
     n = 2000
     dt = run(n)
-    n2 = int(max(2000, min(5_000_000, n * seconds / max(dt, 1e-3))))
+    n2 = int(max(2000, min(40_000_000, n * seconds / max(dt, 1e-3))))
     dt2 = run(n2)
     return {"value": n2 / dt2 / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
             "sample": f"{n2} seeded random rays of the {len(workload.angles)}x{workload.res}^2 "
