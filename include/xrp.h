@@ -181,6 +181,28 @@ XRP_API int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples);
 /* Frees the device buffers the library caches between calls. */
 XRP_API void xrp_release_cache(void);
 
+/*
+ * RenderVolumeProjectionsCUDA for callers that cannot allocate device
+ * memory (code running under CUDA graph capture, a framework allocator that
+ * owns the device, a fixed memory budget).  No counterpart in the reference
+ * library.  `d_volume` ([z][x][y], float32) and `d_out` (num_cameras*res*res
+ * float32) are device buffers of the caller; `cameras` stay on the host; the
+ * work is queued on `stream` (a cudaStream_t, NULL for the legacy stream) and
+ * the call returns after queuing.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine: its tables go to one static 1 MiB device array that
+ * every GPU loading the library holds until exit.  Limits: the tables of one
+ * call (about 192 B per camera, 8 B per image row and 12 B per sample of
+ * the lattice [R-1.74, R+1.74]) must fit in 1 MiB (code 2 otherwise), and
+ * every camera of a call must share R.  The first call on each device looks
+ * the array up (cudaGetSymbolAddress) and should come before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race:
+ * order them on one stream.  Results equal RenderVolumeProjectionsCUDA's.
+ */
+XRP_API int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, int nz,
+                                      const XRayCameraParams* cameras, int num_cameras,
+                                      int image_res, float ds, float flat_field, float* d_out,
+                                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,8 @@ SIGNATURES = {
     "xrp_render_device": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "xrp_last_stats": (c_int, [c_void_p, c_void_p]),
     "xrp_release_cache": (None, []),
+    "xrp_render_volume_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int,
+                                          c_float, c_float, c_void_p, c_void_p]),
 }
 
 _lib = None

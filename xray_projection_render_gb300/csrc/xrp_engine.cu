@@ -814,6 +814,126 @@ int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
     return 0;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// render without device allocation
+// ---------------------------------------------------------------------------
+//
+// For callers that must not allocate device memory -- code that runs while
+// a CUDA graph is being captured, allocators that own the whole device, or
+// hosts whose memory budget is fixed up front.  The per-call tables (scene
+// image, sample lattice, pixel table, cameras) live in the static array
+// below instead of a stream-ordered pool allocation; the volume and the
+// images are the caller's device buffers.  Every GPU that loads the library
+// reserves this array until the process exits.
+static constexpr size_t kNoAllocScratchBytes = (size_t)1 << 20;  // 1 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mtx;
+static std::map<int, unsigned char*> g_noalloc_addr;  // device -> address of the array
+
+// Device address of the scratch array on the current device, looked up once
+// per device (host code cannot use the symbol itself as a device address).
+static int noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(3, "cudaGetDevice", e);
+    std::lock_guard<std::mutex> g(g_noalloc_mtx);
+    auto it = g_noalloc_addr.find(dev);
+    if (it != g_noalloc_addr.end()) {
+        *out = it->second;
+        return 0;
+    }
+    unsigned char* p = nullptr;
+    e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(3, "scratch symbol address", e);
+    g_noalloc_addr[dev] = p;
+    *out = p;
+    return 0;
+}
+
+extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, int nz,
+                                         const XRayCameraParams* cams, int ncams, int res,
+                                         float ds, float flat_field, float* d_out, void* stream) {
+    if (!d_volume || !cams || !d_out) return fail(1, "null pointer");
+    if (nx <= 0 || ny <= 0 || nz <= 0 || res <= 0 || ncams <= 0) return fail(2, "bad sizes");
+    if (!(ds > 0.0f) || !std::isfinite(ds)) return fail(2, "ds must be > 0 and finite");
+    for (int c = 1; c < ncams; c++)
+        if (cams[c].R != cams[0].R) return fail(2, "all cameras of one call must share R");
+    unsigned char* base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<ViewDev> views(ncams);
+    double fov_max = 0;
+    for (int c = 0; c < ncams; c++) {
+        double eye[3], m[16];
+        for (int a = 0; a < 3; a++) eye[a] = (double)cams[c].eye[a];
+        for (int r = 0; r < 4; r++)
+            for (int k = 0; k < 4; k++) m[k * 4 + r] = (double)cams[c].view[r * 4 + k];
+        view_from_camera(eye, m, (double)cams[c].fov_y, views[c]);
+        fov_max = std::max(fov_max, std::fabs((double)cams[c].fov_y));
+    }
+    HostScene hs = volume_scene(d_volume, nx, ny, nz);
+    HostPrepared hp;
+    try {
+        hp = prepare_host(hs, res, XRP_INTEGRATE_SIMPLE, (double)ds, (double)cams[0].R,
+                          (double)flat_field, 1.0, fov_max);
+    } catch (const std::exception& ex) {
+        return fail(2, "%s", ex.what());
+    }
+    hp.vols[0].data = d_volume;
+    hp.vols[0].data64 = nullptr;
+    const FlatScene& fs = hp.fs;
+    const HostLattice& hl = hp.hl;
+    Tables T;
+    size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
+    size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
+    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs);
+    size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
+    size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
+    if (T.host.size() > kNoAllocScratchBytes)
+        return fail(2, "this call needs %zu bytes of tables; the no-allocation entry point holds "
+                       "at most %zu (fewer cameras, a smaller resolution or a larger ds fit)",
+                    T.host.size(), kNoAllocScratchBytes);
+    // every byte the kernel reads is written here, so nothing needs clearing
+    cudaError_t e = cudaMemcpyAsync(base, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(5, "table upload", e);
+    Prepared pr;
+    pr.S = hp.S;
+    pr.S.nodes = (const Node*)(base + o_nodes);
+    pr.S.nodes64 = (const Node64*)(base + o_n64);
+    pr.S.child = (const int32_t*)(base + o_child);
+    pr.S.cells = (const int32_t*)(base + o_cells);
+    pr.S.items = (const int32_t*)(base + o_items);
+    pr.S.defs = (const DefStep*)(base + o_defs);
+    pr.S.vols = (const Volume*)(base + o_vols);
+    pr.L = hl.hdr;
+    pr.L.s64 = (const double*)(base + o_s64);
+    pr.L.t32 = (const float*)(base + o_t32);
+    pr.L.fstart = (const int32_t*)(base + o_fs);
+    pr.L.f64 = (const double*)(base + o_f64);
+    pr.L.ft32 = (const float*)(base + o_ft32);
+    pr.P = hp.P;
+    pr.P.nviews = ncams;
+    pr.P.xs = (const double*)(base + o_xs);
+    pr.views = (const ViewDev*)(base + o_views);
+    pr.volume_fast = hp.volume_fast;  // per-tap loads: a texture would need an array allocation
+    pr.tex = 0;
+    const int tpv = ((res + 15) / 16) * ((res + 15) / 16);
+    const int per_launch = std::max(1, (int)(0x7fffffffL / tpv));
+    size_t img = (size_t)res * res;
+    for (int v0 = 0; v0 < ncams; v0 += per_launch) {
+        int n = std::min(per_launch, ncams - v0);
+        if ((e = launch(pr, v0, n, XRP_INTEGRATE_SIMPLE, d_out + (size_t)v0 * img, nullptr, st)) != cudaSuccess)
+            return cuda_fail(7, "kernel launch", e);
+    }
+    return 0;
+}
+
+extern "C" {
+
 static int voxelize(const CylinderParams* cyl, int ncyl, int res, float dm, int grid_dim,
                     const int* off, const int* idx, int nidx, float* out, bool spatial) {
     int code = 0;
