@@ -180,7 +180,16 @@ struct Lattice {
     float ds32, dsf32;    // float(ds), float(ds_fine)
     float t_first;        // float(s_0 - s_c)
     float inv_ds;         // 1/ds (FP32, for clipping)
+    float ds_hi, ds_lo;   // ds split so that t_k = t_first + k*(ds_hi + ds_lo)
 };
+
+// FP32 offset of lattice sample k from s_c: t_first + k*ds with ds carried
+// in two parts (error about 3 units of FP32 rounding of |t|, folded into the
+// position error bound on the host).
+XRP_HD float lattice_t(const Lattice& L, int k) {
+    float kf = (float)k;
+    return fmaf(kf, L.ds_hi, fmaf(kf, L.ds_lo, L.t_first));
+}
 
 struct RenderParams {
     int32_t res;
@@ -641,7 +650,7 @@ XRP_HD void deform64(const SceneDev& S, double& x, double& y, double& z) {
 }
 
 // density() without the multiplier (main.go:137-140).
-XRP_HDN double density64(const SceneDev& S, double x, double y, double z) {
+XRP_HD double density64(const SceneDev& S, double x, double y, double z) {
     if (S.ndefs) deform64(S, x, y, z);
     if (S.nodes[S.root].type == N_COLL) return coll64<kMaxDepth>(S, S.root, x, y, z);
     return item64<kMaxDepth>(S, S.root, x, y, z);
@@ -651,16 +660,21 @@ XRP_HDN double density64(const SceneDev& S, double x, double y, double z) {
 // per-ray setup and the two integrators
 // ---------------------------------------------------------------------------
 
+// FP64 ray exactly as the reference forms it (origin = eye, normalised
+// direction), and its FP32 working copy: the point at s_c and the direction.
+struct Ray64 {
+    double o[3];
+    double d[3];
+};
+
 struct Ray {
-    double o[3];   // eye
-    double d[3];   // normalised direction, bit-identical to the reference
     float pc[3];   // float(o + d*s_c)
     float d32[3];  // float(d)
 };
 
 // main.go:457-465 and the Normalize() at main.go:145 / 160.
-XRP_HD void setup_ray(const ViewDev& V, const RenderParams& P, int i, int j, double s_c, Ray& r) {
-    double v0 = P.xs[i], v1 = P.xs[j], v2 = -V.f;
+XRP_HD void setup_ray64(const ViewDev& V, const double* xs, int i, int j, Ray64& r) {
+    double v0 = xs[i], v1 = xs[j], v2 = -V.f;
     const double* m = V.m;
     double t0 = dadd(dadd(dadd(dmul(m[0], v0), dmul(m[4], v1)), dmul(m[8], v2)), dmul(m[12], 1.0));
     double t1 = dadd(dadd(dadd(dmul(m[1], v0), dmul(m[5], v1)), dmul(m[9], v2)), dmul(m[13], 1.0));
@@ -680,19 +694,34 @@ XRP_HD void setup_ray(const ViewDev& V, const RenderParams& P, int i, int j, dou
     r.o[0] = V.eye[0];
     r.o[1] = V.eye[1];
     r.o[2] = V.eye[2];
+}
+
+XRP_HD void setup_ray32(const Ray64& r64, double s_c, Ray& r) {
     for (int a = 0; a < 3; a++) {
-        r.pc[a] = (float)fma(r.d[a], s_c, r.o[a]);
-        r.d32[a] = (float)r.d[a];
+        r.pc[a] = (float)fma(r64.d[a], s_c, r64.o[a]);
+        r.d32[a] = (float)r64.d[a];
     }
 }
 
-// FP64 position of sample s exactly as the reference forms it (main.go:148-150).
-XRP_HD double sample64(const SceneDev& S, const Ray& r, double s) {
+// FP64 density of sample s of pixel (i, j), positions formed exactly as the
+// reference does (main.go:148-150).  The ray is recomputed here so that the
+// FP32 march keeps no FP64 state live.
+XRP_HDN double sample64_pixel(const SceneDev& S, const ViewDev& V, const double* xs, int i, int j,
+                              double s) {
+    Ray64 r;
+    setup_ray64(V, xs, i, j, r);
     double x = dadd(r.o[0], dmul(r.d[0], s));
     double y = dadd(r.o[1], dmul(r.d[1], s));
     double z = dadd(r.o[2], dmul(r.d[2], s));
     return density64(S, x, y, z);
 }
+
+// The pixel a sampler works for, for the FP64 re-evaluation.
+struct PixelRef {
+    const ViewDev* V;
+    const double* xs;
+    int i, j;
+};
 
 // Parameter interval [t0, t1] (offsets from s_c) where the ray is inside the
 // dilated support box; t0 > t1 when it misses.
@@ -748,13 +777,16 @@ struct RayStats {
 struct SceneSampler {
     const SceneDev& S;
     const Ray& r;
+    PixelRef px;
+    static constexpr bool kHasInner = false;
     XRP_HD float f32(float t) const {
         float x = fmaf(r.d32[0], t, r.pc[0]);
         float y = fmaf(r.d32[1], t, r.pc[1]);
         float z = fmaf(r.d32[2], t, r.pc[2]);
         return density32(S, x, y, z);
     }
-    XRP_HD double f64(double s) const { return sample64(S, r, s); }
+    XRP_HD float f32_inner(float t) const { return f32(t); }
+    XRP_HD double f64(double s) const { return sample64_pixel(S, *px.V, px.xs, px.i, px.j, s); }
 };
 
 // A scene whose root is a voxel grid (no deformation): samples are formed
@@ -764,7 +796,7 @@ struct VolRay {
     float du[3];  // float(d * scale)
 };
 
-XRP_HD void setup_volray(const Volume& V, const Ray& r, double s_c, VolRay& vr) {
+XRP_HD void setup_volray(const Volume& V, const Ray64& r, double s_c, VolRay& vr) {
     for (int a = 0; a < 3; a++) {
         double sc = (double)V.scale[a];
         vr.uc[a] = (float)((fma(r.d[a], s_c, r.o[a]) + 1.0) * sc);
@@ -772,27 +804,28 @@ XRP_HD void setup_volray(const Volume& V, const Ray& r, double s_c, VolRay& vr) 
     }
 }
 
-// VoxelGrid.Density in grid coordinates; all dimensions >= 2.
-XRP_HD float vol32(const Volume& V, const float* inv_scale, float band_zero, int zero_guard,
-                   float ux, float uy, float uz) {
-    float nx1 = (float)(V.nx - 1), ny1 = (float)(V.ny - 1), nz1 = (float)(V.nz - 1);
-    // world-space margin to the inclusive [-1, 1] bounds
-    float mx = fminf(ux, nx1 - ux) * inv_scale[0];
-    float my = fminf(uy, ny1 - uy) * inv_scale[1];
-    float mz = fminf(uz, nz1 - uz) * inv_scale[2];
-    float m = fminf(mx, fminf(my, mz));
-    float b = V.band_w;
-    if (m < -b) return 0.0f;
-    if (!(m > b)) return xnan();
+// Trilinear interpolation of the 8 taps (objects.go:847-854), FP32.
+XRP_HD float trilerp(float wx, float wy, float wz, float v000, float v001, float v010, float v011,
+                     float v100, float v101, float v110, float v111) {
+    float v00 = fmaf(wz, v001 - v000, v000);
+    float v01 = fmaf(wz, v011 - v010, v010);
+    float v10 = fmaf(wz, v101 - v100, v100);
+    float v11 = fmaf(wz, v111 - v110, v110);
+    float v0 = fmaf(wy, v01 - v00, v00);
+    float v1 = fmaf(wy, v11 - v10, v10);
+    return fmaf(wx, v1 - v0, v0);
+}
+
+// VoxelGrid.Density in grid coordinates, all dimensions >= 2, for a point
+// known to lie inside [-1,1]^3 with margin (no bounds test).
+XRP_HD float vol32_inner(const Volume& V, float band_zero, int zero_guard, float ux, float uy,
+                         float uz) {
     float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
     int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
-    float wx = ux - fx, wy = uy - fy, wz = uz - fz;
-    x0 = x0 > V.nx - 2 ? V.nx - 2 : x0;
-    y0 = y0 > V.ny - 2 ? V.ny - 2 : y0;
-    z0 = z0 > V.nz - 2 ? V.nz - 2 : z0;
-    x0 = x0 < 0 ? 0 : x0;
-    y0 = y0 < 0 ? 0 : y0;
-    z0 = z0 < 0 ? 0 : z0;
+    x0 = x0 > V.nx - 2 ? V.nx - 2 : (x0 < 0 ? 0 : x0);
+    y0 = y0 > V.ny - 2 ? V.ny - 2 : (y0 < 0 ? 0 : y0);
+    z0 = z0 > V.nz - 2 ? V.nz - 2 : (z0 < 0 ? 0 : z0);
+    float wx = ux - (float)x0, wy = uy - (float)y0, wz = uz - (float)z0;
     long NY = V.ny, NXY = (long)V.nx * V.ny;
     const float* p0 = V.data + z0 * NXY + x0 * NY + y0;
     const float* p1 = p0 + NXY;
@@ -803,13 +836,7 @@ XRP_HD float vol32(const Volume& V, const float* inv_scale, float band_zero, int
     float v000 = p0[0], v010 = p0[1], v100 = p0[NY], v110 = p0[NY + 1];
     float v001 = p1[0], v011 = p1[1], v101 = p1[NY], v111 = p1[NY + 1];
 #endif
-    float v00 = fmaf(wz, v001 - v000, v000);
-    float v01 = fmaf(wz, v011 - v010, v010);
-    float v10 = fmaf(wz, v101 - v100, v100);
-    float v11 = fmaf(wz, v111 - v110, v110);
-    float v0 = fmaf(wy, v01 - v00, v00);
-    float v1 = fmaf(wy, v11 - v10, v10);
-    float v = fmaf(wx, v1 - v0, v0);
+    float v = trilerp(wx, wy, wz, v000, v001, v010, v011, v100, v101, v110, v111);
     if (zero_guard) {
         float amax = fmaxf(fmaxf(fmaxf(fabsf(v000), fabsf(v001)), fmaxf(fabsf(v010), fabsf(v011))),
                            fmaxf(fmaxf(fabsf(v100), fabsf(v101)), fmaxf(fabsf(v110), fabsf(v111))));
@@ -818,39 +845,111 @@ XRP_HD float vol32(const Volume& V, const float* inv_scale, float band_zero, int
     return v;
 }
 
+// World-space margin of grid point u to the inclusive [-1, 1]^3 bounds
+// compared with the guard band: 0 outside, 1 inside, 2 uncertain.
+XRP_HD int vol_bounds(const Volume& V, const float* inv_scale, float ux, float uy, float uz) {
+    float mx = fminf(ux, (float)(V.nx - 1) - ux) * inv_scale[0];
+    float my = fminf(uy, (float)(V.ny - 1) - uy) * inv_scale[1];
+    float mz = fminf(uz, (float)(V.nz - 1) - uz) * inv_scale[2];
+    float m = fminf(mx, fminf(my, mz));
+    if (m < -V.band_w) return 0;
+    if (m > V.band_w) return 1;
+    return 2;
+}
+
+// VoxelGrid.Density in grid coordinates; all dimensions >= 2.
+XRP_HD float vol32(const Volume& V, const float* inv_scale, float band_zero, int zero_guard,
+                   float ux, float uy, float uz) {
+    int b = vol_bounds(V, inv_scale, ux, uy, uz);
+    if (b == 0) return 0.0f;
+    if (b == 2) return xnan();
+    return vol32_inner(V, band_zero, zero_guard, ux, uy, uz);
+}
+
 struct VolumeSampler {
     const SceneDev& S;
     const Volume& V;
-    const Ray& r;
     const VolRay& vr;
+    PixelRef px;
     float inv_scale[3];
     float band_zero;
+    static constexpr bool kHasInner = true;
     XRP_HD float f32(float t) const {
         return vol32(V, inv_scale, band_zero, S.hier_zero_guard, fmaf(vr.du[0], t, vr.uc[0]),
                      fmaf(vr.du[1], t, vr.uc[1]), fmaf(vr.du[2], t, vr.uc[2]));
     }
-    XRP_HD double f64(double s) const { return sample64(S, r, s); }
+    XRP_HD float f32_inner(float t) const {
+        return vol32_inner(V, band_zero, S.hier_zero_guard, fmaf(vr.du[0], t, vr.uc[0]),
+                           fmaf(vr.du[1], t, vr.uc[1]), fmaf(vr.du[2], t, vr.uc[2]));
+    }
+    XRP_HD double f64(double s) const { return sample64_pixel(S, *px.V, px.xs, px.i, px.j, s); }
 };
 
-// integrate_along_ray (main.go:144-154): returns the sum of densities over
-// the lattice samples (pre-multiplier, pre-ds).
-template <class Sampler>
-XRP_HD float march_simple(const Lattice& L, const float* lo, const float* hi, const Ray& r,
-                          const Sampler& smp, RayStats& st) {
+// Sample range [a, b] that lies inside the box [lo+m, hi-m] (m > guard band
+// plus the FP32 error of the clip itself): there the bounds test of the
+// sampler always passes and is skipped.  Empty (a > b) when there is none.
+XRP_HD void inner_range(const Lattice& L, const Ray& r, const float* lo, const float* hi, float m,
+                        int k0, int k1, int& a, int& b) {
+    float ilo[3] = {lo[0] + m, lo[1] + m, lo[2] + m};
+    float ihi[3] = {hi[0] - m, hi[1] - m, hi[2] - m};
     float t0, t1;
-    clip_ray(lo, hi, r, t0, t1);
-    int k0, k1;
-    KahanF acc;
-    if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
+    clip_ray(ilo, ihi, r, t0, t1);
+    a = k1 + 1;
+    b = k1;
+    if (!(t0 < t1)) return;
+    float fa = (t0 - L.t_first) * L.inv_ds, fb = (t1 - L.t_first) * L.inv_ds;
+    fa = fmaxf(fa, (float)k0 - 4.0f);
+    fb = fminf(fb, (float)k1 + 4.0f);
+    a = (int)ceilf(fa) + 2;
+    b = (int)floorf(fb) - 2;
+    if (a < k0) a = k0;
+    if (b > k1) b = k1;
+}
+
+// integrate_along_ray (main.go:144-154): returns the sum of densities over
+// the lattice samples (pre-multiplier, pre-ds).  With `in_lo <= in_hi` the
+// samples in [in_lo, in_hi] skip the sampler's bounds test.
+template <class Sampler>
+XRP_HD float march_range(const Lattice& L, const Sampler& smp, int k0, int k1, KahanF& acc,
+                         RayStats& st) {
     for (int k = k0; k <= k1; k++) {
-        float rho = smp.f32(L.t32[k]);
+        float rho = smp.f32(lattice_t(L, k));
         if (isunc(rho)) {
             rho = (float)smp.f64(L.s64[k]);
             st.fallbacks++;
         }
         acc.add(rho);
     }
+    return acc.s;
+}
+
+template <class Sampler>
+XRP_HD float march_simple(const Lattice& L, const float* lo, const float* hi, const Ray& r,
+                          const Sampler& smp, RayStats& st, float inner_margin = 0.0f) {
+    float t0, t1;
+    clip_ray(lo, hi, r, t0, t1);
+    int k0, k1;
+    KahanF acc;
+    if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
     st.samples += (uint32_t)(k1 - k0 + 1);
+    if constexpr (Sampler::kHasInner) {
+        int a, b;
+        inner_range(L, r, lo, hi, inner_margin, k0, k1, a, b);
+        if (a <= b) {
+            march_range(L, smp, k0, a - 1, acc, st);
+            for (int k = a; k <= b; k++) {
+                float rho = smp.f32_inner(lattice_t(L, k));
+                if (isunc(rho)) {
+                    rho = (float)smp.f64(L.s64[k]);
+                    st.fallbacks++;
+                }
+                acc.add(rho);
+            }
+            march_range(L, smp, b + 1, k1, acc, st);
+            return acc.s;
+        }
+    }
+    march_range(L, smp, k0, k1, acc, st);
     return acc.s;
 }
 
@@ -866,7 +965,7 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
     if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
     bool prev_zero = true;  // coarse samples before k0 are outside the support
     for (int k = k0; k <= k1; k++) {
-        float rho = smp.f32(L.t32[k]);
+        float rho = smp.f32(lattice_t(L, k));
         if (isunc(rho)) {
             rho = (float)smp.f64(L.s64[k]);
             st.fallbacks++;
@@ -899,18 +998,29 @@ template <bool HIER, bool VOLUME>
 XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P,
                           const ViewDev& V, int i, int j, RayStats& st) {
     Ray r;
-    setup_ray(V, P, i, j, L.s_c, r);
     float acc;
+    PixelRef px{&V, P.xs, i, j};
     if constexpr (VOLUME) {
         const Volume& vol = S.vols[0];
         VolRay vr;
-        setup_volray(vol, r, L.s_c, vr);
-        VolumeSampler smp{S, vol, r, vr, {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
+        {
+            Ray64 r64;
+            setup_ray64(V, P.xs, i, j, r64);
+            setup_ray32(r64, L.s_c, r);
+            setup_volray(vol, r64, L.s_c, vr);
+        }
+        VolumeSampler smp{S, vol, vr, px,
+                          {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
                           S.nodes[S.root].f[0]};
         acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
-                   : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+                   : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st, 4.0f * vol.band_w + 2e-4f);
     } else {
-        SceneSampler smp{S, r};
+        {
+            Ray64 r64;
+            setup_ray64(V, P.xs, i, j, r64);
+            setup_ray32(r64, L.s_c, r);
+        }
+        SceneSampler smp{S, r, px};
         acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
                    : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
     }

@@ -70,72 +70,84 @@ __device__ __forceinline__ float4 gather_a2d(cudaTextureObject_t tex, int layer,
 struct VolumeTexSampler {
     const SceneDev& S;
     const Volume& V;
-    const Ray& r;
     const VolRay& vr;
+    PixelRef px;
     float inv_scale[3];
     float band_zero;
     cudaTextureObject_t tex;
-    __device__ __forceinline__ float f32(float t) const {
-        float ux = fmaf(vr.du[0], t, vr.uc[0]);
-        float uy = fmaf(vr.du[1], t, vr.uc[1]);
-        float uz = fmaf(vr.du[2], t, vr.uc[2]);
-        float nx1 = (float)(V.nx - 1), ny1 = (float)(V.ny - 1), nz1 = (float)(V.nz - 1);
-        float mx = fminf(ux, nx1 - ux) * inv_scale[0];
-        float my = fminf(uy, ny1 - uy) * inv_scale[1];
-        float mz = fminf(uz, nz1 - uz) * inv_scale[2];
-        float m = fminf(mx, fminf(my, mz));
-        float b = V.band_w;
-        if (m < -b) return 0.0f;
-        if (!(m > b)) return xnan();
+    static constexpr bool kHasInner = true;
+    __device__ __forceinline__ float inner(float ux, float uy, float uz) const {
         float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
         int x0 = min(max((int)fx, 0), V.nx - 2);
         int y0 = min(max((int)fy, 0), V.ny - 2);
         int z0 = min(max((int)fz, 0), V.nz - 2);
         float wx = ux - (float)x0, wy = uy - (float)y0, wz = uz - (float)z0;
-        float4 g0 = gather_a2d(tex, z0, (float)y0 + 1.0f, (float)x0 + 1.0f);
-        float4 g1 = gather_a2d(tex, z0 + 1, (float)y0 + 1.0f, (float)x0 + 1.0f);
-        float v000 = g0.w, v010 = g0.z, v100 = g0.x, v110 = g0.y;
-        float v001 = g1.w, v011 = g1.z, v101 = g1.x, v111 = g1.y;
-        float v00 = fmaf(wz, v001 - v000, v000);
-        float v01 = fmaf(wz, v011 - v010, v010);
-        float v10 = fmaf(wz, v101 - v100, v100);
-        float v11 = fmaf(wz, v111 - v110, v110);
-        float v0 = fmaf(wy, v01 - v00, v00);
-        float v1 = fmaf(wy, v11 - v10, v10);
-        float v = fmaf(wx, v1 - v0, v0);
+        float gu = (float)y0 + 1.0f, gv = (float)x0 + 1.0f;
+        float4 g0 = gather_a2d(tex, z0, gu, gv);
+        float4 g1 = gather_a2d(tex, z0 + 1, gu, gv);
+        float v = trilerp(wx, wy, wz, g0.w, g1.w, g0.z, g1.z, g0.x, g1.x, g0.y, g1.y);
         if (S.hier_zero_guard) {
-            float amax = fmaxf(fmaxf(fmaxf(fabsf(v000), fabsf(v001)), fmaxf(fabsf(v010), fabsf(v011))),
-                               fmaxf(fmaxf(fabsf(v100), fabsf(v101)), fmaxf(fabsf(v110), fabsf(v111))));
+            float amax = fmaxf(fmaxf(fmaxf(fabsf(g0.x), fabsf(g0.y)), fmaxf(fabsf(g0.z), fabsf(g0.w))),
+                               fmaxf(fmaxf(fabsf(g1.x), fabsf(g1.y)), fmaxf(fabsf(g1.z), fabsf(g1.w))));
             if (amax > 0.0f && fabsf(v) <= band_zero * amax) return xnan();
         }
         return v;
     }
-    __device__ __forceinline__ double f64(double s) const { return sample64(S, r, s); }
+    __device__ __forceinline__ float f32(float t) const {
+        float ux = fmaf(vr.du[0], t, vr.uc[0]);
+        float uy = fmaf(vr.du[1], t, vr.uc[1]);
+        float uz = fmaf(vr.du[2], t, vr.uc[2]);
+        int b = vol_bounds(V, inv_scale, ux, uy, uz);
+        if (b == 0) return 0.0f;
+        if (b == 2) return xnan();
+        return inner(ux, uy, uz);
+    }
+    __device__ __forceinline__ float f32_inner(float t) const {
+        return inner(fmaf(vr.du[0], t, vr.uc[0]), fmaf(vr.du[1], t, vr.uc[1]),
+                     fmaf(vr.du[2], t, vr.uc[2]));
+    }
+    __device__ __forceinline__ double f64(double s) const {
+        return sample64_pixel(S, *px.V, px.xs, px.i, px.j, s);
+    }
 };
 
 template <bool HIER>
 __device__ __forceinline__ float render_pixel_tex(const SceneDev& S, const Lattice& L,
                                                   const RenderParams& P, const ViewDev& V, int i,
                                                   int j, cudaTextureObject_t tex, RayStats& st) {
-    Ray r;
-    setup_ray(V, P, i, j, L.s_c, r);
     const Volume& vol = S.vols[0];
+    Ray r;
     VolRay vr;
-    setup_volray(vol, r, L.s_c, vr);
-    VolumeTexSampler smp{S, vol, r, vr,
+    {
+        Ray64 r64;
+        setup_ray64(V, P.xs, i, j, r64);
+        setup_ray32(r64, L.s_c, r);
+        setup_volray(vol, r64, L.s_c, vr);
+    }
+    VolumeTexSampler smp{S, vol, vr, PixelRef{&V, P.xs, i, j},
                          {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
                          S.nodes[S.root].f[0], tex};
     float acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
-                     : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+                     : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st, 4.0f * vol.band_w + 2e-4f);
     float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
     return expf(-fmaf(w, acc, P.flat_field));
 }
 
+// Minimum resident blocks per SM asked of the compiler (register budget):
+// tuned on GB300 for the voxel-grid and the general-scene kernels.
+#ifndef XRP_VOLUME_MIN_BLOCKS
+#define XRP_VOLUME_MIN_BLOCKS 4
+#endif
+#ifndef XRP_SCENE_MIN_BLOCKS
+#define XRP_SCENE_MIN_BLOCKS 2
+#endif
+
 // MODE: 0 general scene, 1 voxel grid through loads, 2 voxel grid through
 // texture gathers.
 template <bool HIER, int MODE>
-__global__ void __launch_bounds__(256, MODE == 0 ? 1 : 4)
-    k_render(SceneDev S, Lattice L, RenderParams P, const ViewDev* __restrict__ views, int view0,
+__global__ void __launch_bounds__(256, MODE == 0 ? XRP_SCENE_MIN_BLOCKS : XRP_VOLUME_MIN_BLOCKS)
+    k_render(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
+             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
              int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats,
              cudaTextureObject_t tex) {
     const int res = P.res;

@@ -996,7 +996,9 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
     double T = g.half_span + 1e-3;
     // magnitude of sample points: the support box if bounded, else the span
     double Pspan = std::fabs(g.R) + T + Pc;
-    double E0 = kSafety * kU * (Pc + 2 * T + Pspan) + 1e-12;
+    // rounding of p_c, of the direction (times |t|), of the offset t (three
+    // roundings, lattice_t) and of the final fma
+    double E0 = kSafety * kU * (Pc + 4 * T + Pspan) + 1e-12;
     double E = E0, P = Pspan;
     for (auto& d : hs.defs) {
         E = def_error(d, E, P);
@@ -1220,6 +1222,8 @@ HostLattice build_lattice(double R, double ds, bool hierarchical) {
     L.hdr.smin = smin;
     L.hdr.t_first = L.t32.empty() ? 0.0f : L.t32[0];
     L.hdr.inv_ds = (float)(1.0 / ds);
+    L.hdr.ds_hi = (float)ds;
+    L.hdr.ds_lo = (float)(ds - (double)L.hdr.ds_hi);
     return L;
 }
 
