@@ -46,8 +46,10 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--views", type=int, default=180)
-    p.add_argument("--res", type=int, default=1024)
+    p.add_argument("--workload", default="voxel", choices=["voxel", "cube", "lattice", "gyroid"],
+                   help="voxel (default, the headline) or one of the analytic scenes")
+    p.add_argument("--views", type=int, default=0, help="view count (0: the workload's)")
+    p.add_argument("--res", type=int, default=0, help="resolution (0: the workload's)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer ABI timing")
@@ -146,16 +148,26 @@ def cpu_baseline(workload, seconds, threads=None):
     """FP64 oracle on a seeded subset of the workload's rays, all host cores."""
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
-    from xray_projection_render_gb300 import engine  # camera rows only (host code)
-    cams21 = engine.xray_camera_params(workload.angles, workload.R, workload.fov)
-    scene = O.VolumeABIScene(workload.volume)
     rng = np.random.default_rng(1234)
+    if workload.volume is not None:
+        from xray_projection_render_gb300 import engine  # camera rows only (host code)
+        cams21 = engine.xray_camera_params(workload.angles, workload.R, workload.fov)
+        scene = O.VolumeABIScene(workload.volume)
+
+        def render(rays):
+            scene.render_rays(cams21, workload.res, np.float32(workload.ds), rays, nthreads=threads)
+    else:
+        scene = O.Scene(workload.obj, workload.deformation)
+
+        def render(rays):
+            O.render(scene, workload.angles, workload.res, workload.ds, R=workload.R,
+                     fov=workload.fov, rays=rays, nthreads=threads)
 
     def run(n):
         rays = np.stack([rng.integers(0, len(workload.angles), n), rng.integers(0, workload.res, n),
                          rng.integers(0, workload.res, n)], 1).astype(np.int32)
         t = time.perf_counter()
-        scene.render_rays(cams21, workload.res, np.float32(workload.ds), rays, nthreads=threads)
+        render(rays)
         return time.perf_counter() - t
 
     n = 2000
@@ -163,8 +175,7 @@ def cpu_baseline(workload, seconds, threads=None):
     n2 = int(max(2000, min(40_000_000, n * seconds / max(dt, 1e-3))))
     dt2 = run(n2)
     return {"value": n2 / dt2 / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{n2} seeded random rays of the {len(workload.angles)}x{workload.res}^2 "
-                      f"voxel workload ({dt2:.1f} s)"}
+            "sample": f"{n2} seeded random rays of {workload.name} ({dt2:.1f} s)"}
 
 
 def run_reference(args):
@@ -172,7 +183,7 @@ def run_reference(args):
     if rank != 0:
         return
     from xray_projection_render_gb300 import workloads as W
-    w = W.voxel_blobs(args.res, args.views)
+    w = make_workload(args.workload, W, args.views, args.res)
     vals = []
     for i in range(args.warmup + args.steps):
         cb = cpu_baseline(w, max(2.0, args.cpu_seconds / max(1, args.steps)))
@@ -180,7 +191,9 @@ def run_reference(args):
             vals.append(cb["value"])
     v = float(np.median(vals))
     cb["value"] = v
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s",
+    line = {"impl": "reference",
+            "metric": METRIC if args.workload == "voxel" else f"Mrays/s on 1 GB300 ({w.name})",
+            "value": v, "unit": "Mrays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
@@ -188,6 +201,32 @@ def run_reference(args):
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# Algorithmic FP32 work per evaluated sample (FMA = 2), from the per-item
+# table of the benchmark definitions: common 8 + object terms.
+FLOPS = {
+    "voxel": 58,     # 50 trilinear
+    "cube": 54,      # sphere 9 + box 9 + cylinder 23 + collection 3 + clip 2
+    "lattice": 437,  # linear deformation 18 + fold/bounds 27 + 16 cylinders x 23 + 16
+    "gyroid": 53,    # gyroid 13 (+6 SFU) + sigmoid 5 (+2 SFU) + fold/bounds 27
+}
+
+
+def make_workload(name, W, views, res):
+    if name == "voxel":
+        return W.voxel_blobs(res or 1024, views or 180)
+    if name == "cube":
+        w = W.cube_minus_sphere_cylinder(res or 512)
+    elif name == "lattice":
+        w = W.deformed_lattice(res or 1024, 360)
+    elif name == "gyroid":
+        w = W.gyroid_sigmoid(res or 2048, 720)
+    else:
+        raise ValueError(name)
+    if views:
+        w = W.reduced(w, w.res, views)
+    return w
 
 
 def main():
@@ -205,30 +244,30 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     G.build()
-    w = W.voxel_blobs(args.res, args.views)
+    w = make_workload(args.workload, W, args.views, args.res)
+    is_voxel = w.volume is not None
     my_angles = w.angles[rank::world]
     n_my = len(my_angles)
     res = w.res
     img = res * res
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
-    vol_dev = torch.from_numpy(w.volume).to(dev)
-    scene = X.Scene(w.obj, None, [vol_dev])
+    vols = [torch.from_numpy(w.volume).to(dev)] if is_voxel else []
+    scene = X.Scene(w.obj, w.deformation, vols)
     out = torch.empty((n_my, res, res), device=dev, dtype=torch.float32)
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)  # 256 MiB > L2
+    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov, volume_path=args.volume_path)
 
     def step():
-        X.render(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, out=out,
-                 stream=stream, volume_path=args.volume_path)
+        X.render(scene, my_angles, out=out, stream=stream, **kw)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    # exact sample count of one step (counter pass, untimed)
-    _, samples, fp64 = X.render(scene, my_angles[:max(1, min(8, n_my))], resolution=res, ds=w.ds,
-                                R=w.R, fov=w.fov, stats=True, volume_path=args.volume_path)
-    frac = min(8, n_my) / n_my
-    samples_step = samples / frac
+    # exact sample count of one step (counter pass, untimed, on a view subset)
+    nstat = max(1, min(8, n_my))
+    _, samples, fp64 = X.render(scene, my_angles[:nstat], stats=True, **kw)
+    samples_step = samples * n_my / nstat
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -250,21 +289,36 @@ def main():
     rays_total = len(w.angles) * img
     value = rays_total / t_step / 1e6
 
-    # end to end through the reference ABI with pinned host buffers
-    cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
-    if args.no_e2e:
-        e2e_times = [float("nan")]
+    # end to end through the host-facing C ABI, pinned host buffers, inputs
+    # uploaded and images read back inside the timed region
+    e2e_times = []
+    out_host = None if args.no_e2e else torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
+    if is_voxel:
+        cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
+        h2d = int(w.volume.nbytes + cams21.nbytes)
+        path = "RenderVolumeProjectionsCUDA, pinned host buffers"
+        if not args.no_e2e:
+            vol_host = torch.from_numpy(w.volume).pin_memory()
+
+        def e2e_call():
+            X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
     else:
-        e2e_times = []
-        vol_host = torch.from_numpy(w.volume).pin_memory()
-        out_host = torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
-        X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)  # warm
-    for _ in range(0 if args.no_e2e else max(1, min(args.steps, 3))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
-        e2e_times.append(time.perf_counter() - t0)
-    t_e2e = float(np.mean(e2e_times))
+        obj_json = json.dumps(w.obj)
+        def_json = json.dumps(w.deformation) if w.deformation else None
+        h2d = len(obj_json) + (len(def_json) if def_json else 0) + n_my * 192
+        path = "xrp_scene_create + xrp_render, pinned host output"
+
+        def e2e_call():
+            with X.Scene(obj_json, def_json) as s2:
+                X.render(s2, my_angles, out=out_host, **kw)
+    if not args.no_e2e:
+        e2e_call()  # warm
+        for _ in range(max(1, min(args.steps, 3))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_call()
+            e2e_times.append(time.perf_counter() - t0)
+    t_e2e = float(np.mean(e2e_times)) if e2e_times else float("nan")
     if world > 1:
         t = torch.tensor([t_e2e], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -273,26 +327,26 @@ def main():
 
     peaks = measured_peaks()
     fp32_peak = fp32_peak_tflops(torch)
-    achieved = samples_step * FLOPS_PER_SAMPLE / t_step / 1e12
+    fps = FLOPS[args.workload]
+    achieved = samples_step * fps / t_step / 1e12
     line = {
-        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC if args.workload == "voxel" else f"Mrays/s on 1 GB300 ({w.name})",
+        "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded Gaussian-blob grid)",
+        "data": "synthetic (seeded)",
         "config": {"workload": w.name, "views": len(w.angles), "res": res, "ds": w.ds,
-                   "grid": [256, 256, 256], "integrator": "simple", "R": w.R, "fov": w.fov,
+                   "integrator": "simple", "R": w.R, "fov": w.fov,
                    "l2": "flushed before every timed step (256 MiB write)",
-                   "volume_path": args.volume_path,
+                   "volume_path": args.volume_path if is_voxel else None,
                    "parallelism": f"views k mod {world}"},
-        "e2e": {"value": e2e_value, "unit": "Mrays/s",
-                "h2d_bytes_per_step": int(w.volume.nbytes + cams21.nbytes),
-                "d2h_bytes_per_step": int(n_my * img * 4),
-                "path": "RenderVolumeProjectionsCUDA, pinned host buffers"},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
         "gpu_launches": args.steps,  # one render launch per step (all views)
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                      "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
-                     "samples_per_step": samples_step, "flops_per_sample": FLOPS_PER_SAMPLE,
+                     "samples_per_step": samples_step, "flops_per_sample": fps,
                      "fp64_fallback_fraction": fp64 / max(samples, 1),
                      "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
         "clocks": clk.summary(),

@@ -1,0 +1,118 @@
+"""The engine's per-pixel code, built for the CPU (tests/hostsim), against
+the FP64 oracle.
+
+The same source runs in the CUDA kernels; on the CPU it checks, without a
+GPU, the scene flattening, the guard bands that decide each predicate in
+FP32, the FP64 re-evaluation of uncertain samples, the lattices and both
+integrators.  Tolerance: 1e-5 relative on transmittance."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "hostsim"))
+import hostsim  # noqa: E402
+
+from xray_projection_render_gb300 import workloads as W  # noqa: E402
+
+REL_TOL = 1e-5
+
+
+def cams_of(w):
+    eyes, cams = O.cameras(w.angles, w.R)
+    return np.concatenate([eyes, cams, np.full((len(w.angles), 1), w.fov)], axis=1)
+
+
+def check(w, integration="simple", nrays=2500, seed=0, **kw):
+    rng = np.random.default_rng(seed)
+    rays = np.stack([rng.integers(0, len(w.angles), nrays), rng.integers(0, w.res, nrays),
+                     rng.integers(0, w.res, nrays)], 1).astype(np.int32)
+    obj = {"type": "voxel_grid", "_voxels": w.volume} if w.volume is not None else w.obj
+    ref = O.render(O.Scene(obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                   integration=integration, rays=rays,
+                   density_multiplier=kw.get("density_multiplier", 1.0),
+                   flat_field=kw.get("flat_field", 0.0))
+    got, st = hostsim.render(w.obj, cams_of(w), w.res, w.ds, deformation=w.deformation,
+                             volume=w.volume, R=w.R, integration=integration, rays=rays, **kw)
+    rel = np.abs(got - ref) / ref
+    assert rel.max() <= REL_TOL, f"{w.name}: max rel error {rel.max():.3g}"
+    return st
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_config1(integration):
+    st = check(W.cube_minus_sphere_cylinder(256), integration)
+    assert st[1] < 0.01 * st[0]
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_deformed_lattice(integration):
+    st = check(W.reduced(W.deformed_lattice(), 256, 6), integration)
+    assert st[1] < 0.02 * st[0]
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_gyroid_sigmoid(integration):
+    check(W.reduced(W.gyroid_sigmoid(), 256, 6), integration)
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+@pytest.mark.parametrize("general", [False, True])
+def test_voxel(integration, general):
+    w = W.reduced(W.voxel_blobs(n=48), 192, 6)
+    check(w, integration, force_general=general)
+
+
+def test_batched_scenes():
+    for w in W.batched_scenes(10):
+        check(W.reduced(w, 128, 3), nrays=800)
+
+
+def test_multiplier_and_flat_field():
+    w = W.cube_minus_sphere_cylinder(128)
+    check(w, density_multiplier=1.7, flat_field=0.4)
+    check(w, "hierarchical", density_multiplier=1.7, flat_field=0.4)
+
+
+def test_every_primitive_under_every_deformation():
+    prims = [
+        {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+        {"type": "box", "center": [0.0, 0.2, 0.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5},
+        {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+        {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+         "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9},
+        {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0},
+    ]
+    defs = [None,
+            {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02], "sigmas": [0.3, 0.3, 0.5],
+             "centers": [0.0, 0.1, 0.0]},
+            {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]},
+            {"type": "rigid", "displacements": [0.05, -0.1, 0.02]},
+            {"type": "sigmoid", "amplitude": 0.2, "center": 0.0, "lengthscale": 0.2,
+             "direction": "y"},
+            {"type": "affine", "matrix": [[1.1, 0.0, 0.1], [0.0, 0.9, 0.0], [0.05, 0.0, 1.0]]}]
+    for p in prims:
+        for d in defs:
+            check(W.Workload("p", p, d, [(10.0, 80.0), (200.0, 120.0)], 64, 0.01), nrays=600)
+    coll = {"type": "object_collection", "objects": prims}
+    for d in defs:
+        w = W.Workload("c", coll, d, [(10.0, 80.0), (200.0, 120.0)], 64, 0.01)
+        check(w, nrays=600)
+        check(w, "hierarchical", nrays=600)
+
+
+def test_greedy_sum_and_cancellation():
+    # 0.7 + 0.3 - 1.0 is not exact in FP32: the cancellation guard must hand
+    # such samples to FP64 so the hierarchical zero test agrees
+    coll = {"type": "object_collection", "objects": [
+        {"type": "sphere", "center": [0, 0, 0], "radius": 0.5, "rho": 0.7},
+        {"type": "sphere", "center": [0.1, 0, 0], "radius": 0.5, "rho": 0.3},
+        {"type": "sphere", "center": [0, 0.1, 0], "radius": 0.45, "rho": -1.0}]}
+    for greedy in (False, True):
+        c = dict(coll, greedy_dens_eval=greedy)
+        w = W.Workload("g", c, None, [(0.0, 90.0), (70.0, 60.0)], 96, 0.004)
+        check(w)
+        check(w, "hierarchical")

@@ -649,6 +649,105 @@ XRP_HD void deform64(const SceneDev& S, double& x, double& y, double& z) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// hybrid exact evaluation for uncertain samples
+// ---------------------------------------------------------------------------
+// The position pipeline (sample position, deformation, tessellation bounds
+// and folds) runs in FP64 exactly as the reference does; each primitive is
+// then first decided in FP32 at that FP64 point -- its guard band was sized
+// for the much larger FP32 march error, so a certain FP32 decision equals the
+// FP64 one -- and only primitives that stay undecided are evaluated in FP64.
+// The value returned is the same as density64's, for a fraction of the FP64
+// work (GB300 runs FP64 at a small fraction of its FP32 rate).
+
+XRP_HD double leaf_rho64(const SceneDev& S, int id) {
+    const double* d = S.nodes64[id].d;
+    switch (S.nodes[id].type) {
+    case N_SPHERE: return d[4];
+    case N_BOX: return d[6];
+    case N_CYL: return d[7];
+    case N_PPD: return d[12];
+    case N_GYROID: return d[5];
+    default: return 0.0;
+    }
+}
+
+XRP_HD double leaf_hyb(const SceneDev& S, int id, double x, double y, double z) {
+    float r = leaf32(S.nodes[id], (float)x, (float)y, (float)z);
+    if (!isunc(r)) return r != 0.0f ? leaf_rho64(S, id) : 0.0;
+    return leaf64(S, id, x, y, z);
+}
+
+template <int D>
+XRP_HD double coll_hyb(const SceneDev& S, int id, double x, double y, double z);
+
+template <int D>
+XRP_HD double item_hyb(const SceneDev& S, int id, double x, double y, double z) {
+    const Node& n = S.nodes[id];
+    if (n.type <= N_GYROID) return leaf_hyb(S, id, x, y, z);
+    if (n.type == N_VOXEL) return voxel64(S.vols[n.a], x, y, z);
+    if (n.type == N_TESS) {
+        if constexpr (D > 0) {
+            const double* t = S.nodes64[id].d;
+            if (x < t[0] || x > t[1] || y < t[2] || y > t[3] || z < t[4] || z > t[5]) return 0.0;
+            const double* u = &t[6];
+            double dx = dsub(u[1], u[0]);
+            x = dsub(x, dmul(dx, floor(ddiv(dsub(x, u[0]), dx))));
+            double dy = dsub(u[3], u[2]);
+            y = dsub(y, dmul(dy, floor(ddiv(dsub(y, u[2]), dy))));
+            double dz = dsub(u[5], u[4]);
+            z = dsub(z, dmul(dz, floor(ddiv(dsub(z, u[4]), dz))));
+            if (x < u[0] || x > u[1] || y < u[2] || y > u[3] || z < u[4] || z > u[5]) return 0.0;
+            return coll_hyb<D - 1>(S, n.a, x, y, z);
+        }
+    }
+    return 0.0;
+}
+
+// ObjectCollection.Density in FP64 over the candidate list of the point's
+// cell (children outside it are exactly 0; order is kept, so greedy picks and
+// FP64 sums equal the full loop's).
+template <int D>
+XRP_HD double coll_hyb(const SceneDev& S, int id, double x, double y, double z) {
+    const Node& c = S.nodes[id];
+    const int32_t* kids = S.child + c.a;
+    int cnt = c.b;
+    const int32_t* list = nullptr;
+    if (c.flags & C_ACCEL) {
+        int G = (c.flags >> 16) & 0xff;
+        int ix = (int)floorf(((float)x - c.f[0]) * c.f[3]);
+        int iy = (int)floorf(((float)y - c.f[1]) * c.f[4]);
+        int iz = (int)floorf(((float)z - c.f[2]) * c.f[5]);
+        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
+        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
+        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
+        const int32_t* off = S.cells + f2i(c.f[6]) + (iz * G + iy) * G + ix;
+        list = S.items + off[0];
+        cnt = off[1] - off[0];
+    }
+    const bool greedy = (c.flags & C_GREEDY) != 0;
+    double density = 0.0;
+    for (int k = 0; k < cnt; k++) {
+        int slot = list ? list[k] : k;
+        double rho = item_hyb<D>(S, kids[slot], x, y, z);
+        if (greedy && rho > 0.0) return rho;
+        density = dadd(density, rho);
+    }
+    if (c.flags & C_CLIP) {
+        if (density < 0.0)
+            density = 0.0;
+        else if (density > 1.0)
+            density = 1.0;
+    }
+    return density;
+}
+
+XRP_HD double density_hyb(const SceneDev& S, double x, double y, double z) {
+    if (S.ndefs) deform64(S, x, y, z);
+    if (S.nodes[S.root].type == N_COLL) return coll_hyb<kMaxDepth>(S, S.root, x, y, z);
+    return item_hyb<kMaxDepth>(S, S.root, x, y, z);
+}
+
 // density() without the multiplier (main.go:137-140).
 XRP_HD double density64(const SceneDev& S, double x, double y, double z) {
     if (S.ndefs) deform64(S, x, y, z);
@@ -713,7 +812,7 @@ XRP_HDN double sample64_pixel(const SceneDev& S, const ViewDev& V, const double*
     double x = dadd(r.o[0], dmul(r.d[0], s));
     double y = dadd(r.o[1], dmul(r.d[1], s));
     double z = dadd(r.o[2], dmul(r.d[2], s));
-    return density64(S, x, y, z);
+    return density_hyb(S, x, y, z);
 }
 
 // The pixel a sampler works for, for the FP64 re-evaluation.

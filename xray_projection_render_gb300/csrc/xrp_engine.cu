@@ -63,93 +63,103 @@ __device__ __forceinline__ float4 gather_a2d(cudaTextureObject_t tex, int layer,
     return r;
 }
 
-// Voxel-grid sampler reading the 8 taps with two gathers: the grid is a
-// layered texture with one layer per z slice, width ny (j) and height nx (i),
-// point-sampled and clamped to the edge (so x1 = min(x0+1, N-1) as in
-// objects.go:822-830).  Bounds, weights and interpolation are those of vol32.
-struct VolumeTexSampler {
-    const SceneDev& S;
-    const Volume& V;
-    const VolRay& vr;
-    PixelRef px;
+// Parameters of a voxel-grid root (no deformation), read by the voxel
+// kernels from their constant bank so the march keeps few live registers.
+struct VoxParams {
+    cudaTextureObject_t tex;  // layered texture of the grid (gather path)
+    const float* data;        // [z][x][y] (load path, FP64 re-evaluation)
+    const double* data64;     // exact values when FP32 cannot hold them, else null
+    int nx, ny, nz;
+    int zero_guard;           // hierarchical integrator: guard the density == 0 test
+    float scale[3];           // (N-1)/2
     float inv_scale[3];
-    float band_zero;
-    cudaTextureObject_t tex;
-    static constexpr bool kHasInner = true;
-    __device__ __forceinline__ float inner(float ux, float uy, float uz) const {
-        float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
-        int x0 = min(max((int)fx, 0), V.nx - 2);
-        int y0 = min(max((int)fy, 0), V.ny - 2);
-        int z0 = min(max((int)fz, 0), V.nz - 2);
-        float wx = ux - (float)x0, wy = uy - (float)y0, wz = uz - (float)z0;
-        float gu = (float)y0 + 1.0f, gv = (float)x0 + 1.0f;
-        float4 g0 = gather_a2d(tex, z0, gu, gv);
-        float4 g1 = gather_a2d(tex, z0 + 1, gu, gv);
-        float v = trilerp(wx, wy, wz, g0.w, g1.w, g0.z, g1.z, g0.x, g1.x, g0.y, g1.y);
-        if (S.hier_zero_guard) {
-            float amax = fmaxf(fmaxf(fmaxf(fabsf(g0.x), fabsf(g0.y)), fmaxf(fabsf(g0.z), fabsf(g0.w))),
-                               fmaxf(fmaxf(fabsf(g1.x), fabsf(g1.y)), fmaxf(fabsf(g1.z), fabsf(g1.w))));
-            if (amax > 0.0f && fabsf(v) <= band_zero * amax) return xnan();
-        }
-        return v;
-    }
-    __device__ __forceinline__ float f32(float t) const {
-        float ux = fmaf(vr.du[0], t, vr.uc[0]);
-        float uy = fmaf(vr.du[1], t, vr.uc[1]);
-        float uz = fmaf(vr.du[2], t, vr.uc[2]);
-        int b = vol_bounds(V, inv_scale, ux, uy, uz);
-        if (b == 0) return 0.0f;
-        if (b == 2) return xnan();
-        return inner(ux, uy, uz);
-    }
-    __device__ __forceinline__ float f32_inner(float t) const {
-        return inner(fmaf(vr.du[0], t, vr.uc[0]), fmaf(vr.du[1], t, vr.uc[1]),
-                     fmaf(vr.du[2], t, vr.uc[2]));
-    }
-    __device__ __forceinline__ double f64(double s) const {
-        return sample64_pixel(S, *px.V, px.xs, px.i, px.j, s);
-    }
+    float band_w;             // world-space guard band of the inclusive [-1,1] test
+    float band_zero;          // relative band of the zero test
+    float inner_margin;       // clip margin of the bounds-free interior range
+    float lo[3], hi[3];       // dilated support box
 };
 
-template <bool HIER>
-__device__ __forceinline__ float render_pixel_tex(const SceneDev& S, const Lattice& L,
-                                                  const RenderParams& P, const ViewDev& V, int i,
-                                                  int j, cudaTextureObject_t tex, RayStats& st) {
-    const Volume& vol = S.vols[0];
-    Ray r;
-    VolRay vr;
-    {
-        Ray64 r64;
-        setup_ray64(V, P.xs, i, j, r64);
-        setup_ray32(r64, L.s_c, r);
-        setup_volray(vol, r64, L.s_c, vr);
-    }
-    VolumeTexSampler smp{S, vol, vr, PixelRef{&V, P.xs, i, j},
-                         {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
-                         S.nodes[S.root].f[0], tex};
-    float acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
-                     : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st, 4.0f * vol.band_w + 2e-4f);
-    float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
-    return expf(-fmaf(w, acc, P.flat_field));
+// FP64 density of sample s of pixel (i, j) (VoxelGrid.Density at the
+// reference's own position, objects.go:789-855, main.go:148-150).
+__device__ __noinline__ double vox_sample64(const VoxParams& Q, const ViewDev& V, const double* xs,
+                                            int i, int j, double s) {
+    Ray64 r;
+    setup_ray64(V, xs, i, j, r);
+    double x = xrp::dadd(r.o[0], xrp::dmul(r.d[0], s));
+    double y = xrp::dadd(r.o[1], xrp::dmul(r.d[1], s));
+    double z = xrp::dadd(r.o[2], xrp::dmul(r.d[2], s));
+    Volume vol;
+    vol.data = Q.data;
+    vol.data64 = Q.data64;
+    vol.nx = Q.nx;
+    vol.ny = Q.ny;
+    vol.nz = Q.nz;
+    return voxel64(vol, x, y, z);
 }
 
-// Minimum resident blocks per SM asked of the compiler (register budget):
-// tuned on GB300 for the voxel-grid and the general-scene kernels.
-#ifndef XRP_VOLUME_MIN_BLOCKS
-#define XRP_VOLUME_MIN_BLOCKS 4
-#endif
-#ifndef XRP_SCENE_MIN_BLOCKS
-#define XRP_SCENE_MIN_BLOCKS 2
-#endif
+// Trilinear value at grid point u (interior: no bounds test).  TEX: the 8
+// taps come from two gathers of the layered texture (layer = z slice, width
+// ny, height nx, point sampling, clamp to edge so x1 = min(x0+1, N-1) as in
+// objects.go:822-830); otherwise from eight loads.
+template <bool TEX>
+__device__ __forceinline__ float vox_inner(const VoxParams& Q, float ux, float uy, float uz) {
+    int x0 = min(max((int)floorf(ux), 0), Q.nx - 2);
+    int y0 = min(max((int)floorf(uy), 0), Q.ny - 2);
+    int z0 = min(max((int)floorf(uz), 0), Q.nz - 2);
+    float wx = ux - (float)x0, wy = uy - (float)y0, wz = uz - (float)z0;
+    float v000, v001, v010, v011, v100, v101, v110, v111;
+    if constexpr (TEX) {
+        float gu = (float)y0 + 1.0f, gv = (float)x0 + 1.0f;
+        float4 g0 = gather_a2d(Q.tex, z0, gu, gv);
+        float4 g1 = gather_a2d(Q.tex, z0 + 1, gu, gv);
+        v000 = g0.w; v010 = g0.z; v100 = g0.x; v110 = g0.y;
+        v001 = g1.w; v011 = g1.z; v101 = g1.x; v111 = g1.y;
+    } else {
+        const long NY = Q.ny, NXY = (long)Q.nx * Q.ny;
+        const float* p0 = Q.data + z0 * NXY + x0 * NY + y0;
+        const float* p1 = p0 + NXY;
+        v000 = __ldg(p0); v010 = __ldg(p0 + 1); v100 = __ldg(p0 + NY); v110 = __ldg(p0 + NY + 1);
+        v001 = __ldg(p1); v011 = __ldg(p1 + 1); v101 = __ldg(p1 + NY); v111 = __ldg(p1 + NY + 1);
+    }
+    float v = trilerp(wx, wy, wz, v000, v001, v010, v011, v100, v101, v110, v111);
+    if (Q.zero_guard) {
+        float amax = fmaxf(fmaxf(fmaxf(fabsf(v000), fabsf(v001)), fmaxf(fabsf(v010), fabsf(v011))),
+                           fmaxf(fmaxf(fabsf(v100), fabsf(v101)), fmaxf(fabsf(v110), fabsf(v111))));
+        if (amax > 0.0f && fabsf(v) <= Q.band_zero * amax) return xnan();
+    }
+    return v;
+}
 
-// MODE: 0 general scene, 1 voxel grid through loads, 2 voxel grid through
-// texture gathers.
-template <bool HIER, int MODE>
-__global__ void __launch_bounds__(256, MODE == 0 ? XRP_SCENE_MIN_BLOCKS : XRP_VOLUME_MIN_BLOCKS)
-    k_render(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
-             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
-             int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats,
-             cudaTextureObject_t tex) {
+template <bool TEX>
+struct VoxSampler {
+    const VoxParams& Q;
+    const ViewDev* V;
+    const double* xs;
+    float uc[3], du[3];
+    int i, j;
+    static constexpr bool kHasInner = true;
+    __device__ __forceinline__ float f32(float t) const {
+        float ux = fmaf(du[0], t, uc[0]), uy = fmaf(du[1], t, uc[1]), uz = fmaf(du[2], t, uc[2]);
+        float mx = fminf(ux, (float)(Q.nx - 1) - ux) * Q.inv_scale[0];
+        float my = fminf(uy, (float)(Q.ny - 1) - uy) * Q.inv_scale[1];
+        float mz = fminf(uz, (float)(Q.nz - 1) - uz) * Q.inv_scale[2];
+        float m = fminf(mx, fminf(my, mz));
+        if (m < -Q.band_w) return 0.0f;
+        if (!(m > Q.band_w)) return xnan();
+        return vox_inner<TEX>(Q, ux, uy, uz);
+    }
+    __device__ __forceinline__ float f32_inner(float t) const {
+        return vox_inner<TEX>(Q, fmaf(du[0], t, uc[0]), fmaf(du[1], t, uc[1]), fmaf(du[2], t, uc[2]));
+    }
+    __device__ __forceinline__ double f64(double s) const { return vox_sample64(Q, *V, xs, i, j, s); }
+};
+
+// Voxel-grid root: one thread per pixel, same tiling as k_render.
+template <bool TEX, bool HIER>
+__global__ void __launch_bounds__(256, 4)
+    k_voxel(const __grid_constant__ VoxParams Q, const __grid_constant__ Lattice L,
+            const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
+            int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats) {
     const int res = P.res;
     const int tpr = (res + 15) >> 4;
     const int tpv = tpr * tpr;
@@ -162,11 +172,59 @@ __global__ void __launch_bounds__(256, MODE == 0 ? XRP_SCENE_MIN_BLOCKS : XRP_VO
     const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
     RayStats st{0, 0};
     if (v < nviews && i < res && j < res) {
-        float val;
-        if constexpr (MODE == 2)
-            val = render_pixel_tex<HIER>(S, L, P, views[view0 + v], i, j, tex, st);
-        else
-            val = render_pixel<HIER, MODE == 1>(S, L, P, views[view0 + v], i, j, st);
+        const ViewDev* V = views + view0 + v;
+        Ray r;
+        VoxSampler<TEX> smp{Q, V, P.xs, {0, 0, 0}, {0, 0, 0}, i, j};
+        {
+            Ray64 r64;
+            setup_ray64(*V, P.xs, i, j, r64);
+            setup_ray32(r64, L.s_c, r);
+            for (int a = 0; a < 3; a++) {
+                double sc = (double)Q.scale[a];
+                smp.uc[a] = (float)((fma(r64.d[a], L.s_c, r64.o[a]) + 1.0) * sc);
+                smp.du[a] = (float)(r64.d[a] * sc);
+            }
+        }
+        float acc = HIER ? march_hier(L, Q.lo, Q.hi, r, smp, st)
+                         : march_simple(L, Q.lo, Q.hi, r, smp, st, Q.inner_margin);
+        float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+        out[((size_t)v * res + i) * res + j] = expf(-fmaf(w, acc, P.flat_field));
+    }
+    if (stats) {
+        unsigned s1 = __reduce_add_sync(0xffffffffu, st.samples);
+        unsigned f1 = __reduce_add_sync(0xffffffffu, st.fallbacks);
+        if (lane == 0) {
+            atomicAdd(&stats[0], (unsigned long long)s1);
+            if (f1) atomicAdd(&stats[1], (unsigned long long)f1);
+        }
+    }
+}
+
+// Minimum resident blocks per SM asked of the compiler (register budget)
+// for the general-scene kernel, tuned on GB300.
+#ifndef XRP_SCENE_MIN_BLOCKS
+#define XRP_SCENE_MIN_BLOCKS 2
+#endif
+
+// General scenes (any object tree, deformation).
+template <bool HIER>
+__global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
+    k_render(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
+             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
+             int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats) {
+    const int res = P.res;
+    const int tpr = (res + 15) >> 4;
+    const int tpv = tpr * tpr;
+    const int b = blockIdx.x;
+    const int v = b / tpv;
+    const int t = b - v * tpv;
+    const int ti = t / tpr, tj = t - ti * tpr;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = (ti << 4) + ((warp >> 1) << 2) + (lane >> 3);
+    const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
+    RayStats st{0, 0};
+    if (v < nviews && i < res && j < res) {
+        float val = render_pixel<HIER, false>(S, L, P, views[view0 + v], i, j, st);
         out[((size_t)v * res + i) * res + j] = val;
     }
     if (stats) {  // every lane reaches this point
@@ -370,8 +428,31 @@ struct Prepared {
     const ViewDev* views = nullptr;
     bool volume_fast = false;
     cudaTextureObject_t tex = 0;  // layered texture of the root grid (0: use loads)
+    VoxParams vq;                 // voxel-grid root parameters (volume_fast)
     bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
 };
+
+void fill_voxparams(const HostPrepared& hp, const float* data, const double* data64,
+                    cudaTextureObject_t tex, VoxParams& q) {
+    memset(&q, 0, sizeof(q));
+    const Volume& v = hp.vols[0];
+    q.tex = tex;
+    q.data = data;
+    q.data64 = data64;
+    q.nx = v.nx;
+    q.ny = v.ny;
+    q.nz = v.nz;
+    q.zero_guard = hp.S.hier_zero_guard;
+    for (int a = 0; a < 3; a++) {
+        q.scale[a] = v.scale[a];
+        q.inv_scale[a] = 1.0f / v.scale[a];
+        q.lo[a] = hp.S.sup_lo[a];
+        q.hi[a] = hp.S.sup_hi[a];
+    }
+    q.band_w = v.band_w;
+    q.band_zero = hp.fs.nodes[hp.fs.root].f[0];
+    q.inner_margin = 4.0f * v.band_w + 2e-4f;
+}
 
 // Everything a render needs on the device except the volume data.
 int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol_dev,
@@ -424,6 +505,7 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     out.volume_fast = hp.volume_fast;
     out.tex = hp.volume_fast ? tex : 0;
     out.empty = hl.hdr.K <= 0;
+    if (hp.volume_fast) fill_voxparams(hp, vol_dev[0], vol64_dev[0], out.tex, out.vq);
     return 0;
 }
 
@@ -443,19 +525,16 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
     if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
     dim3 grid((unsigned)blocks), block(256);
     bool hier = integration == XRP_INTEGRATE_HIERARCHICAL;
-    int mode = pr.volume_fast ? (pr.tex ? 2 : 1) : 0;
-#define XRP_LAUNCH(H, M) \
-    k_render<H, M><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats, pr.tex)
-    if (hier) {
-        if (mode == 2) XRP_LAUNCH(true, 2);
-        else if (mode == 1) XRP_LAUNCH(true, 1);
-        else XRP_LAUNCH(true, 0);
+    if (pr.volume_fast) {
+        bool tex = pr.vq.tex != 0;
+        if (hier && tex) k_voxel<true, true><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        else if (hier) k_voxel<false, true><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        else if (tex) k_voxel<true, false><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        else k_voxel<false, false><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
     } else {
-        if (mode == 2) XRP_LAUNCH(false, 2);
-        else if (mode == 1) XRP_LAUNCH(false, 1);
-        else XRP_LAUNCH(false, 0);
+        if (hier) k_render<true><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+        else k_render<false><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
     }
-#undef XRP_LAUNCH
     return cudaGetLastError();
 }
 
@@ -933,6 +1012,7 @@ extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, 
     pr.views = (const ViewDev*)(base + o_views);
     pr.volume_fast = hp.volume_fast;  // per-tap loads: a texture would need an array allocation
     pr.tex = 0;
+    if (pr.volume_fast) fill_voxparams(hp, d_volume, nullptr, 0, pr.vq);
     const int tpv = ((res + 15) / 16) * ((res + 15) / 16);
     const int per_launch = std::max(1, (int)(0x7fffffffL / tpv));
     size_t img = (size_t)res * res;
