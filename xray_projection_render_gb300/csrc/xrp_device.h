@@ -444,12 +444,16 @@ XRP_HD void deform32(const SceneDev& S, float& x, float& y, float& z) {
 
 constexpr int kMaxDepth = 3;  // nested tessellations supported by the evaluators
 
+// DEPTH: deepest tessellation nesting of the scene (kernels are specialised
+// on it so that evaluator code a scene cannot reach is not compiled in);
+// DEFS: whether a deformation is applied.
+template <int DEPTH, bool DEFS>
 XRP_HD float density32(const SceneDev& S, float x, float y, float z) {
-    if (S.ndefs) deform32(S, x, y, z);
+    if constexpr (DEFS) deform32(S, x, y, z);
     const Node& r = S.nodes[S.root];
     if (r.type <= N_GYROID) return leaf32(r, x, y, z);
-    if (r.type == N_COLL) return coll32<kMaxDepth>(S, r, x, y, z);
-    return item32<kMaxDepth>(S, S.root, x, y, z);
+    if (r.type == N_COLL) return coll32<DEPTH>(S, r, x, y, z);
+    return item32<DEPTH>(S, S.root, x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -805,14 +809,19 @@ XRP_HD void setup_ray32(const Ray64& r64, double s_c, Ray& r) {
 // FP64 density of sample s of pixel (i, j), positions formed exactly as the
 // reference does (main.go:148-150).  The ray is recomputed here so that the
 // FP32 march keeps no FP64 state live.
-XRP_HDN double sample64_pixel(const SceneDev& S, const ViewDev& V, const double* xs, int i, int j,
-                              double s) {
+XRP_HD double sample64_pixel_inl(const SceneDev& S, const ViewDev& V, const double* xs, int i,
+                                 int j, double s) {
     Ray64 r;
     setup_ray64(V, xs, i, j, r);
     double x = dadd(r.o[0], dmul(r.d[0], s));
     double y = dadd(r.o[1], dmul(r.d[1], s));
     double z = dadd(r.o[2], dmul(r.d[2], s));
     return density_hyb(S, x, y, z);
+}
+
+XRP_HDN double sample64_pixel(const SceneDev& S, const ViewDev& V, const double* xs, int i, int j,
+                              double s) {
+    return sample64_pixel_inl(S, V, xs, i, j, s);
 }
 
 // The pixel a sampler works for, for the FP64 re-evaluation.
@@ -873,6 +882,7 @@ struct RayStats {
 
 // Samplers: density at lattice offset t (FP32, NaN when uncertain) and the
 // exact FP64 density at reference position s.
+template <int DEPTH, bool DEFS>
 struct SceneSampler {
     const SceneDev& S;
     const Ray& r;
@@ -882,10 +892,13 @@ struct SceneSampler {
         float x = fmaf(r.d32[0], t, r.pc[0]);
         float y = fmaf(r.d32[1], t, r.pc[1]);
         float z = fmaf(r.d32[2], t, r.pc[2]);
-        return density32(S, x, y, z);
+        return density32<DEPTH, DEFS>(S, x, y, z);
     }
     XRP_HD float f32_inner(float t) const { return f32(t); }
     XRP_HD double f64(double s) const { return sample64_pixel(S, *px.V, px.xs, px.i, px.j, s); }
+    XRP_HD double f64_inline(double s) const {
+        return sample64_pixel_inl(S, *px.V, px.xs, px.i, px.j, s);
+    }
 };
 
 // A scene whose root is a voxel grid (no deformation): samples are formed
@@ -982,6 +995,9 @@ struct VolumeSampler {
                            fmaf(vr.du[1], t, vr.uc[1]), fmaf(vr.du[2], t, vr.uc[2]));
     }
     XRP_HD double f64(double s) const { return sample64_pixel(S, *px.V, px.xs, px.i, px.j, s); }
+    XRP_HD double f64_inline(double s) const {
+        return sample64_pixel_inl(S, *px.V, px.xs, px.i, px.j, s);
+    }
 };
 
 // Sample range [a, b] that lies inside the box [lo+m, hi-m] (m > guard band
@@ -1006,20 +1022,44 @@ XRP_HD void inner_range(const Lattice& L, const Ray& r, const float* lo, const f
 }
 
 // integrate_along_ray (main.go:144-154): returns the sum of densities over
-// the lattice samples (pre-multiplier, pre-ds).  With `in_lo <= in_hi` the
-// samples in [in_lo, in_hi] skip the sampler's bounds test.
-template <class Sampler>
-XRP_HD float march_range(const Lattice& L, const Sampler& smp, int k0, int k1, KahanF& acc,
-                         RayStats& st) {
+// the lattice samples (pre-multiplier, pre-ds).
+//
+// Uncertain samples are not re-evaluated inside the loop: their indices go to
+// a six-entry register buffer and the FP64 evaluation runs after the loop.
+// A call site inside the loop would hold every loop value across a call and
+// push the kernel into spills.  In the rare ray with more than six uncertain
+// samples the march is repeated in FP32 to find the rest.  The sum's order
+// changes, not its terms (Kahan-compensated either way).
+struct Deferred {
+    int n = 0;
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0, b5 = 0;
+    XRP_HD void push(int k) {
+        if (n == 0) b0 = k;
+        else if (n == 1) b1 = k;
+        else if (n == 2) b2 = k;
+        else if (n == 3) b3 = k;
+        else if (n == 4) b4 = k;
+        else if (n == 5) b5 = k;
+        n++;
+    }
+    XRP_HD int get(int q) const {
+        return q == 0 ? b0 : q == 1 ? b1 : q == 2 ? b2 : q == 3 ? b3 : q == 4 ? b4 : b5;
+    }
+    static constexpr int kCap = 6;
+};
+
+template <class Sampler, bool INNER>
+XRP_HD void march_range(const Lattice& L, const Sampler& smp, int k0, int k1, KahanF& acc,
+                        Deferred& dq) {
     for (int k = k0; k <= k1; k++) {
-        float rho = smp.f32(lattice_t(L, k));
+        float t = lattice_t(L, k);
+        float rho = INNER ? smp.f32_inner(t) : smp.f32(t);
         if (isunc(rho)) {
-            rho = (float)smp.f64(L.s64[k]);
-            st.fallbacks++;
+            dq.push(k);
+            rho = 0.0f;
         }
         acc.add(rho);
     }
-    return acc.s;
 }
 
 template <class Sampler>
@@ -1031,24 +1071,37 @@ XRP_HD float march_simple(const Lattice& L, const float* lo, const float* hi, co
     KahanF acc;
     if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
     st.samples += (uint32_t)(k1 - k0 + 1);
-    if constexpr (Sampler::kHasInner) {
-        int a, b;
-        inner_range(L, r, lo, hi, inner_margin, k0, k1, a, b);
-        if (a <= b) {
-            march_range(L, smp, k0, a - 1, acc, st);
-            for (int k = a; k <= b; k++) {
-                float rho = smp.f32_inner(lattice_t(L, k));
-                if (isunc(rho)) {
-                    rho = (float)smp.f64(L.s64[k]);
-                    st.fallbacks++;
-                }
-                acc.add(rho);
+    Deferred dq;
+    int a = k1 + 1, b = k1;
+    if constexpr (Sampler::kHasInner) inner_range(L, r, lo, hi, inner_margin, k0, k1, a, b);
+    if (a <= b) {
+        march_range<Sampler, false>(L, smp, k0, a - 1, acc, dq);
+        march_range<Sampler, true>(L, smp, a, b, acc, dq);
+        march_range<Sampler, false>(L, smp, b + 1, k1, acc, dq);
+    } else {
+        march_range<Sampler, false>(L, smp, k0, k1, acc, dq);
+    }
+    if (dq.n) {
+        // FP64 for the buffered samples; when more than kCap were uncertain,
+        // refill the buffer by scanning on from the last one evaluated (the
+        // FP32 decisions repeat exactly, so the same samples are found)
+        const int total = dq.n;
+        st.fallbacks += (uint32_t)total;
+        int done = 0;
+        for (;;) {
+            int nb = dq.n < Deferred::kCap ? dq.n : Deferred::kCap;
+            for (int q = 0; q < nb; q++) acc.add((float)smp.f64_inline(L.s64[dq.get(q)]));
+            done += nb;
+            if (done >= total || nb == 0) break;
+            int from = dq.get(nb - 1) + 1;
+            dq.n = 0;
+            for (int k = from; k <= k1 && dq.n < Deferred::kCap; k++) {
+                float t = lattice_t(L, k);
+                float rho = (k >= a && k <= b) ? smp.f32_inner(t) : smp.f32(t);
+                if (isunc(rho)) dq.push(k);
             }
-            march_range(L, smp, b + 1, k1, acc, st);
-            return acc.s;
         }
     }
-    march_range(L, smp, k0, k1, acc, st);
     return acc.s;
 }
 
@@ -1093,7 +1146,7 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
 
 // One pixel: optical depth T = flat_field + multiplier * (sum), as
 // transmittance exp(-T) (main.go:146, 153, 175, 198).
-template <bool HIER, bool VOLUME>
+template <bool HIER, bool VOLUME, int DEPTH = kMaxDepth, bool DEFS = true>
 XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P,
                           const ViewDev& V, int i, int j, RayStats& st) {
     Ray r;
@@ -1119,7 +1172,7 @@ XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParam
             setup_ray64(V, P.xs, i, j, r64);
             setup_ray32(r64, L.s_c, r);
         }
-        SceneSampler smp{S, r, px};
+        SceneSampler<DEPTH, DEFS> smp{S, r, px};
         acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
                    : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
     }

@@ -81,8 +81,8 @@ struct VoxParams {
 
 // FP64 density of sample s of pixel (i, j) (VoxelGrid.Density at the
 // reference's own position, objects.go:789-855, main.go:148-150).
-__device__ __noinline__ double vox_sample64(const VoxParams& Q, const ViewDev& V, const double* xs,
-                                            int i, int j, double s) {
+__device__ __forceinline__ double vox_sample64_inl(const VoxParams& Q, const ViewDev& V,
+                                                   const double* xs, int i, int j, double s) {
     Ray64 r;
     setup_ray64(V, xs, i, j, r);
     double x = xrp::dadd(r.o[0], xrp::dmul(r.d[0], s));
@@ -95,6 +95,11 @@ __device__ __noinline__ double vox_sample64(const VoxParams& Q, const ViewDev& V
     vol.ny = Q.ny;
     vol.nz = Q.nz;
     return voxel64(vol, x, y, z);
+}
+
+__device__ __noinline__ double vox_sample64(const VoxParams& Q, const ViewDev& V, const double* xs,
+                                            int i, int j, double s) {
+    return vox_sample64_inl(Q, V, xs, i, j, s);
 }
 
 // Trilinear value at grid point u (interior: no bounds test).  TEX: the 8
@@ -152,6 +157,9 @@ struct VoxSampler {
         return vox_inner<TEX>(Q, fmaf(du[0], t, uc[0]), fmaf(du[1], t, uc[1]), fmaf(du[2], t, uc[2]));
     }
     __device__ __forceinline__ double f64(double s) const { return vox_sample64(Q, *V, xs, i, j, s); }
+    __device__ __forceinline__ double f64_inline(double s) const {
+        return vox_sample64_inl(Q, *V, xs, i, j, s);
+    }
 };
 
 // Voxel-grid root: one thread per pixel, same tiling as k_render.
@@ -206,8 +214,9 @@ __global__ void __launch_bounds__(256, 4)
 #define XRP_SCENE_MIN_BLOCKS 2
 #endif
 
-// General scenes (any object tree, deformation).
-template <bool HIER>
+// General scenes (any object tree, deformation), specialised on the deepest
+// tessellation nesting and on the presence of a deformation.
+template <bool HIER, int DEPTH, bool DEFS>
 __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
     k_render(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
              const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
     const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
     RayStats st{0, 0};
     if (v < nviews && i < res && j < res) {
-        float val = render_pixel<HIER, false>(S, L, P, views[view0 + v], i, j, st);
+        float val = render_pixel<HIER, false, DEPTH, DEFS>(S, L, P, views[view0 + v], i, j, st);
         out[((size_t)v * res + i) * res + j] = val;
     }
     if (stats) {  // every lane reaches this point
@@ -429,6 +438,8 @@ struct Prepared {
     bool volume_fast = false;
     cudaTextureObject_t tex = 0;  // layered texture of the root grid (0: use loads)
     VoxParams vq;                 // voxel-grid root parameters (volume_fast)
+    int depth = kMaxDepth;        // kernel specialisation of general scenes
+    bool defs = true;
     bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
 };
 
@@ -503,6 +514,8 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     out.P.xs = (const double*)(base + o_xs);
     out.views = (const ViewDev*)(base + o_views);
     out.volume_fast = hp.volume_fast;
+    out.depth = fs.depth;
+    out.defs = !fs.defs.empty();
     out.tex = hp.volume_fast ? tex : 0;
     out.empty = hl.hdr.K <= 0;
     if (hp.volume_fast) fill_voxparams(hp, vol_dev[0], vol64_dev[0], out.tex, out.vq);
@@ -532,8 +545,19 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
         else if (tex) k_voxel<true, false><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
         else k_voxel<false, false><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
     } else {
-        if (hier) k_render<true><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
-        else k_render<false><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats);
+#define XRP_GEN(H, D, F) \
+    k_render<H, D, F><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats)
+#define XRP_GEN_D(H, F)                  \
+    if (pr.depth == 0) XRP_GEN(H, 0, F); \
+    else if (pr.depth == 1) XRP_GEN(H, 1, F); \
+    else XRP_GEN(H, 3, F);
+        if (hier) {
+            if (pr.defs) { XRP_GEN_D(true, true) } else { XRP_GEN_D(true, false) }
+        } else {
+            if (pr.defs) { XRP_GEN_D(false, true) } else { XRP_GEN_D(false, false) }
+        }
+#undef XRP_GEN_D
+#undef XRP_GEN
     }
     return cudaGetLastError();
 }

@@ -715,8 +715,11 @@ struct Flattener {
         throw SchemaError("internal: bad node type");
     }
 
+    int max_depth = 0;
+
     int tess(const HNode& h, double E, double P, int depth, Info& info) {
         if (depth >= kMaxDepth) throw SchemaError("tessellations nested deeper than supported (3)");
+        max_depth = std::max(max_depth, depth + 1);
         const double* o = h.d;
         const double* u = h.d + 6;
         Node n;
@@ -1065,6 +1068,7 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
         fs.defs.push_back(s);
     }
     fs.volume_root = (r.type == N_VOXEL) && hs.defs.empty();
+    fs.depth = F.max_depth;
     // world-space band of the inclusive [-1,1] voxel-grid test: the position
     // error plus the rounding of grid coordinates (|u| <= N-1) seen in world
     // units (the fast path forms u = (p+1)(N-1)/2 directly)

@@ -79,6 +79,7 @@ struct FlatScene {
     float sup32_lo[3], sup32_hi[3];
     bool volume_root = false;     // root is a voxel grid and there is no deformation
     double vol_band_w = 0.0;      // world-space guard band of the voxel bounds test
+    int depth = 0;                // deepest tessellation nesting (0: none)
 };
 
 FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical);
