@@ -213,6 +213,17 @@ FLOPS = {
 }
 
 
+# DRAM bytes (read + write) of the render kernel per view, from the ncu
+# captures summarised in profiles/ (small cases scaled by view count: the
+# grid streams through L2 once per view, so traffic grows with the views).
+TRAFFIC = {
+    "voxel": {"bytes_per_view": (404.93e6 + 47.01e6) / 8,
+              "source": "profiles/k_voxel_gather_voxel256_8x1024.md (8-view capture, x views)"},
+    "lattice": {"bytes_per_view": (0.611e6 + 0.472e6) / 2 * 4,
+                "source": "profiles/k_render_lattice_2x512.md (2 views at 512^2, x views x 4)"},
+}
+
+
 def make_workload(name, W, views, res):
     if name == "voxel":
         return W.voxel_blobs(res or 1024, views or 180)
@@ -344,7 +355,9 @@ def main():
                 "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
         "gpu_launches": args.steps,  # one render launch per step (all views)
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                     "frac": achieved / fp32_peak if fp32_peak else None,
+                     "traffic": TRAFFIC.get(args.workload, {}).get("bytes_per_view", 0) * n_my or None,
+                     "traffic_source": TRAFFIC.get(args.workload, {}).get("source"),
                      "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
                      "samples_per_step": samples_step, "flops_per_sample": fps,
                      "fp64_fallback_fraction": fp64 / max(samples, 1),
