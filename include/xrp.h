@@ -113,7 +113,8 @@ XRP_API int xrp_cameras_from_angles(const double* az_polar_deg, int n, double R,
 enum { XRP_INTEGRATE_SIMPLE = 0, XRP_INTEGRATE_HIERARCHICAL = 1 };
 enum {
     XRP_FLAG_STATS = 1,        /* count evaluated and FP64-re-evaluated samples */
-    XRP_FLAG_VOLUME_LOADS = 2  /* voxel-grid roots: per-tap loads instead of texture gathers */
+    XRP_FLAG_VOLUME_LOADS = 2, /* voxel-grid roots: per-tap loads instead of texture gathers */
+    XRP_FLAG_NO_REFINE = 4     /* proposal march: no certificate refinement of segments */
 };
 
 /* Per-call options: the globals and flags of the reference CLI
@@ -180,6 +181,84 @@ XRP_API int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples);
 
 /* Frees the device buffers the library caches between calls. */
 XRP_API void xrp_release_cache(void);
+
+/*
+ * Proposal march (no counterpart in the reference, whose integrators are
+ * main.go:144-199).  The plain integrator's samples are cut into segments.
+ * A segment whose end densities agree and whose end-point distance
+ * certificates cover it is counted as constant.  The rest are either
+ * refined (split at the middle sample, halves certified, recursively down to
+ * 8 samples) or integrated sample by sample like the plain integrator; a
+ * small network (64 positional features -> 3 x 64 ReLU -> 1 logit, BF16
+ * weights, FP32 accumulation on tensor cores) proposes which of the two,
+ * trained on the GPU on labels the plain integrator produces for the scene.
+ * Every sample is either evaluated or covered by a certificate, so results
+ * equal the plain integrator's (within FP32 summation order) whatever the
+ * network predicts; it changes the speed only.  Analytic scenes and the
+ * simple integrator only (code 2 otherwise).
+ */
+typedef struct xrp_proposal xrp_proposal;
+
+typedef struct {
+    int segment;       /* samples per segment, a multiple of 32 (0: 64) */
+    int train_rays;    /* rays sampled for training rows (0: 65536) */
+    int val_rays;      /* rays sampled for the threshold (0: 32768) */
+    int steps;         /* Adam steps (0: 2000) */
+    int batch;         /* rows per step (0: 4096) */
+    float lr;          /* Adam learning rate (0: 2e-3) */
+    float pos_weight;  /* loss weight of non-constant rows (0: 8) */
+    float tau_margin;  /* routing threshold = log(pos_weight) + tau_margin */
+    uint64_t seed;     /* ray sampling and initialisation */
+    int reserved[4];
+} xrp_proposal_opts;
+
+typedef struct {
+    float tau;           /* logits above tau route a candidate to dense integration */
+    int segment;
+    long long train_rows, train_pos;  /* candidate segments seen in training / non-constant */
+    long long val_rows, val_pos;
+    long long val_accepted;           /* validation candidates the network routes to refinement */
+    float final_loss;    /* mean weighted BCE over the last 10% of steps */
+    float train_ms;      /* wall time of data generation + training */
+} xrp_proposal_info;
+
+XRP_API int xrp_proposal_train(xrp_scene* scene, const xrp_camera* views, int num_views,
+                               const xrp_render_opts* opts, const xrp_proposal_opts* popts,
+                               xrp_proposal** out);
+XRP_API int xrp_proposal_get_info(const xrp_proposal* p, xrp_proposal_info* out);
+/* Copies the FP32 master parameters (xrp_mlp_param_count() floats; layout
+ * W1[64][64], b1[64], W2, b2, W3, b3, w4[64], b4). */
+XRP_API int xrp_proposal_params(const xrp_proposal* p, float* out, int n);
+XRP_API int xrp_proposal_set_tau(xrp_proposal* p, float tau);
+XRP_API void xrp_proposal_destroy(xrp_proposal* p);
+
+/* Renders like xrp_render with the proposal march.  `proposal` NULL: every
+ * candidate is refined (or, with XRP_FLAG_NO_REFINE, integrated densely);
+ * segment: samples per segment, 0 for the proposal's own or 64.  The device variant queues the work on `stream`
+ * and then waits for it (it reads back whether the list of samples left to
+ * FP64 overflowed, in which case the plain integrator renders the call). */
+XRP_API int xrp_render_proposal(xrp_scene* scene, const xrp_proposal* proposal, int segment,
+                                const xrp_camera* views, int num_views, const xrp_render_opts* opts,
+                                float* out);
+XRP_API int xrp_render_proposal_device(xrp_scene* scene, const xrp_proposal* proposal, int segment,
+                                       const xrp_camera* views, int num_views,
+                                       const xrp_render_opts* opts, float* out_device, void* stream);
+/* Counters of the last xrp_render_proposal on this thread with
+ * XRP_FLAG_STATS: segments, segments certified, pieces certified in
+ * refinement, pieces integrated densely, dense samples, certificate
+ * evaluations, FP64 re-evaluations, network rounds, candidates routed to
+ * dense integration, candidates refined. */
+XRP_API int xrp_proposal_last_stats(uint64_t out[10]);
+
+/* The network's training step on the GPU, exposed for gradient checks:
+ * for `rows` BF16 feature rows X (uint16 bit patterns, [rows][64]) and 0/1
+ * labels y, writes the gradient of (1/rows) sum w_r BCE(logit_r, y_r)
+ * (w_r = pos_weight for y_r = 1, else 1) with respect to `params` into
+ * `grad`, the loss into *loss and the logits into `logits` (each may be
+ * NULL).  Host buffers. */
+XRP_API int xrp_mlp_param_count(void);
+XRP_API int xrp_mlp_grad(const float* params, const uint16_t* X, const float* y, int rows,
+                         float pos_weight, float* grad, float* loss, float* logits);
 
 /*
  * RenderVolumeProjectionsCUDA for callers that cannot allocate device

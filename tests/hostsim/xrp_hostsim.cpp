@@ -105,3 +105,36 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
         return 2;
     }
 }
+
+// Density (FP32 guarded; NaN when uncertain) and distance certificate
+// (margin32, world units) at FP64 points rounded to FP32, for the soundness
+// tests of the certificates.  R and fov enter the error analysis as for a
+// render with those cameras.
+extern "C" __attribute__((visibility("default"))) int hs_margin(
+    const char* obj_json, const char* def_json, const double* pts, long n, double R, double fov,
+    double ds, float* rho_out, float* m_out, char* err, int errlen) {
+    try {
+        HostScene hs = load_scene(obj_json, def_json, {});
+        HostPrepared hp = prepare_host(hs, 8, 0, ds, R, 0.0, 1.0, fov);
+        SceneDev S = hp.S;
+        S.nodes = hp.fs.nodes.data();
+        S.nodes64 = hp.fs.nodes64.data();
+        S.child = hp.fs.child.data();
+        S.cells = hp.fs.cells.data();
+        S.items = hp.fs.items.data();
+        S.defs = hp.fs.defs.data();
+        S.vols = hp.vols.data();
+        for (long q = 0; q < n; q++) {
+            float x = (float)pts[3 * q], y = (float)pts[3 * q + 1], z = (float)pts[3 * q + 2];
+            rho_out[q] = density32<kMaxDepth, true>(S, x, y, z);
+            m_out[q] = margin32<kMaxDepth, true>(S, x, y, z);
+        }
+        return 0;
+    } catch (const std::exception& ex) {
+        if (err && errlen > 0) {
+            strncpy(err, ex.what(), errlen - 1);
+            err[errlen - 1] = 0;
+        }
+        return 2;
+    }
+}

@@ -1,0 +1,94 @@
+"""Soundness of the distance certificates (margin32) the proposal march uses
+to count segments without sampling them.
+
+The engine's FP32 code runs on the CPU (tests/hostsim).  For sample points
+of several scenes it returns the density and a radius m; every point within
+m of the sample must then have the same FP64 density (oracle) as the sample
+itself.  Points are drawn inside the ball and on its surface, where a
+too-large radius would show first."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "hostsim"))
+import hostsim  # noqa: E402
+
+from xray_projection_render_gb300 import workloads as W  # noqa: E402
+
+
+def check_scene(obj, deformation=None, n=1500, per=6, seed=0, lo=-1.1, hi=1.1, ds=0.002):
+    rng = np.random.default_rng(seed)
+    P = rng.uniform(lo, hi, (n, 3))
+    rho, m = hostsim.margin(obj, P, deformation=deformation, ds=ds)
+    sc = O.Scene(obj, deformation)
+    certified = 0
+    for k in range(n):
+        if not (m[k] > 0) or np.isnan(rho[k]):
+            continue
+        r0 = sc.density(*P[k])
+        assert np.float32(r0) == rho[k], (k, P[k], r0, rho[k])
+        u = rng.normal(size=(per, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        rad = m[k] * np.concatenate([np.full(per // 2, 0.999), rng.uniform(0, 1, per - per // 2)])
+        for q in P[k] + u * rad[:, None]:
+            assert sc.density(*q) == r0, (k, P[k], q, float(m[k]))
+        certified += 1
+    return certified, n
+
+
+def test_config1_collection():
+    c, n = check_scene(W.cube_minus_sphere_cylinder(8).obj)
+    assert c > n // 2
+
+
+def test_deformed_lattice():
+    w = W.deformed_lattice()
+    c, n = check_scene(w.obj, w.deformation, n=800)
+    assert c > n // 5
+
+
+def test_gyroid_sigmoid():
+    w = W.gyroid_sigmoid()
+    c, n = check_scene(w.obj, w.deformation)
+    assert c > n // 2
+
+
+def test_fine_gyroid():
+    obj = {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.3, "rho": 1.0}
+    c, n = check_scene(obj, n=800)
+    assert c > n // 4
+
+
+@pytest.mark.parametrize("k", [0, 3, 7])
+def test_batched_scene_with_candidate_lists(k):
+    w = W.batched_scenes(8)[k]
+    check_scene(w.obj, n=800, seed=k)
+
+
+def test_every_primitive_under_every_deformation():
+    prims = [
+        {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+        {"type": "box", "center": [0.0, 0.2, 0.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5},
+        {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+        {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+         "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9},
+        {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0},
+    ]
+    defs = [None,
+            {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02], "sigmas": [0.3, 0.3, 0.5],
+             "centers": [0.0, 0.1, 0.0]},
+            {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]},
+            {"type": "rigid", "displacements": [0.05, -0.1, 0.02]},
+            {"type": "sigmoid", "amplitude": 0.2, "center": 0.0, "lengthscale": 0.2,
+             "direction": "y"},
+            {"type": "affine", "matrix": [[1.1, 0.0, 0.1], [0.0, 0.9, 0.0], [0.05, 0.0, 1.0]]}]
+    for p in prims:
+        for d in defs:
+            check_scene(p, d, n=200, per=4)
+    coll = {"type": "object_collection", "objects": prims}
+    for d in defs:
+        check_scene(coll, d, n=300, per=4)

@@ -1,0 +1,184 @@
+"""The proposal march on the GPU: the tensor-core training step against the
+FP64 network of oracle/mlp.py; the march against the FP64 oracle (every
+sample is evaluated or covered by a certificate, so the bar is the plain
+integrator's 1e-5 relative, with or without the network); and what the
+trained network changes in work and speed against the march without it."""
+import time
+
+import numpy as np
+import pytest
+
+from oracle import mlp as M
+from oracle import oracle as O
+from xray_projection_render_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5  # relative transmittance error vs the FP64 oracle, as the plain integrator
+
+
+@pytest.fixture(scope="module")
+def X():
+    import __graft_entry__ as g
+    g.build()
+    import xray_projection_render_gb300 as X
+    return X
+
+
+def _oracle(w):
+    return O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov)
+
+
+def test_mlp_grad_matches_fp64_oracle(X):
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1, 1, (1000, 3))
+    b = a + rng.normal(0, 0.1, (1000, 3))
+    bits = M.bf16_bits(M.segment_features(a, b))
+    Xv = M.from_bf16_bits(bits)
+    y = (rng.uniform(size=1000) < 0.3).astype(np.float32)
+    p = M.init_params(3).astype(np.float32)
+    grad, loss, logits = X.mlp_grad(p, bits, y, pos_weight=8.0)
+    l_ref, z_ref, g_ref = M.forward_backward(p.astype(np.float64), Xv, y, 8.0, emulate=True)
+    assert abs(loss - l_ref) <= 1e-4 * abs(l_ref)
+    assert np.max(np.abs(logits - z_ref)) <= 1e-3 * (1 + np.max(np.abs(z_ref)))
+    rel = np.linalg.norm(grad - g_ref) / np.linalg.norm(g_ref)
+    assert rel <= 5e-3, rel
+    for name, (o, n) in M.OFF.items():
+        gr = g_ref[o:o + n]
+        d = np.linalg.norm(grad[o:o + n] - gr) / max(np.linalg.norm(gr), 1e-30)
+        assert d <= 2e-2, (name, d)
+
+
+def test_mlp_grad_small_batches_and_padding(X):
+    # rows not a multiple of the 128-row tile: padded rows contribute nothing
+    rng = np.random.default_rng(6)
+    for rows in (1, 37, 129):
+        bits = M.bf16_bits(rng.normal(size=(rows, 64)))
+        y = (rng.uniform(size=rows) < 0.5).astype(np.float32)
+        p = M.init_params(rows).astype(np.float32)
+        grad, loss, _ = X.mlp_grad(p, bits, y, pos_weight=2.0)
+        l_ref, _, g_ref = M.forward_backward(p.astype(np.float64), M.from_bf16_bits(bits), y, 2.0)
+        assert abs(loss - l_ref) <= 1e-4 * abs(l_ref)
+        assert np.linalg.norm(grad - g_ref) <= 5e-3 * np.linalg.norm(g_ref)
+
+
+CASES = {
+    "gyroid_sigmoid": lambda: W.reduced(W.gyroid_sigmoid(), 48, 2),
+    "deformed_lattice": lambda: W.reduced(W.deformed_lattice(), 40, 2),
+    "cube_minus_sphere_cylinder": lambda: W.cube_minus_sphere_cylinder(48),
+    "batched_scene0": lambda: W.reduced(W.batched_scenes(1)[0], 48, 2),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("segment,refine", [(32, False), (128, False), (64, True), (256, True)])
+def test_certificate_march_matches_oracle(X, name, segment, refine):
+    w = CASES[name]()
+    ref = _oracle(w)
+    with X.Scene(w.obj, w.deformation) as s:
+        img, st = X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                                    segment=segment, refine=refine, stats=True)
+        plain = X.render(s, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov)
+    assert np.max(np.abs(img - ref) / ref) <= REL_TOL
+    assert np.max(np.abs(plain - ref) / ref) <= REL_TOL
+    assert st["routed_dense"] == 0 and st["mlp_rounds"] == 0
+    if not refine:
+        assert st["subdivided"] == 0 and st["refined"] == 0
+        assert st["certified"] + st["dense"] == st["segments"]
+    if name == "gyroid_sigmoid" or (name == "cube_minus_sphere_cylinder" and segment == 32):
+        assert st["certified"] > 0
+    if refine and name == "gyroid_sigmoid":
+        assert st["refined"] > 0
+
+
+def test_certificate_march_device_path_and_options(X):
+    import torch
+    w = W.cube_minus_sphere_cylinder(40)
+    ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                   density_multiplier=1.7, flat_field=0.3)
+    with X.Scene(w.obj) as s:
+        out = torch.empty(len(w.angles) * w.res * w.res, device="cuda", dtype=torch.float32)
+        X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                          density_multiplier=1.7, flat_field=0.3, out=out)
+        torch.cuda.synchronize()
+        img = out.cpu().numpy().reshape(ref.shape)
+    assert np.max(np.abs(img - ref) / ref) <= REL_TOL
+
+
+def test_proposal_rejects_unsupported(X):
+    w = W.cube_minus_sphere_cylinder(16)
+    with X.Scene(w.obj) as s:
+        from xray_projection_render_gb300._lib import EngineError
+        with pytest.raises(EngineError):
+            X.render_proposal(s, None, w.angles, resolution=16, ds=w.ds, segment=48)
+        vol = W.gaussian_blob_volume(8, 2, seed=1)
+        with X.Scene({"type": "voxel_grid", "volume": 0}, volumes=[vol]) as sv:
+            with pytest.raises(EngineError):
+                X.render_proposal(sv, None, w.angles, resolution=16, ds=w.ds)
+
+
+@pytest.fixture(scope="module")
+def gyroid_trained(X):
+    w = W.reduced(W.gyroid_sigmoid(), 96, 4)
+    s = X.Scene(w.obj, w.deformation)
+    P = X.Proposal(s, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, segment=128,
+                   train_rays=16384, val_rays=8192, steps=1000, seed=1)
+    yield w, s, P
+    P.close()
+    s.close()
+
+
+def _work(st):
+    # samples evaluated, a certificate evaluation counted as two
+    return st["dense_samples"] + 2 * st["evaluations"]
+
+
+def test_trained_proposal_is_exact_and_routes(X, gyroid_trained):
+    w, s, P = gyroid_trained
+    info = P.info()
+    assert info["train_rows"] > 0 and np.isfinite(info["final_loss"])
+    ref = _oracle(w)
+    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, stats=True)
+    img, st = X.render_proposal(s, P, w.angles, **kw)
+    ref_only, st_r = X.render_proposal(s, None, w.angles, segment=info["segment"], **kw)
+    dense_only, st_d = X.render_proposal(s, None, w.angles, segment=info["segment"], refine=False,
+                                         **kw)
+    for im in (img, ref_only, dense_only):
+        assert np.max(np.abs(im - ref) / ref) <= REL_TOL
+    assert st["mlp_rounds"] > 0 and st["routed_dense"] + st["subdivided"] > 0
+    # against integrating every uncertified segment densely, the proposal
+    # (network + refinement) evaluates fewer samples
+    assert _work(st) < _work(st_d)
+    print(f"\nwork: proposal {_work(st)}, refinement only {_work(st_r)}, dense only {_work(st_d)}"
+          f"\nproposal {st}\ninfo {info}")
+
+
+def test_proposal_speed_against_plain_and_without_network(X, gyroid_trained):
+    """Times the plain integrator, the march without the network and the
+    proposal on the same rays (device output).  Prints the three rates; the
+    assertions are on the results, which must agree whatever the speed."""
+    import torch
+    w, s, P = gyroid_trained
+    res, views = 256, w.angles[:4]
+    n = len(views) * res * res
+    outs = [torch.empty(n, device="cuda", dtype=torch.float32) for _ in range(3)]
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov)
+    t_plain = timed(lambda: X.render(s, views, out=outs[0], **kw))
+    t_prop = timed(lambda: X.render_proposal(s, P, views, out=outs[1], **kw))
+    t_cert = timed(lambda: X.render_proposal(s, None, views, segment=P.info()["segment"],
+                                             refine=False, out=outs[2], **kw))
+    print(f"\nplain {n / t_plain / 1e6:.1f} Mrays/s, march without network {n / t_cert / 1e6:.1f}, "
+          f"proposal {n / t_prop / 1e6:.1f}")
+    a, b, c = (o.cpu().numpy() for o in outs)
+    assert np.max(np.abs(b - a) / a) <= 2 * REL_TOL
+    assert np.max(np.abs(c - a) / a) <= 2 * REL_TOL

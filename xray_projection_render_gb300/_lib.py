@@ -38,10 +38,24 @@ class XrpVolumeDesc(ctypes.Structure):
                 ("on_device", c_int)]
 
 
+class XrpProposalOpts(ctypes.Structure):
+    _fields_ = [("segment", c_int), ("train_rays", c_int), ("val_rays", c_int), ("steps", c_int),
+                ("batch", c_int), ("lr", c_float), ("pos_weight", c_float), ("tau_margin", c_float),
+                ("seed", ctypes.c_uint64), ("reserved", c_int * 4)]
+
+
+class XrpProposalInfo(ctypes.Structure):
+    _fields_ = [("tau", c_float), ("segment", c_int), ("train_rows", ctypes.c_longlong),
+                ("train_pos", ctypes.c_longlong), ("val_rows", ctypes.c_longlong),
+                ("val_pos", ctypes.c_longlong), ("val_accepted", ctypes.c_longlong),
+                ("final_loss", c_float), ("train_ms", c_float)]
+
+
 XRP_INTEGRATE_SIMPLE = 0
 XRP_INTEGRATE_HIERARCHICAL = 1
 XRP_FLAG_STATS = 1
 XRP_FLAG_VOLUME_LOADS = 2
+XRP_FLAG_NO_REFINE = 4
 
 # Every symbol include/xrp.h declares, with (restype, argtypes).
 SIGNATURES = {
@@ -62,6 +76,18 @@ SIGNATURES = {
     "xrp_release_cache": (None, []),
     "xrp_render_volume_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int,
                                           c_float, c_float, c_void_p, c_void_p]),
+    "xrp_proposal_train": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "xrp_proposal_get_info": (c_int, [c_void_p, c_void_p]),
+    "xrp_proposal_params": (c_int, [c_void_p, c_void_p, c_int]),
+    "xrp_proposal_set_tau": (c_int, [c_void_p, c_float]),
+    "xrp_proposal_destroy": (None, [c_void_p]),
+    "xrp_render_proposal": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "xrp_render_proposal_device": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                                           c_void_p, c_void_p]),
+    "xrp_proposal_last_stats": (c_int, [c_void_p]),
+    "xrp_mlp_param_count": (c_int, []),
+    "xrp_mlp_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p, c_void_p,
+                             c_void_p]),
 }
 
 _lib = None

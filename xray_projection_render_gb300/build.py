@@ -1,9 +1,10 @@
-"""Build recipe for libcuda_render.so (sm_103a) -- no cmake, two translation units.
+"""Build recipe for libcuda_render.so (sm_103a) -- no cmake.
 
     python -m xray_projection_render_gb300.build
 
-compiles ``csrc/xrp_scene.cpp`` with g++ and ``csrc/xrp_engine.cu`` with nvcc for
-``sm_103a`` in parallel, then links ``libcuda_render.so`` next to this file (the
+compiles ``csrc/xrp_scene.cpp`` with g++ and the CUDA units (host code and
+voxel kernels, general-scene kernels, proposal march, training) with nvcc for
+``sm_103a``, all in parallel, then links ``libcuda_render.so`` next to this file (the
 name the reference's Go loader looks for, cuda_backend.go:103-114).  Host
 floating point is built with contraction off so the FP64 camera and scene
 arithmetic rounds every operation, as the reference does.
@@ -56,6 +57,9 @@ def _run(cmd, verbose):
     return r
 
 
+CUDA_UNITS = ["xrp_engine.cu", "xrp_kern_scene.cu", "xrp_kern_prop.cu", "xrp_kern_train.cu"]
+
+
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
     """Compile the engine for sm_103a and return the path of the shared library."""
     if not force and not ptxas_info and not _stale(LIB):
@@ -64,23 +68,24 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     nvcc = _nvcc()
     common_host = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fvisibility=hidden"]
     o_scene = os.path.join(BUILD, "xrp_scene.o")
-    o_engine = os.path.join(BUILD, "xrp_engine.o")
-    cmd_scene = ["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, "-c",
-                 os.path.join(CSRC, "xrp_scene.cpp"), "-o", o_scene]
-    cmd_engine = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler",
-                  ",".join(common_host), "-I", INCLUDE, "-c", os.path.join(CSRC, "xrp_engine.cu"),
-                  "-o", o_engine]
-    if ptxas_info:
-        cmd_engine.insert(1, "-Xptxas=-v")
-    with ThreadPoolExecutor(2) as ex:
-        futs = [ex.submit(_run, cmd_scene, verbose), ex.submit(_run, cmd_engine, verbose)]
-        results = [f.result() for f in futs]
+    cmds = [["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, "-c",
+             os.path.join(CSRC, "xrp_scene.cpp"), "-o", o_scene]]
+    objs = [o_scene]
+    for unit in CUDA_UNITS:
+        o = os.path.join(BUILD, unit.replace(".cu", ".o"))
+        cmd = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", ",".join(common_host),
+               "-I", INCLUDE, "-c", os.path.join(CSRC, unit), "-o", o]
+        if ptxas_info:
+            cmd.insert(1, "-Xptxas=-v")
+        cmds.append(cmd)
+        objs.append(o)
+    with ThreadPoolExecutor(len(cmds)) as ex:
+        results = list(ex.map(lambda c: _run(c, verbose), cmds))
     tmp = LIB + f".tmp{os.getpid()}"
-    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, o_engine, o_scene, "-lpthread"],
-         verbose)
+    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lpthread"], verbose)
     os.replace(tmp, LIB)
     if ptxas_info:
-        return results[1].stderr
+        return "".join(r.stderr for r in results[1:])
     return LIB
 
 

@@ -152,6 +152,11 @@ struct SceneDev {
     int32_t hier_zero_guard;  // 1: flag near-zero voxel values (hierarchical zero test)
     int32_t pad;
     float sup_lo[3], sup_hi[3];  // dilated support box (FP32, world)
+    // distance certificates (margin32): 1 / Lipschitz bound of the
+    // deformation chain, and the absolute error allowance of a margin in
+    // deformed coordinates (position error plus FP32 arithmetic)
+    float inv_lip;
+    float m_slack;
 };
 
 // One view (camera) of a batch, prepared on the host.
@@ -454,6 +459,151 @@ XRP_HD float density32(const SceneDev& S, float x, float y, float z) {
     if (r.type <= N_GYROID) return leaf32(r, x, y, z);
     if (r.type == N_COLL) return coll32<DEPTH>(S, r, x, y, z);
     return item32<DEPTH>(S, S.root, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// Distance certificates
+// ---------------------------------------------------------------------------
+// margin32 returns a lower bound on the world-space distance from a sample
+// point to the nearest place where the density can change (a primitive
+// surface, a container bound, a tessellation cell face).  Inside a ball of
+// that radius the set of primitives containing the point is fixed, so the
+// reference's FP64 density is the same value everywhere in it.  Each leaf
+// bound is |max of the signed distances of the convex pieces it intersects|,
+// which under-estimates the distance to the boundary inside and outside.
+
+XRP_HD float leaf_margin(const Node& n, float x, float y, float z) {
+    const float* f = n.f;
+    switch (n.type) {
+    case N_SPHERE: {
+        float dx = x - f[0], dy = y - f[1], dz = z - f[2];
+        float d = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+        return fabsf(d - sqrtf(f[3]));
+    }
+    case N_BOX: {
+        float mx = f[3] - fabsf(x - f[0]);
+        float my = f[4] - fabsf(y - f[1]);
+        float mz = f[5] - fabsf(z - f[2]);
+        return fabsf(fminf(mx, fminf(my, mz)));
+    }
+    case N_CYL: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
+        float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
+        float pr = sqrtf(fmaf(pz, pz, fmaf(py, py, px * px)));
+        float len = sqrtf(1.0f / f[6]);
+        float sd = fmaxf(pr - sqrtf(f[7]), fmaxf(-c * len, (c - 1.0f) * len));
+        return fabsf(sd);
+    }
+    case N_PPD: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float sd = -3.0e38f;
+        for (int a = 0; a < 3; a++) {
+            const float* m = f + 3 + 3 * a;
+            float q = fmaf(m[2], wz, fmaf(m[1], wy, m[0] * wx));
+            float nrm = sqrtf(fmaf(m[2], m[2], fmaf(m[1], m[1], m[0] * m[0])));
+            sd = fmaxf(sd, fmaxf(-q, q - 1.0f) / nrm);
+        }
+        return fabsf(sd);
+    }
+    case N_GYROID: {
+        float X = (x - f[0]) * f[3], Y = (y - f[1]) * f[3], Z = (z - f[2]) * f[3];
+        float sx, cx, sy, cy, sz, cz;
+        f_sincos(X, &sx, &cx);
+        f_sincos(Y, &sy, &cy);
+        f_sincos(Z, &sz, &cz);
+        float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
+        // |grad g| <= sqrt(6) |1/scale| (each component is a sum of two
+        // products of sines and cosines)
+        float m = fabsf(f[4] - fabsf(g)) - f[F_BAND];
+        return fmaxf(m, 0.0f) / (2.4494898f * fabsf(f[3]));
+    }
+    default: return 0.0f;
+    }
+}
+
+template <int D>
+XRP_HD float collm32(const SceneDev& S, const Node& c, float x, float y, float z);
+
+template <int D>
+XRP_HD float itemm32(const SceneDev& S, int id, float x, float y, float z) {
+    const Node& n = S.nodes[id];
+    if (n.type <= N_GYROID) return leaf_margin(n, x, y, z);
+    if (n.type == N_TESS) {
+        if constexpr (D > 0) {
+            const float* f = n.f;
+            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
+                             fminf(z - f[4], f[5] - z));
+            if (mo <= 0.0f) return -mo;  // outside the outer bounds: zero up to the box
+            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
+            float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
+            // distance to the faces of this tessellation cell
+            float fc = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)) * fabsf(f[14]),
+                                   fminf(qy - ny, 1.0f - (qy - ny)) * fabsf(f[15])),
+                             fminf(qz - nz, 1.0f - (qz - nz)) * fabsf(f[16]));
+            float m = fminf(mo, fc);
+            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
+            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
+                             fminf(fz - f[11], f[12] - fz));
+            if (mu <= 0.0f) return fminf(m, -mu);  // outside the unit-cell bounds: zero
+            m = fminf(m, mu);
+            return fminf(m, collm32<D - 1>(S, S.nodes[n.a], fx, fy, fz));
+        }
+    }
+    return 0.0f;  // voxel grids and anything deeper: no certificate
+}
+
+// Collections: the density is a function of which children contain the
+// point, so the nearest child boundary bounds it.  With candidate lists
+// only the children overlapping the point's cell are listed; the others
+// cannot reach inside the cell, so the distance to the cell's inner faces
+// caps the bound.
+template <int D>
+XRP_HD float collm32(const SceneDev& S, const Node& c, float x, float y, float z) {
+    const int32_t* kids = S.child + c.a;
+    int cnt = c.b;
+    const int32_t* list = nullptr;
+    float m = 3.0e38f;
+    if (c.flags & C_ACCEL) {
+        int G = (c.flags >> 16) & 0xff;
+        float ux = (x - c.f[0]) * c.f[3], uy = (y - c.f[1]) * c.f[4], uz = (z - c.f[2]) * c.f[5];
+        int ix = (int)floorf(ux), iy = (int)floorf(uy), iz = (int)floorf(uz);
+        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
+        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
+        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
+        // inner faces only (the outer cells extend to infinity by the clamp)
+        if (ix > 0) m = fminf(m, (ux - (float)ix) / c.f[3]);
+        if (ix < G - 1) m = fminf(m, ((float)(ix + 1) - ux) / c.f[3]);
+        if (iy > 0) m = fminf(m, (uy - (float)iy) / c.f[4]);
+        if (iy < G - 1) m = fminf(m, ((float)(iy + 1) - uy) / c.f[4]);
+        if (iz > 0) m = fminf(m, (uz - (float)iz) / c.f[5]);
+        if (iz < G - 1) m = fminf(m, ((float)(iz + 1) - uz) / c.f[5]);
+        m = fmaxf(m, 0.0f);
+        int cell_base = f2i(c.f[6]);
+        const int32_t* off = S.cells + cell_base + (iz * G + iy) * G + ix;
+        int s0 = off[0], s1 = off[1];
+        list = S.items + s0;
+        cnt = s1 - s0;
+    }
+    for (int k = 0; k < cnt; k++) {
+        int slot = list ? list[k] : k;
+        m = fminf(m, itemm32<D>(S, kids[slot], x, y, z));
+    }
+    return m;
+}
+
+// World-space certificate radius at a sample point (deformation applied
+// here); 0 when nothing can be certified.
+template <int DEPTH, bool DEFS>
+XRP_HD float margin32(const SceneDev& S, float x, float y, float z) {
+    if constexpr (DEFS) deform32(S, x, y, z);
+    const Node& r = S.nodes[S.root];
+    float m;
+    if (r.type <= N_GYROID) m = leaf_margin(r, x, y, z);
+    else if (r.type == N_COLL) m = collm32<DEPTH>(S, r, x, y, z);
+    else m = itemm32<DEPTH>(S, S.root, x, y, z);
+    m = fmaf(m, 0.9999f, -S.m_slack);
+    return m > 0.0f ? m * S.inv_lip : 0.0f;
 }
 
 // ---------------------------------------------------------------------------

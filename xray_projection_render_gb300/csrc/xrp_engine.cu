@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -21,7 +22,7 @@
 #include <vector>
 
 #include "../../include/xrp.h"
-#include "xrp_device.h"
+#include "xrp_launch.h"
 #include "xrp_scene.h"
 
 using namespace xrp;
@@ -63,21 +64,7 @@ __device__ __forceinline__ float4 gather_a2d(cudaTextureObject_t tex, int layer,
     return r;
 }
 
-// Parameters of a voxel-grid root (no deformation), read by the voxel
-// kernels from their constant bank so the march keeps few live registers.
-struct VoxParams {
-    cudaTextureObject_t tex;  // layered texture of the grid (gather path)
-    const float* data;        // [z][x][y] (load path, FP64 re-evaluation)
-    const double* data64;     // exact values when FP32 cannot hold them, else null
-    int nx, ny, nz;
-    int zero_guard;           // hierarchical integrator: guard the density == 0 test
-    float scale[3];           // (N-1)/2
-    float inv_scale[3];
-    float band_w;             // world-space guard band of the inclusive [-1,1] test
-    float band_zero;          // relative band of the zero test
-    float inner_margin;       // clip margin of the bounds-free interior range
-    float lo[3], hi[3];       // dilated support box
-};
+
 
 // FP64 density of sample s of pixel (i, j) (VoxelGrid.Density at the
 // reference's own position, objects.go:789-855, main.go:148-150).
@@ -204,44 +191,6 @@ __global__ void __launch_bounds__(256, 4)
         if (lane == 0) {
             atomicAdd(&stats[0], (unsigned long long)s1);
             if (f1) atomicAdd(&stats[1], (unsigned long long)f1);
-        }
-    }
-}
-
-// Minimum resident blocks per SM asked of the compiler (register budget)
-// for the general-scene kernel, tuned on GB300.
-#ifndef XRP_SCENE_MIN_BLOCKS
-#define XRP_SCENE_MIN_BLOCKS 2
-#endif
-
-// General scenes (any object tree, deformation), specialised on the deepest
-// tessellation nesting and on the presence of a deformation.
-template <bool HIER, int DEPTH, bool DEFS>
-__global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
-    k_render(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
-             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
-             int nviews, float* __restrict__ out, unsigned long long* __restrict__ stats) {
-    const int res = P.res;
-    const int tpr = (res + 15) >> 4;
-    const int tpv = tpr * tpr;
-    const int b = blockIdx.x;
-    const int v = b / tpv;
-    const int t = b - v * tpv;
-    const int ti = t / tpr, tj = t - ti * tpr;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = (ti << 4) + ((warp >> 1) << 2) + (lane >> 3);
-    const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
-    RayStats st{0, 0};
-    if (v < nviews && i < res && j < res) {
-        float val = render_pixel<HIER, false, DEPTH, DEFS>(S, L, P, views[view0 + v], i, j, st);
-        out[((size_t)v * res + i) * res + j] = val;
-    }
-    if (stats) {  // every lane reaches this point
-        unsigned s = __reduce_add_sync(0xffffffffu, st.samples);
-        unsigned f = __reduce_add_sync(0xffffffffu, st.fallbacks);
-        if (lane == 0) {
-            atomicAdd(&stats[0], (unsigned long long)s);
-            if (f) atomicAdd(&stats[1], (unsigned long long)f);
         }
     }
 }
@@ -430,18 +379,7 @@ struct Tables {
     }
 };
 
-struct Prepared {
-    SceneDev S;
-    Lattice L;
-    RenderParams P;
-    const ViewDev* views = nullptr;
-    bool volume_fast = false;
-    cudaTextureObject_t tex = 0;  // layered texture of the root grid (0: use loads)
-    VoxParams vq;                 // voxel-grid root parameters (volume_fast)
-    int depth = kMaxDepth;        // kernel specialisation of general scenes
-    bool defs = true;
-    bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
-};
+
 
 void fill_voxparams(const HostPrepared& hp, const float* data, const double* data64,
                     cudaTextureObject_t tex, VoxParams& q) {
@@ -528,8 +466,15 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
 // launch
 // ---------------------------------------------------------------------------
 
+static cudaError_t launch_prop(const Prepared& pr, int view0, int nviews, const PropLaunch& pl,
+                               float* dout, cudaStream_t st) {
+    return pl.train ? launch_prop_train(pr, view0, nviews, pl.Q, st)
+                    : launch_prop_render(pr, view0, nviews, pl.Q, dout, st);
+}
+
 static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integration, float* dout,
-                          unsigned long long* stats, cudaStream_t st) {
+                          unsigned long long* stats, cudaStream_t st, const PropLaunch* pl = nullptr) {
+    if (pl) return launch_prop(pr, view0, nviews, *pl, dout, st);
     const ViewDev* dviews = pr.views;
     const int res = pr.P.res;
     const int tpr = (res + 15) / 16;
@@ -545,19 +490,7 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
         else if (tex) k_voxel<true, false><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
         else k_voxel<false, false><<<grid, block, 0, st>>>(pr.vq, pr.L, pr.P, dviews, view0, nviews, dout, stats);
     } else {
-#define XRP_GEN(H, D, F) \
-    k_render<H, D, F><<<grid, block, 0, st>>>(pr.S, pr.L, pr.P, dviews, view0, nviews, dout, stats)
-#define XRP_GEN_D(H, F)                  \
-    if (pr.depth == 0) XRP_GEN(H, 0, F); \
-    else if (pr.depth == 1) XRP_GEN(H, 1, F); \
-    else XRP_GEN(H, 3, F);
-        if (hier) {
-            if (pr.defs) { XRP_GEN_D(true, true) } else { XRP_GEN_D(true, false) }
-        } else {
-            if (pr.defs) { XRP_GEN_D(false, true) } else { XRP_GEN_D(false, false) }
-        }
-#undef XRP_GEN_D
-#undef XRP_GEN
+        return launch_scene(pr, view0, nviews, hier, dout, stats, st);
     }
     return cudaGetLastError();
 }
@@ -569,7 +502,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
                         const std::vector<const double*>& v64, const std::vector<ViewDev>& views,
                         const xrp_render_opts& o, double fov_max, float* out, bool out_host,
                         cudaStream_t st, cudaStream_t st_copy, bool want_stats,
-                        cudaTextureObject_t tex) {
+                        cudaTextureObject_t tex, const PropLaunch* pl = nullptr) {
     const int res = o.resolution;
     const int nviews = (int)views.size();
     PoolBuf tab;
@@ -591,7 +524,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     if (!out_host) {
         for (int v0 = 0; v0 < nviews; v0 += max_views_per_launch) {
             int n = std::min(max_views_per_launch, nviews - v0);
-            if ((e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st)) != cudaSuccess)
+            if ((e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st, pl)) != cudaSuccess)
                 return cuda_fail(7, "kernel launch", e);
         }
     } else {
@@ -612,7 +545,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
             if (c >= 2) cudaStreamWaitEvent(st, cev[b], 0);
             int v0 = (int)(c * chunk);
             int n = (int)std::min(chunk, (size_t)(nviews - v0));
-            cudaError_t le = launch(pr, v0, n, o.integration, (float*)buf[b].p, stats, st);
+            cudaError_t le = launch(pr, v0, n, o.integration, (float*)buf[b].p, stats, st, pl);
             cudaEventRecord(kev[b], st);
             return le;
         };
@@ -862,6 +795,424 @@ void xrp_release_cache(void) {
         cudaStreamSynchronize(kv.second->copy);
         cudaMemPoolTrimTo(kv.second->pool, 0);
     }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// learned proposal
+// ---------------------------------------------------------------------------
+
+struct xrp_proposal {
+    int device = -1;
+    float* params = nullptr;  // device, FP32 master parameters (MlpLayout)
+    float tau = 0.0f;
+    int segment = 64;
+    float fc[3] = {0, 0, 0}, fs[3] = {1, 1, 1};  // feature normalisation
+    xrp_proposal_info info;
+};
+
+static thread_local uint64_t t_prop_stats[kStatCount] = {0};
+
+namespace {
+
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+double unit_rand(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+bool proposal_scene_ok(const xrp_scene* s, const xrp_render_opts* o, std::string& why) {
+    if (o->integration != XRP_INTEGRATE_SIMPLE) {
+        why = "the proposal march supports the simple integrator only";
+        return false;
+    }
+    for (const HNode& n : s->hs.nodes)
+        if (n.type == N_VOXEL) {
+            why = "the proposal march supports analytic scenes only (no voxel grids)";
+            return false;
+        }
+    return true;
+}
+
+// Feature normalisation from the dilated support box.
+void feature_frame(const SceneDev& S, float fc[3], float fs[3]) {
+    for (int a = 0; a < 3; a++) {
+        float lo = S.sup_lo[a], hi = S.sup_hi[a];
+        if (!(hi > lo) || hi - lo > 1e30f) {
+            fc[a] = 0.0f;
+            fs[a] = 1.0f;
+        } else {
+            fc[a] = 0.5f * (lo + hi);
+            fs[a] = 2.0f / (hi - lo);
+        }
+    }
+}
+
+// Rows of training data: candidate segments of `nrays` random rays.
+int gen_rows(Engine* E, const Prepared& pr, int nviews, int res, int segment, const float fc[3],
+             const float fs[3], long nrays, uint64_t& rng, cudaStream_t st, PoolBuf& rays_buf, PoolBuf& X,
+             PoolBuf& y, PoolBuf& cnt, unsigned cap, unsigned* count_out) {
+    std::vector<int> rays(3 * (size_t)nrays);
+    for (long r = 0; r < nrays; r++) {
+        rays[3 * r] = (int)(splitmix(rng) % (uint64_t)nviews);
+        rays[3 * r + 1] = (int)(splitmix(rng) % (uint64_t)res);
+        rays[3 * r + 2] = (int)(splitmix(rng) % (uint64_t)res);
+    }
+    cudaError_t e;
+    if ((e = rays_buf.alloc(E, rays.size() * sizeof(int), st)) != cudaSuccess ||
+        (e = X.alloc(E, (size_t)cap * kMlpIn * sizeof(__nv_bfloat16), st)) != cudaSuccess ||
+        (e = y.alloc(E, (size_t)cap * sizeof(float), st)) != cudaSuccess ||
+        (e = cnt.alloc(E, sizeof(unsigned), st)) != cudaSuccess)
+        return cuda_fail(3, "proposal training buffers", e);
+    if ((e = cudaMemcpyAsync(rays_buf.p, rays.data(), rays.size() * sizeof(int), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(cnt.p, 0, sizeof(unsigned), st)) != cudaSuccess)
+        return cuda_fail(4, "proposal training upload", e);
+    PropLaunch pl;
+    memset(&pl.Q, 0, sizeof(pl.Q));
+    pl.train = true;
+    pl.Q.mc = segment;
+    for (int a = 0; a < 3; a++) {
+        pl.Q.fc[a] = fc[a];
+        pl.Q.fs[a] = fs[a];
+    }
+    pl.Q.rays = (const int*)rays_buf.p;
+    pl.Q.nrays = (int)nrays;
+    pl.Q.X = (__nv_bfloat16*)X.p;
+    pl.Q.y = (float*)y.p;
+    pl.Q.count = (unsigned*)cnt.p;
+    pl.Q.cap = cap;
+    if ((e = launch_prop(pr, 0, nviews, pl, nullptr, st)) != cudaSuccess)
+        return cuda_fail(7, "proposal training rows", e);
+    unsigned c = 0;
+    if ((e = cudaMemcpyAsync(&c, cnt.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return cuda_fail(7, "proposal training rows", e);
+    *count_out = std::min(c, cap);
+    return 0;
+}
+
+cudaError_t mlp_attrs_once() {
+    static std::mutex m;
+    static std::map<int, bool> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(m);
+    if (done[dev]) return cudaSuccess;
+    cudaError_t e = mlp_kernel_attrs();
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
+}
+
+// He-uniform initialisation of the hidden layers, small output layer.
+std::vector<float> mlp_init(uint64_t& rng) {
+    std::vector<float> p(MlpLayout::N, 0.0f);
+    auto fill = [&](int off, int n, double bound) {
+        for (int k = 0; k < n; k++) p[off + k] = (float)((2.0 * unit_rand(rng) - 1.0) * bound);
+    };
+    fill(MlpLayout::W1, kMlpHid * kMlpIn, std::sqrt(6.0 / kMlpIn));
+    fill(MlpLayout::W2, kMlpHid * kMlpHid, std::sqrt(6.0 / kMlpHid));
+    fill(MlpLayout::W3, kMlpHid * kMlpHid, std::sqrt(6.0 / kMlpHid));
+    fill(MlpLayout::W4, kMlpHid, std::sqrt(3.0 / kMlpHid));
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xrp_mlp_param_count(void) { return MlpLayout::N; }
+
+int xrp_mlp_grad(const float* params, const uint16_t* X, const float* y, int rows, float pos_weight,
+                 float* grad, float* loss, float* logits) {
+    if (!params || !X || !y) return fail(1, "null pointer");
+    if (rows <= 0) return fail(2, "rows must be > 0");
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    std::lock_guard<std::mutex> g(E->mtx);
+    cudaStream_t st = E->compute;
+    cudaError_t e = mlp_attrs_once();
+    if (e != cudaSuccess) return cuda_fail(7, "training kernel attributes", e);
+    PoolBuf dp, dX, dy, dg, dl, dlog;
+    const size_t N = MlpLayout::N;
+    if ((e = dp.alloc(E, N * 4, st)) != cudaSuccess || (e = dX.alloc(E, (size_t)rows * kMlpIn * 2, st)) != cudaSuccess ||
+        (e = dy.alloc(E, (size_t)rows * 4, st)) != cudaSuccess || (e = dg.alloc(E, N * 4, st)) != cudaSuccess ||
+        (e = dl.alloc(E, 4, st)) != cudaSuccess || (e = dlog.alloc(E, (size_t)rows * 4, st)) != cudaSuccess)
+        return cuda_fail(3, "gradient buffers", e);
+    if ((e = cudaMemcpyAsync(dp.p, params, N * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dX.p, X, (size_t)rows * kMlpIn * 2, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dy.p, y, (size_t)rows * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(dg.p, 0, N * 4, st)) != cudaSuccess || (e = cudaMemsetAsync(dl.p, 0, 4, st)) != cudaSuccess)
+        return cuda_fail(4, "gradient upload", e);
+    e = mlp_train_launch(st, (const float*)dp.p, (const __nv_bfloat16*)dX.p, (const float*)dy.p, nullptr,
+                         rows, pos_weight, 1.0f / (float)rows, (float*)dg.p, (float*)dl.p, (float*)dlog.p);
+    if (e != cudaSuccess) return cuda_fail(7, "training kernel launch", e);
+    if (grad && (e = cudaMemcpyAsync(grad, dg.p, N * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(7, "gradient read", e);
+    if (loss && (e = cudaMemcpyAsync(loss, dl.p, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(7, "loss read", e);
+    if (logits && (e = cudaMemcpyAsync(logits, dlog.p, (size_t)rows * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(7, "logit read", e);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(7, "training kernel", e);
+    return 0;
+}
+
+int xrp_proposal_train(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_render_opts* o,
+                       const xrp_proposal_opts* po, xrp_proposal** out) {
+    if (!s || !views || !o || !out) return fail(1, "null pointer");
+    *out = nullptr;
+    std::string why;
+    if (nviews <= 0) return fail(2, "num_views must be > 0");
+    if (!opts_ok(o, why) || !proposal_scene_ok(s, o, why)) return fail(2, "%s", why.c_str());
+    xrp_proposal_opts d;
+    memset(&d, 0, sizeof(d));
+    if (po) d = *po;
+    const int segment = d.segment ? d.segment : 64;
+    if (segment < 32 || segment > 4096 || segment % 32) return fail(2, "segment must be a multiple of 32 in [32, 4096]");
+    const long train_rays = d.train_rays > 0 ? d.train_rays : 65536;
+    const long val_rays = d.val_rays > 0 ? d.val_rays : 32768;
+    const int steps = d.steps > 0 ? d.steps : 2000;
+    const int batch = d.batch > 0 ? d.batch : 4096;
+    const float lr = d.lr > 0 ? d.lr : 2e-3f;
+    const float pw = d.pos_weight > 0 ? d.pos_weight : 8.0f;
+    const float tmargin = d.tau_margin;
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
+    double fov_max;
+    std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
+    std::lock_guard<std::mutex> g(E->mtx);
+    cudaStream_t st = E->compute;
+    auto t_start = std::chrono::steady_clock::now();
+    PoolBuf tab;
+    Prepared pr;
+    int rc = prepare(E, s->hs, s->vdev, s->v64, v, o->resolution, XRP_INTEGRATE_SIMPLE, o->ds, o->R,
+                     o->flat_field, o->density_multiplier, fov_max, st, tab, pr, 0);
+    if (rc) return rc;
+    auto P = std::make_unique<xrp_proposal>();
+    P->device = E->device;
+    P->segment = segment;
+    feature_frame(pr.S, P->fc, P->fs);
+    memset(&P->info, 0, sizeof(P->info));
+    P->info.segment = segment;
+    uint64_t rng = d.seed ^ 0x5eedull;
+    const long segs_per_ray = (pr.L.K + segment - 1) / segment + 1;
+    const unsigned cap_t = (unsigned)std::min<long>(train_rays * segs_per_ray, 1L << 22);
+    const unsigned cap_v = (unsigned)std::min<long>(val_rays * segs_per_ray, 1L << 22);
+    PoolBuf rays_t, X_t, y_t, c_t, rays_v, X_v, y_v, c_v;
+    unsigned n_t = 0, n_v = 0;
+    if (!pr.empty) {
+        if ((rc = gen_rows(E, pr, nviews, o->resolution, segment, P->fc, P->fs, train_rays, rng, st, rays_t, X_t, y_t, c_t, cap_t, &n_t)))
+            return rc;
+        if ((rc = gen_rows(E, pr, nviews, o->resolution, segment, P->fc, P->fs, val_rays, rng, st, rays_v, X_v, y_v, c_v, cap_v, &n_v)))
+            return rc;
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc(&P->params, MlpLayout::N * sizeof(float))) != cudaSuccess)
+        return cuda_fail(3, "proposal parameters", e);
+    std::unique_ptr<xrp_proposal, void (*)(xrp_proposal*)> guard(P.release(), xrp_proposal_destroy);
+    xrp_proposal* Pp = guard.get();
+    std::vector<float> init = mlp_init(rng);
+    if ((e = cudaMemcpyAsync(Pp->params, init.data(), init.size() * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(4, "proposal parameters", e);
+    if ((e = mlp_attrs_once()) != cudaSuccess) return cuda_fail(7, "training kernel attributes", e);
+    std::vector<float> ylab;
+    if (n_t > 0) {
+        ylab.resize(n_t);
+        if ((e = cudaMemcpyAsync(ylab.data(), y_t.p, n_t * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return cuda_fail(7, "training labels", e);
+        for (float q : ylab) Pp->info.train_pos += q > 0.5f;
+        Pp->info.train_rows = n_t;
+        // Adam: batches drawn with replacement, linear decay of the rate
+        const size_t N = MlpLayout::N;
+        PoolBuf grad, m1, m2, idx, lossb;
+        std::vector<int> hidx((size_t)steps * batch);
+        for (auto& q : hidx) q = (int)(splitmix(rng) % n_t);
+        if ((e = grad.alloc(E, N * 4, st)) != cudaSuccess || (e = m1.alloc(E, N * 4, st)) != cudaSuccess ||
+            (e = m2.alloc(E, N * 4, st)) != cudaSuccess || (e = idx.alloc(E, hidx.size() * 4, st)) != cudaSuccess ||
+            (e = lossb.alloc(E, (size_t)steps * 4, st)) != cudaSuccess)
+            return cuda_fail(3, "training buffers", e);
+        cudaMemsetAsync(grad.p, 0, N * 4, st);
+        cudaMemsetAsync(m1.p, 0, N * 4, st);
+        cudaMemsetAsync(m2.p, 0, N * 4, st);
+        cudaMemsetAsync(lossb.p, 0, (size_t)steps * 4, st);
+        if ((e = cudaMemcpyAsync(idx.p, hidx.data(), hidx.size() * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_fail(4, "training batches", e);
+        double b1p = 1.0, b2p = 1.0;
+        for (int it = 0; it < steps && e == cudaSuccess; it++) {
+            e = mlp_train_launch(st, Pp->params, (const __nv_bfloat16*)X_t.p, (const float*)y_t.p,
+                                 (const int*)idx.p + (size_t)it * batch, batch, pw, 1.0f / (float)batch,
+                                 (float*)grad.p, (float*)lossb.p + it, nullptr);
+            b1p *= 0.9;
+            b2p *= 0.999;
+            float rate = lr * (1.0f - 0.9f * (float)it / (float)steps);
+            if (e == cudaSuccess)
+                e = mlp_adam_launch(st, Pp->params, (float*)grad.p, (float*)m1.p, (float*)m2.p, (int)N, rate,
+                                    0.9f, 0.999f, 1e-8f, (float)(1.0 / (1.0 - b1p)), (float)(1.0 / (1.0 - b2p)));
+        }
+        if (e != cudaSuccess) return cuda_fail(7, "training launch", e);
+        std::vector<float> hl(steps);
+        if ((e = cudaMemcpyAsync(hl.data(), lossb.p, (size_t)steps * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return cuda_fail(7, "training", e);
+        int tail = std::max(1, steps / 10);
+        double sl = 0;
+        for (int k = steps - tail; k < steps; k++) sl += hl[k];
+        Pp->info.final_loss = (float)(sl / tail);
+    }
+    float tau = std::log(pw) + tmargin;
+    if (n_v > 0 && n_t > 0) {
+        PoolBuf lg;
+        if ((e = lg.alloc(E, (size_t)n_v * 4, st)) != cudaSuccess) return cuda_fail(3, "validation buffers", e);
+        e = mlp_logits_launch(st, Pp->params, (const __nv_bfloat16*)X_v.p, (int)n_v, (float*)lg.p);
+        if (e != cudaSuccess) return cuda_fail(7, "validation launch", e);
+        std::vector<float> hl(n_v), hy(n_v);
+        if ((e = cudaMemcpyAsync(hl.data(), lg.p, (size_t)n_v * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(hy.data(), y_v.p, (size_t)n_v * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return cuda_fail(7, "validation", e);
+        long long npos = 0;
+        for (unsigned k = 0; k < n_v; k++) npos += hy[k] > 0.5f;
+        // routing threshold: a candidate goes dense when the network's
+        // (class-weight corrected) probability of a transition exceeds 1/2
+        tau = std::log(pw) + tmargin;
+        long long acc = 0;
+        for (unsigned k = 0; k < n_v; k++) acc += (hl[k] <= tau);
+        Pp->info.val_rows = n_v;
+        Pp->info.val_pos = npos;
+        Pp->info.val_accepted = acc;
+    }
+    Pp->tau = tau;
+    Pp->info.tau = tau;
+    Pp->info.train_ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    *out = guard.release();
+    return 0;
+}
+
+int xrp_proposal_get_info(const xrp_proposal* p, xrp_proposal_info* out) {
+    if (!p || !out) return fail(1, "null pointer");
+    *out = p->info;
+    return 0;
+}
+
+int xrp_proposal_params(const xrp_proposal* p, float* out, int n) {
+    if (!p || !out) return fail(1, "null pointer");
+    if (n < MlpLayout::N) return fail(2, "need %d floats", MlpLayout::N);
+    cudaError_t e = cudaMemcpy(out, p->params, MlpLayout::N * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(7, "parameter read", e);
+    return 0;
+}
+
+int xrp_proposal_set_tau(xrp_proposal* p, float tau) {
+    if (!p) return fail(1, "null pointer");
+    p->tau = tau;
+    return 0;
+}
+
+void xrp_proposal_destroy(xrp_proposal* p) {
+    if (!p) return;
+    if (p->params) cudaFree(p->params);
+    delete p;
+}
+
+static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, const xrp_camera* views,
+                           int nviews, const xrp_render_opts* o, float* out, bool out_host, void* stream) {
+    if (!s || !views || !o || !out) return fail(1, "null pointer");
+    std::string why;
+    if (nviews <= 0) return fail(2, "num_views must be > 0");
+    if (!opts_ok(o, why) || !proposal_scene_ok(s, o, why)) return fail(2, "%s", why.c_str());
+    if (segment == 0) segment = prop ? prop->segment : 64;
+    if (segment < 32 || segment > 4096 || segment % 32) return fail(2, "segment must be a multiple of 32 in [32, 4096]");
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
+    if (prop && prop->device != s->device) return fail(2, "proposal belongs to device %d", prop->device);
+    double fov_max;
+    std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
+    std::unique_lock<std::mutex> g(E->mtx, std::defer_lock);
+    if (out_host) g.lock();
+    cudaStream_t st = out_host ? E->compute : (cudaStream_t)stream;
+    const bool want_stats = out_host && (o->flags & XRP_FLAG_STATS);
+    PoolBuf sb;
+    PropLaunch pl;
+    memset(&pl.Q, 0, sizeof(pl.Q));
+    pl.Q.mc = segment;
+    pl.Q.refine = (o->flags & XRP_FLAG_NO_REFINE) ? 0 : 1;
+    pl.Q.min_piece = 8;
+    if (prop) {
+        pl.Q.mlp = prop->params;
+        pl.Q.tau = prop->tau;
+        for (int a = 0; a < 3; a++) {
+            pl.Q.fc[a] = prop->fc[a];
+            pl.Q.fs[a] = prop->fs[a];
+        }
+    }
+    cudaError_t e;
+    if (want_stats) {
+        if ((e = sb.alloc(E, kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
+            return cuda_fail(3, "stats buffer", e);
+        if ((e = cudaMemsetAsync(sb.p, 0, kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
+            return cuda_fail(7, "stats reset", e);
+        pl.Q.stats = (unsigned long long*)sb.p;
+    }
+    // list of samples for FP64 re-evaluation (per launch; reused)
+    const unsigned fb_cap = 1u << 22;
+    PoolBuf fb, fbc;
+    if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
+        (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)
+        return cuda_fail(3, "fallback list", e);
+    if ((e = cudaMemsetAsync(fbc.p, 0, 2 * sizeof(unsigned), st)) != cudaSuccess)
+        return cuda_fail(7, "fallback list reset", e);
+    pl.Q.fb = (uint2*)fb.p;
+    pl.Q.fb_count = (unsigned*)fbc.p;
+    pl.Q.fb_overflow = (unsigned*)fbc.p + 1;
+    pl.Q.fb_cap = fb_cap;
+    xrp_render_opts oo = *o;
+    int rc = render_views(E, s->hs, s->vdev, s->v64, v, oo, fov_max, out, out_host, st,
+                          out_host ? E->copy : st, false, 0, &pl);
+    if (rc) return rc;
+    // an overflowed list (more undecided samples in one launch than it
+    // holds) is not expected; the plain integrator then renders the call
+    unsigned ovf = 0;
+    if ((e = cudaMemcpyAsync(&ovf, pl.Q.fb_overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return cuda_fail(7, "proposal march", e);
+    if (ovf) {
+        rc = render_views(E, s->hs, s->vdev, s->v64, v, oo, fov_max, out, out_host, st,
+                          out_host ? E->copy : st, false, 0, nullptr);
+        if (rc) return rc;
+    }
+    if (want_stats) {
+        unsigned long long h[kStatCount];
+        if ((e = cudaMemcpyAsync(h, sb.p, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return cuda_fail(7, "stats read", e);
+        for (int q = 0; q < kStatCount; q++) t_prop_stats[q] = h[q];
+    }
+    return 0;
+}
+
+int xrp_render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, const xrp_camera* views,
+                        int nviews, const xrp_render_opts* o, float* out) {
+    return render_proposal(s, prop, segment, views, nviews, o, out, true, nullptr);
+}
+
+int xrp_render_proposal_device(xrp_scene* s, const xrp_proposal* prop, int segment, const xrp_camera* views,
+                               int nviews, const xrp_render_opts* o, float* out_device, void* stream) {
+    return render_proposal(s, prop, segment, views, nviews, o, out_device, false, stream);
+}
+
+int xrp_proposal_last_stats(uint64_t out[10]) {
+    if (!out) return fail(1, "null pointer");
+    for (int q = 0; q < kStatCount; q++) out[q] = t_prop_stats[q];
+    return 0;
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,37 @@
+// xrp_kern_prop.cu -- the proposal march's rendering kernels
+// (xrp_proposal.cuh), specialised like the general-scene kernel.
+#define XRP_PROP_RENDER_KERNELS
+#include "xrp_launch.h"
+
+namespace xrp {
+
+static cudaError_t march(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                         cudaStream_t st) {
+    XRP_PROP_DISPATCH(false, dout)
+}
+
+// March (optical depths), FP64 for the samples it left undecided, exp(-T).
+cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,
+                               float* dout, cudaStream_t st) {
+    const long rays = (long)nviews * pr.P.res * pr.P.res;
+    if (rays <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(Q.fb_count, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    if ((e = march(pr, view0, nviews, Q, dout, st)) != cudaSuccess) return e;
+    static int fb_grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& g = fb_grid[dev & 7];
+    if (!g) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        g = sms * 4;
+    }
+    k_prop_fallback<<<g, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, Q.fb, Q.fb_count, Q.fb_cap,
+                                      dout, Q.stats, Q.fb_overflow);
+    long fin = (rays + 255) / 256;
+    k_prop_finish<<<(unsigned)(fin < 65536 ? fin : 65536), 256, 0, st>>>(dout, rays);
+    return cudaGetLastError();
+}
+
+}  // namespace xrp

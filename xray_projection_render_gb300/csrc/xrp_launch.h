@@ -1,0 +1,119 @@
+// xrp_launch.h -- what the engine's host code shares with the kernel
+// translation units: the prepared render state and the launchers.
+//
+// The kernels are split over several translation units (general scenes,
+// proposal march, training) so they compile in parallel; each unit owns its
+// launchers, declared here.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "xrp_device.h"
+#include "xrp_proposal.cuh"
+
+namespace xrp {
+
+// Parameters of a voxel-grid root (no deformation), read by the voxel
+// kernels from their constant bank so the march keeps few live registers.
+struct VoxParams {
+    cudaTextureObject_t tex;  // layered texture of the grid (gather path)
+    const float* data;        // [z][x][y] (load path, FP64 re-evaluation)
+    const double* data64;     // exact values when FP32 cannot hold them, else null
+    int nx, ny, nz;
+    int zero_guard;           // hierarchical integrator: guard the density == 0 test
+    float scale[3];           // (N-1)/2
+    float inv_scale[3];
+    float band_w;             // world-space guard band of the inclusive [-1,1] test
+    float band_zero;          // relative band of the zero test
+    float inner_margin;       // clip margin of the bounds-free interior range
+    float lo[3], hi[3];       // dilated support box
+};
+
+// Everything a render needs on the device except the volume data.
+struct Prepared {
+    SceneDev S;
+    Lattice L;
+    RenderParams P;
+    const ViewDev* views = nullptr;
+    bool volume_fast = false;
+    cudaTextureObject_t tex = 0;  // layered texture of the root grid (0: use loads)
+    VoxParams vq;                 // voxel-grid root parameters (volume_fast)
+    int depth = kMaxDepth;        // kernel specialisation of general scenes
+    bool defs = true;
+    bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
+};
+
+// A proposal-march launch (see xrp_proposal.cuh); Q's scene-independent
+// fields are filled in by the caller.
+struct PropLaunch {
+    PropParams Q;
+    bool train = false;
+};
+
+// xrp_kern_scene.cu: k_render for general scenes.
+cudaError_t launch_scene(const Prepared& pr, int view0, int nviews, bool hier, float* dout,
+                         unsigned long long* stats, cudaStream_t st);
+
+// xrp_kern_prop.cu: the proposal march (rendering).
+cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,
+                               float* dout, cudaStream_t st);
+
+// xrp_kern_train.cu: training-row generation and the network's kernels.
+cudaError_t launch_prop_train(const Prepared& pr, int view0, int nviews, const PropParams& Q,
+                              cudaStream_t st);
+cudaError_t mlp_kernel_attrs();
+cudaError_t mlp_train_launch(cudaStream_t st, const float* params, const __nv_bfloat16* X,
+                             const float* y, const int* idx, int rows, float pos_weight,
+                             float inv_batch, float* grad, float* loss, float* logits);
+cudaError_t mlp_adam_launch(cudaStream_t st, float* params, float* grad, float* m1, float* m2, int n,
+                            float lr, float b1, float b2, float eps, float c1, float c2);
+cudaError_t mlp_logits_launch(cudaStream_t st, const float* params, const __nv_bfloat16* X, int rows,
+                              float* logits);
+
+// Grid of a persistent proposal launch: resident blocks x SMs (cached per
+// kernel and device).
+template <class K>
+cudaError_t persistent_grid(K kern, size_t smem, int block, int* out) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int nb = 0, dev = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block, smem)) != cudaSuccess) return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    *out = sms * (nb > 0 ? nb : 1);
+    return cudaSuccess;
+}
+
+// One proposal-march launch, persistent grid (xrp_kern_prop.cu and
+// xrp_kern_train.cu instantiate it).
+template <int DEPTH, bool DEFS, bool TRAIN>
+cudaError_t launch_prop_t(const Prepared& pr, int view0, int nviews, const PropParams& Q,
+                          float* dout, cudaStream_t st) {
+    auto kern = k_propose<DEPTH, DEFS, TRAIN>;
+    static int grid_cache[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per device (first 8)
+    const size_t smem = sizeof(PropShared);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& gmax = grid_cache[dev & 7];
+    if (!gmax) {
+        cudaError_t e = persistent_grid(kern, smem, 32 * kPropWarps, &gmax);
+        if (e != cudaSuccess) return e;
+    }
+    long rays = Q.rays ? (long)Q.nrays : (long)nviews * pr.P.res * pr.P.res;
+    long need = (rays + 32 * kPropWarps - 1) / (32 * kPropWarps);  // 32 rays per warp batch
+    long grid = need < gmax ? need : gmax;
+    if (grid <= 0) return cudaSuccess;
+    kern<<<(unsigned)grid, 32 * kPropWarps, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0, nviews, Q, dout);
+    return cudaGetLastError();
+}
+
+#define XRP_PROP_DISPATCH(T, OUT)                                                   \
+    if (pr.defs) {                                                                 \
+        if (pr.depth == 0) return launch_prop_t<0, true, T>(pr, view0, nviews, Q, OUT, st);  \
+        if (pr.depth == 1) return launch_prop_t<1, true, T>(pr, view0, nviews, Q, OUT, st);  \
+        return launch_prop_t<3, true, T>(pr, view0, nviews, Q, OUT, st);                     \
+    }                                                                              \
+    if (pr.depth == 0) return launch_prop_t<0, false, T>(pr, view0, nviews, Q, OUT, st);     \
+    if (pr.depth == 1) return launch_prop_t<1, false, T>(pr, view0, nviews, Q, OUT, st);     \
+    return launch_prop_t<3, false, T>(pr, view0, nviews, Q, OUT, st);
+
+}  // namespace xrp

@@ -1,0 +1,482 @@
+// xrp_proposal.cuh -- the proposal march: a learned proposal network plus
+// distance certificates on top of the plain integrator.
+//
+// One warp marches one ray.  The ray's clipped sample range [k0, k1] (the
+// same samples the plain integrator sums) is cut into segments of `mc`
+// samples, 32 segments per round, one per lane.  Each lane evaluates the
+// density and the certificate radius (margin32) at its segment's first
+// sample; the segment's end point is the next segment's first sample.
+// A segment is counted as (number of samples) x (density) when
+//   (a) both end densities are certain and equal, and
+//   (b) either the two certificate balls cover the segment (exact), or the
+//       network's logit for the segment is at most tau (learned).
+// Every other segment is integrated densely by the whole warp, sample by
+// sample, exactly as the plain integrator does (FP32 guarded evaluation).
+// The march writes optical depths; samples FP32 cannot decide go to a list
+// that a second kernel evaluates in FP64 (reference arithmetic) and adds,
+// and a third kernel forms exp(-T).  Keeping FP64 code out of the march
+// keeps its register budget at two blocks per SM.
+//
+// Training data comes from the same march (TRAIN = true): every segment that
+// (a) admits and (b)'s certificate does not settle is integrated densely and
+// labelled 1 when any of its densities differs from the first (or is
+// uncertain in FP32).
+#pragma once
+#include "xrp_train.cuh"
+
+namespace xrp {
+
+struct PropParams {
+    const float* mlp;              // FP32 parameter block (MlpLayout); null: certificate only
+    int mc;                        // samples per segment (multiple of 32)
+    float tau;                     // logits above tau send a candidate to dense integration
+    int refine;                    // 1: refine candidates by certificates; 0: dense
+    int min_piece;                 // pieces of at most this many samples go dense
+    float fc[3], fs[3];            // feature normalisation (p - fc) * fs
+    const int* rays;               // optional ray list: (view, i, j) triples, views absolute
+    int nrays;                     // number of listed rays
+    unsigned long long* stats;     // optional counters, see kPropStat*
+    // training rows (TRAIN): features, labels, capacity, row counter
+    __nv_bfloat16* X;
+    float* y;
+    unsigned* count;
+    unsigned cap;
+    // samples left to FP64 (rendering): (ray, sample) pairs, counter,
+    // capacity, and a flag raised when the list overflowed
+    uint2* fb;
+    unsigned* fb_count;
+    unsigned fb_cap;
+    unsigned* fb_overflow;
+};
+
+enum : int {
+    kStatSegments = 0,  // segments visited
+    kStatCertified,     // segments counted on their end-point certificate
+    kStatRefined,       // pieces counted on a certificate during refinement
+    kStatDense,         // pieces integrated densely
+    kStatDenseSamples,  // samples evaluated by dense integration
+    kStatEvaluations,   // certificate evaluations (density + radius)
+    kStatFallbacks,     // samples re-evaluated in FP64
+    kStatMlpRounds,     // warp-wide network evaluations (32 rows each)
+    kStatRoutedDense,   // candidates the network sent to dense integration
+    kStatSubdivided,    // candidates refined by certificates
+    kStatCount
+};
+
+// Per-warp work lists of the refinement: a stack of pieces (sample range
+// [a, b] with the density and certificate radius at both ends, n samples
+// counted) and a list of pieces to integrate densely.
+constexpr int kStackCap = 128;
+constexpr int kDenseCap = 160;
+struct WarpLists {
+    int a[kStackCap], b[kStackCap], n[kStackCap];
+    float ra[kStackCap], ma[kStackCap], rb[kStackCap], mb[kStackCap];
+    int da[kDenseCap], dn[kDenseCap];
+};
+
+constexpr int kPropWarps = 8;
+
+struct PropShared {
+    MlpShared W;
+    __nv_bfloat16 rows[kPropWarps][32 * kMlpLd];
+    WarpLists lists[kPropWarps];
+    unsigned stats[kStatCount];
+};
+
+#if defined(__CUDACC__)
+
+__device__ __forceinline__ void load_mlp_shared(const float* __restrict__ p, MlpShared& W) {
+    for (int q = threadIdx.x; q < kMlpHid * kMlpIn; q += blockDim.x) {
+        int o = q / kMlpIn, i = q % kMlpIn;
+        W.w[0][o * kMlpLd + i] = __float2bfloat16_rn(p[MlpLayout::W1 + q]);
+        W.w[1][o * kMlpLd + i] = __float2bfloat16_rn(p[MlpLayout::W2 + q]);
+        W.w[2][o * kMlpLd + i] = __float2bfloat16_rn(p[MlpLayout::W3 + q]);
+    }
+    for (int q = threadIdx.x; q < kMlpHid; q += blockDim.x) {
+        W.b[0][q] = p[MlpLayout::B1 + q];
+        W.b[1][q] = p[MlpLayout::B2 + q];
+        W.b[2][q] = p[MlpLayout::B3 + q];
+        W.w4[q] = p[MlpLayout::W4 + q];
+    }
+    if (threadIdx.x == 0) W.b4 = p[MlpLayout::B4];
+}
+
+// Writes the feature row of segment (a, b) (world points) into `row`.
+__device__ __forceinline__ void write_features(const PropParams& Q, const float* a, const float* b,
+                                               __nv_bfloat16* row) {
+    float an[3], bn[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        an[c] = (a[c] - Q.fc[c]) * Q.fs[c];
+        bn[c] = (b[c] - Q.fc[c]) * Q.fs[c];
+    }
+    segment_features(an, bn, [&](int k, float v) { row[k] = __float2bfloat16_rn(v); });
+}
+
+// Density and certificate radius at one point.  Not inlined: the march
+// evaluates points at three places (segment ends, own end, refinement
+// middles) and one shared body keeps the kernel inside the instruction
+// cache; the hot dense loop keeps its own inlined density evaluation.
+template <int DEPTH, bool DEFS>
+__device__ __noinline__ float2 eval_dm(const SceneDev& S, float x, float y, float z) {
+    return make_float2(density32<DEPTH, DEFS>(S, x, y, z), margin32<DEPTH, DEFS>(S, x, y, z));
+}
+
+// Dense integration of the listed pieces, the warp's lanes over each
+// piece's samples; undecided samples go to the FP64 list.
+template <class Smp, class Count>
+__device__ __forceinline__ void dense_pass(const WarpLists& ws, int nd, const Smp& smp, const Lattice& L,
+                                           const PropParams& Q, long ray, KahanF& acc, Count& count) {
+    const int lane = threadIdx.x & 31;
+    count(kStatDense, (unsigned)nd);
+    for (int q = 0; q < nd; q++) {
+        const int a = ws.da[q], n = ws.dn[q];
+        count(kStatDenseSamples, (unsigned)n);
+        for (int k = a + lane; k < a + n; k += 32) {
+            float rho = smp.f32(lattice_t(L, k));
+            if (isunc(rho)) {
+                unsigned slot = atomicAdd(Q.fb_count, 1u);
+                if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)ray, (unsigned)k);
+                rho = 0.0f;
+            }
+            acc.add(rho);
+        }
+    }
+    __syncwarp();
+}
+
+template <int DEPTH, bool DEFS, bool TRAIN>
+__global__ void __launch_bounds__(32 * kPropWarps, 2)
+    k_propose(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
+              const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
+              int nviews, const __grid_constant__ PropParams Q, float* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char prop_smem[];
+    PropShared& sh = *reinterpret_cast<PropShared*>(prop_smem);
+    const bool use_mlp = !TRAIN && Q.mlp != nullptr;
+    if (use_mlp) load_mlp_shared(Q.mlp, sh.W);
+    if (threadIdx.x < kStatCount) sh.stats[threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __nv_bfloat16* xrow = sh.rows[warp];
+    WarpLists& ws = sh.lists[warp];
+    const int res = P.res;
+    const long img = (long)res * res;
+    const long total = Q.rays ? (long)Q.nrays : (long)nviews * img;
+    const long gw = (long)blockIdx.x * kPropWarps + warp;
+    const long tw = (long)gridDim.x * kPropWarps;
+    const bool stats = Q.stats != nullptr;
+    // warp-aggregated counter update (lane 0 adds the warp's total)
+    auto count = [&](int which, unsigned n) {
+        if (stats && lane == 0 && n) atomicAdd(&sh.stats[which], n);
+    };
+    const int mc = Q.mc;
+
+    // Rays go in batches of 32: each lane sets up one ray (the FP64 setup
+    // runs once per ray, SIMT over the batch), then the warp marches the
+    // batch's rays one after another, each cooperatively.
+    for (long rb = gw * 32; rb < total; rb += tw * 32) {
+        const long r = rb + lane;
+        const bool rvalid = r < total;
+        int v = 0, i = 0, j = 0;
+        if (rvalid) {
+            if (Q.rays) {
+                v = Q.rays[3 * r];
+                i = Q.rays[3 * r + 1];
+                j = Q.rays[3 * r + 2];
+            } else {
+                v = view0 + (int)(r / img);
+                long pix = r % img;
+                i = (int)(pix / res);
+                j = (int)(pix % res);
+            }
+        }
+        Ray myray;
+        int my_k0 = 0, my_k1 = -1;
+        if (rvalid) {
+            Ray64 r64;
+            setup_ray64(views[v], P.xs, i, j, r64);
+            setup_ray32(r64, L.s_c, myray);
+            float t0, t1;
+            clip_ray(S.sup_lo, S.sup_hi, myray, t0, t1);
+            if (!sample_range(L, t0, t1, L.K, my_k0, my_k1)) {
+                my_k0 = 0;
+                my_k1 = -1;
+            }
+        }
+        float result = 0.0f;
+        const int nb = (int)min((long)32, total - rb);
+        for (int q = 0; q < nb; q++) {
+            Ray ray;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                ray.pc[c] = __shfl_sync(FULL, myray.pc[c], q);
+                ray.d32[c] = __shfl_sync(FULL, myray.d32[c], q);
+            }
+            const int k0 = __shfl_sync(FULL, my_k0, q), k1 = __shfl_sync(FULL, my_k1, q);
+            const int qv = __shfl_sync(FULL, v, q), qi = __shfl_sync(FULL, i, q),
+                      qj = __shfl_sync(FULL, j, q);
+            PixelRef px{views + qv, P.xs, qi, qj};
+            SceneSampler<DEPTH, DEFS> smp{S, ray, px};
+            KahanF acc;
+            for (int base = k0; base <= k1; base += 32 * mc) {
+                int a = base + lane * mc;
+                const bool valid = a <= k1;
+                if (!valid) a = k1;
+                const int e = min(a + mc, k1 + 1);  // samples [a, e) belong to the segment
+                const int ee = min(e, k1);          // end point of the certificate
+                const float ta = lattice_t(L, a), te = lattice_t(L, ee);
+                float pa[3], pe[3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    pa[c] = fmaf(ray.d32[c], ta, ray.pc[c]);
+                    pe[c] = fmaf(ray.d32[c], te, ray.pc[c]);
+                }
+                float rho_a = 0.0f, m_a = 0.0f;
+                if (valid) {
+                    const float2 dm = eval_dm<DEPTH, DEFS>(S, pa[0], pa[1], pa[2]);
+                    rho_a = dm.x;
+                    m_a = dm.y;
+                }
+                float rho_e = __shfl_down_sync(FULL, rho_a, 1);
+                float m_e = __shfl_down_sync(FULL, m_a, 1);
+                const bool own_end = valid && (lane == 31 || a + mc > k1);
+                if (own_end) {
+                    const float2 dm = eval_dm<DEPTH, DEFS>(S, pe[0], pe[1], pe[2]);
+                    rho_e = dm.x;
+                    m_e = dm.y;
+                }
+                const unsigned nvalid = __popc(__ballot_sync(FULL, valid));
+                count(kStatSegments, nvalid);
+                count(kStatEvaluations, nvalid + __popc(__ballot_sync(FULL, own_end)));
+                const bool same = valid && !isunc(rho_a) && !isunc(rho_e) && rho_a == rho_e;
+                const bool cert = same && (m_a + m_e >= (float)(ee - a) * L.ds32 * 1.00001f);
+                const bool cand = same && !cert;  // refined by certificates or densely
+                if constexpr (TRAIN) {
+                    // label each candidate: does any of its densities differ?
+                    if (cand) write_features(Q, pa, pe, xrow + lane * kMlpLd);
+                    __syncwarp();
+                    unsigned mask = __ballot_sync(FULL, cand);
+                    while (mask) {
+                        const int s = __ffs(mask) - 1;
+                        mask &= mask - 1;
+                        const int sa = __shfl_sync(FULL, a, s), se = __shfl_sync(FULL, e, s);
+                        const float rho0 = __shfl_sync(FULL, rho_a, s);
+                        bool differs = false;
+                        for (int k = sa + 1 + lane; k < se; k += 32) {
+                            float rho = smp.f32(lattice_t(L, k));
+                            differs |= isunc(rho) || rho != rho0;
+                        }
+                        const bool lab = __any_sync(FULL, differs);
+                        unsigned slot = 0;
+                        if (lane == s) slot = atomicAdd(Q.count, 1u);
+                        slot = __shfl_sync(FULL, slot, s);
+                        if (slot < Q.cap) {
+                            const uint32_t* src = reinterpret_cast<const uint32_t*>(xrow + s * kMlpLd);
+                            uint32_t* dst = reinterpret_cast<uint32_t*>(Q.X + (size_t)slot * kMlpIn);
+                            dst[lane] = src[lane];
+                            if (lane == 0) Q.y[slot] = lab ? 1.0f : 0.0f;
+                        }
+                    }
+                    __syncwarp();
+                } else {
+                    // the network routes candidates: likely transitions -> dense,
+                    // the rest -> refinement by certificates
+                    bool to_dense = cand && !Q.refine;
+                    if (use_mlp && Q.refine && __any_sync(FULL, cand)) {
+                        write_features(Q, pa, pe, xrow + lane * kMlpLd);
+                        __syncwarp();
+                        float logit = mlp_forward_warp(sh.W, xrow);
+                        __syncwarp();
+                        to_dense = cand && logit > Q.tau;
+                        count(kStatMlpRounds, 1);
+                    }
+                    if (cert) acc.add(rho_a * (float)(e - a));
+                    count(kStatCertified, __popc(__ballot_sync(FULL, cert)));
+                    const bool sub = cand && !to_dense;
+                    const bool dense = valid && !cert && !sub;
+                    const unsigned smask = __ballot_sync(FULL, sub), dmask = __ballot_sync(FULL, dense);
+                    count(kStatRoutedDense, __popc(__ballot_sync(FULL, cand && to_dense && use_mlp)));
+                    count(kStatSubdivided, __popc(smask));
+                    const unsigned lt = (1u << lane) - 1u;
+                    // the stack and the dense list are empty at this point
+                    if (sub) {
+                        const int q2 = __popc(smask & lt);
+                        ws.a[q2] = a;
+                        ws.b[q2] = ee;
+                        ws.n[q2] = e - a;
+                        ws.ra[q2] = rho_a;
+                        ws.ma[q2] = m_a;
+                        ws.rb[q2] = rho_e;
+                        ws.mb[q2] = m_e;
+                    }
+                    if (dense) {
+                        const int q2 = __popc(dmask & lt);
+                        ws.da[q2] = a;
+                        ws.dn[q2] = e - a;
+                    }
+                    int sp = __popc(smask), nd = __popc(dmask);
+                    __syncwarp();
+                    // refinement waves: split each piece at its middle sample,
+                    // certify the halves, push the rest (dense below min_piece)
+                    while (sp > 0) {
+                        if (nd > kDenseCap - 64) {
+                            dense_pass(ws, nd, smp, L, Q, rb + q, acc, count);
+                            nd = 0;
+                        }
+                        const int take = min(sp, 32);
+                        sp -= take;
+                        const bool have = lane < take;
+                        int pa_ = 0, pb_ = 0, pn = 0;
+                        float pra = 0.f, pma = 0.f, prb = 0.f, pmb = 0.f;
+                        if (have) {
+                            pa_ = ws.a[sp + lane];
+                            pb_ = ws.b[sp + lane];
+                            pn = ws.n[sp + lane];
+                            pra = ws.ra[sp + lane];
+                            pma = ws.ma[sp + lane];
+                            prb = ws.rb[sp + lane];
+                            pmb = ws.mb[sp + lane];
+                        }
+                        __syncwarp();
+                        const int mid = (pa_ + pb_) >> 1;
+                        float rm = 0.0f, mm = 0.0f;
+                        if (have) {
+                            const float tm = lattice_t(L, mid);
+                            const float x = fmaf(ray.d32[0], tm, ray.pc[0]);
+                            const float y = fmaf(ray.d32[1], tm, ray.pc[1]);
+                            const float z = fmaf(ray.d32[2], tm, ray.pc[2]);
+                            const float2 dm = eval_dm<DEPTH, DEFS>(S, x, y, z);
+                            rm = dm.x;
+                            mm = dm.y;
+                        }
+                        count(kStatEvaluations, (unsigned)take);
+                        const int nl = mid - pa_, nr = pn - nl;
+                        const bool mok = have && !isunc(rm);
+                        const bool lcert = mok && rm == pra && pma + mm >= (float)(mid - pa_) * L.ds32 * 1.00001f;
+                        const bool rcert = mok && rm == prb && mm + pmb >= (float)(pb_ - mid) * L.ds32 * 1.00001f;
+                        if (lcert) acc.add(pra * (float)nl);
+                        if (rcert) acc.add(prb * (float)nr);
+                        count(kStatRefined, __popc(__ballot_sync(FULL, lcert)) + __popc(__ballot_sync(FULL, rcert)));
+                        // children: split further while long enough, else dense
+                        const bool room = sp + 2 * take <= kStackCap;
+                        const bool lsplit = have && !lcert && mok && nl > Q.min_piece && room;
+                        const bool rsplit = have && !rcert && mok && nr > Q.min_piece && room;
+                        const bool ldense = have && !lcert && !lsplit && nl > 0;
+                        const bool rdense = have && !rcert && !rsplit && nr > 0;
+                        const unsigned mls = __ballot_sync(FULL, lsplit), mrs = __ballot_sync(FULL, rsplit);
+                        const unsigned mld = __ballot_sync(FULL, ldense), mrd = __ballot_sync(FULL, rdense);
+                        if (lsplit) {
+                            const int q2 = sp + __popc(mls & lt);
+                            ws.a[q2] = pa_; ws.b[q2] = mid; ws.n[q2] = nl;
+                            ws.ra[q2] = pra; ws.ma[q2] = pma; ws.rb[q2] = rm; ws.mb[q2] = mm;
+                        }
+                        if (rsplit) {
+                            const int q2 = sp + __popc(mls) + __popc(mrs & lt);
+                            ws.a[q2] = mid; ws.b[q2] = pb_; ws.n[q2] = nr;
+                            ws.ra[q2] = rm; ws.ma[q2] = mm; ws.rb[q2] = prb; ws.mb[q2] = pmb;
+                        }
+                        if (ldense) {
+                            const int q2 = nd + __popc(mld & lt);
+                            ws.da[q2] = pa_;
+                            ws.dn[q2] = nl;
+                        }
+                        if (rdense) {
+                            const int q2 = nd + __popc(mld) + __popc(mrd & lt);
+                            ws.da[q2] = mid;
+                            ws.dn[q2] = nr;
+                        }
+                        sp += __popc(mls) + __popc(mrs);
+                        nd += __popc(mld) + __popc(mrd);
+                        __syncwarp();
+                    }
+                    if (nd) dense_pass(ws, nd, smp, L, Q, rb + q, acc, count);
+                }
+            }
+            if constexpr (!TRAIN) {
+                float sum = acc.s - acc.c;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+                if (lane == q) {
+                    float w = P.density_multiplier * L.ds32;
+                    result = fmaf(w, sum, P.flat_field);  // optical depth; exp in k_prop_finish
+                }
+            }
+        }
+        if constexpr (!TRAIN) {
+            if (rvalid) out[r] = result;
+        }
+    }
+    if (stats) {
+        __syncthreads();
+        if (threadIdx.x < kStatCount && sh.stats[threadIdx.x])
+            atomicAdd(&Q.stats[threadIdx.x], (unsigned long long)sh.stats[threadIdx.x]);
+    }
+}
+
+#if defined(XRP_PROP_RENDER_KERNELS)
+// FP64 re-evaluation of the samples the march left undecided: adds
+// w * density (reference arithmetic at the reference's position) to the
+// ray's optical depth.  Rays are numbered within the launch (view0 first).
+__global__ void __launch_bounds__(256)
+    k_prop_fallback(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
+                    const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views,
+                    int view0, const uint2* __restrict__ fb, const unsigned* __restrict__ fb_count,
+                    unsigned fb_cap, float* __restrict__ T, unsigned long long* __restrict__ stats,
+                    unsigned* __restrict__ overflow) {
+    const unsigned total = *fb_count;
+    const unsigned n = min(total, fb_cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && total > fb_cap) atomicOr(overflow, 1u);
+    const long img = (long)P.res * P.res;
+    const float w = P.density_multiplier * L.ds32;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint2 e = fb[q];
+        const long r = e.x;
+        const int v = view0 + (int)(r / img);
+        const long pix = r % img;
+        const int i = (int)(pix / P.res), j = (int)(pix % P.res);
+        double rho = sample64_pixel_inl(S, views[v], P.xs, i, j, L.s64[e.y]);
+        atomicAdd(&T[r], w * (float)rho);
+    }
+    if (stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[kStatFallbacks], (unsigned long long)n);
+}
+
+// Transmittance exp(-T) of every ray of a launch.
+__global__ void k_prop_finish(float* __restrict__ T, long n) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        T[q] = expf(-T[q]);
+}
+#endif  // XRP_PROP_RENDER_KERNELS
+
+#if defined(XRP_MLP_KERNELS)
+// Logits of `rows` feature rows (validation and tests), 32 rows per warp.
+__global__ void __launch_bounds__(32 * kPropWarps)
+    k_mlp_logits(const float* __restrict__ params, const __nv_bfloat16* __restrict__ X, int rows,
+                 float* __restrict__ logits) {
+    extern __shared__ __align__(16) unsigned char prop_smem[];
+    PropShared& sh = *reinterpret_cast<PropShared*>(prop_smem);
+    load_mlp_shared(params, sh.W);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __nv_bfloat16* xrow = sh.rows[warp];
+    const int tiles = (rows + 31) / 32;
+    for (int tile = blockIdx.x * kPropWarps + warp; tile < tiles; tile += gridDim.x * kPropWarps) {
+        const int r0 = tile * 32;
+        for (int q = lane; q < 32 * kMlpIn / 2; q += 32) {
+            int rr = q / (kMlpIn / 2), cc = q % (kMlpIn / 2);
+            uint32_t v = 0;
+            if (r0 + rr < rows) v = reinterpret_cast<const uint32_t*>(X + (size_t)(r0 + rr) * kMlpIn)[cc];
+            reinterpret_cast<uint32_t*>(xrow + rr * kMlpLd)[cc] = v;
+        }
+        __syncwarp();
+        float l = mlp_forward_warp(sh.W, xrow);
+        __syncwarp();
+        if (r0 + lane < rows) logits[r0 + lane] = l;
+    }
+}
+
+#endif  // XRP_MLP_KERNELS
+
+#endif  // __CUDACC__
+
+}  // namespace xrp

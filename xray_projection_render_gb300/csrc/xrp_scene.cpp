@@ -920,6 +920,36 @@ double def_error(const HDef& d, double E, double P) {
     return E;
 }
 
+// Lipschitz bound (Euclidean) of one deformation step, for the distance
+// certificates: |def(p) - def(q)| <= lip * |p - q|.
+double def_lip(const HDef& d) {
+    const double* a = d.d;
+    switch (d.type) {
+    case D_GAUSSIAN: {
+        // row i of the Jacobian minus I has norm |a_i| 2 s_i r exp(-s_i r^2)
+        // <= |a_i| / sigma_i * exp(-1/2)
+        double f2 = 0;
+        for (int i = 0; i < 3; i++) {
+            double n = std::fabs(a[i]) / std::fabs(a[3 + i]) * std::exp(-0.5);
+            f2 += n * n;
+        }
+        return 1.0 + std::sqrt(f2);
+    }
+    case D_LINEAR: {
+        double f2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + 2 * (a[3] * a[3] + a[4] * a[4] + a[5] * a[5]);
+        return 1.0 + std::sqrt(f2);
+    }
+    case D_RIGID: return 1.0;
+    case D_SIGMOID: return 1.0 + std::fabs(a[0]) / (4 * std::fabs(a[2]));
+    case D_AFFINE: {
+        double f2 = 0;
+        for (int i = 0; i < 9; i++) f2 += a[i] * a[i];
+        return std::sqrt(f2);
+    }
+    }
+    return 1.0;
+}
+
 double def_mag(const HDef& d, double P) {
     const double* a = d.d;
     switch (d.type) {
@@ -1002,11 +1032,16 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
     // rounding of p_c, of the direction (times |t|), of the offset t (three
     // roundings, lattice_t) and of the final fma
     double E0 = kSafety * kU * (Pc + 4 * T + Pspan) + 1e-12;
-    double E = E0, P = Pspan;
+    double E = E0, P = Pspan, lip = 1.0;
     for (auto& d : hs.defs) {
         E = def_error(d, E, P);
         P = def_mag(d, P);
+        lip *= def_lip(d);
     }
+    fs.def_lip = lip * (1.0 + 1e-3);
+    // a certificate radius is computed in FP32 from deformed coordinates of
+    // magnitude P carrying the per-axis error E
+    fs.margin_slack = 4.0 * (std::sqrt(3.0) * E + 64 * kU * (P + 1.0));
     Flattener F{hs, fs, hierarchical, {}};
     Flattener::Info info;
     fs.root = F.node(hs.root, E, P, 0, info);
@@ -1272,6 +1307,8 @@ HostPrepared prepare_host(const HostScene& hs, int res, int integration, double 
         S.sup_lo[a] = hp.fs.sup32_lo[a];
         S.sup_hi[a] = hp.fs.sup32_hi[a];
     }
+    S.inv_lip = (float)(1.0 / hp.fs.def_lip) * (1.0f - 1e-6f);
+    S.m_slack = (float)hp.fs.margin_slack;
     memset(&hp.P, 0, sizeof(hp.P));
     hp.P.res = res;
     hp.P.flat_field = (float)flat_field;

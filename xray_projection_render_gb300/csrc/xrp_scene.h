@@ -80,6 +80,8 @@ struct FlatScene {
     bool volume_root = false;     // root is a voxel grid and there is no deformation
     double vol_band_w = 0.0;      // world-space guard band of the voxel bounds test
     int depth = 0;                // deepest tessellation nesting (0: none)
+    double def_lip = 1.0;         // Lipschitz bound of the deformation chain
+    double margin_slack = 0.0;    // error allowance of certificate radii (deformed units)
 };
 
 FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical);

@@ -155,6 +155,117 @@ def render(scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, flat_field=
     return out
 
 
+PROPOSAL_STATS = ("segments", "certified", "refined", "dense", "dense_samples", "evaluations",
+                  "fp64_samples", "mlp_rounds", "routed_dense", "subdivided")
+
+
+class Proposal:
+    """The learned proposal of a scene, trained on the GPU (xrp_proposal_train)
+    on the cameras given by ``angles`` and the render options."""
+
+    def __init__(self, scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, segment=64,
+                 train_rays=65536, val_rays=32768, steps=2000, batch=4096, lr=2e-3,
+                 pos_weight=8.0, tau_margin=0.0, seed=0):
+        L = _lib.load()
+        cams, n = cameras_from_angles(angles, R, fov)
+        o = _opts(resolution, ds, R, 0.0, 1.0, "simple", False)
+        po = _lib.XrpProposalOpts(int(segment), int(train_rays), int(val_rays), int(steps),
+                                  int(batch), float(lr), float(pos_weight), float(tau_margin),
+                                  int(seed))
+        h = ctypes.c_void_p()
+        check(L.xrp_proposal_train(scene.handle, cams, n, ctypes.byref(o), ctypes.byref(po),
+                                   ctypes.byref(h)), "xrp_proposal_train")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        i = _lib.XrpProposalInfo()
+        check(_lib.load().xrp_proposal_get_info(self._h, ctypes.byref(i)), "xrp_proposal_get_info")
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def params(self) -> np.ndarray:
+        L = _lib.load()
+        n = L.xrp_mlp_param_count()
+        out = np.empty(n, dtype=np.float32)
+        check(L.xrp_proposal_params(self._h, out.ctypes.data, n), "xrp_proposal_params")
+        return out
+
+    def set_tau(self, tau: float):
+        check(_lib.load().xrp_proposal_set_tau(self._h, float(tau)), "xrp_proposal_set_tau")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().xrp_proposal_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resolution, ds, R=4.0,
+                    fov=40.0, flat_field=0.0, density_multiplier=1.0, segment=0, refine=True,
+                    out=None, stream=None, stats=False):
+    """Render with the proposal march (xrp_render_proposal).  ``proposal``
+    None: no network (every candidate refined, or integrated densely with
+    ``refine=False``).  Host path returns a float32 array [views, res, res]
+    (with ``stats``: (images, dict)); a contiguous float32 CUDA tensor as
+    ``out`` selects the device path."""
+    L = _lib.load()
+    cams, n = cameras_from_angles(angles, R, fov)
+    o = _opts(resolution, ds, R, flat_field, density_multiplier, "simple", stats)
+    if not refine:
+        o.flags |= _lib.XRP_FLAG_NO_REFINE
+    ph = proposal.handle if proposal is not None else None
+    if out is not None and _is_torch_cuda(out):
+        import torch
+        if out.dtype != torch.float32 or not out.is_contiguous() or out.numel() < n * resolution ** 2:
+            raise ValueError("out must be a contiguous float32 CUDA tensor of views*res*res")
+        st = stream if stream is not None else torch.cuda.current_stream(out.device)
+        check(L.xrp_render_proposal_device(scene.handle, ph, int(segment), cams, n, ctypes.byref(o),
+                                           ctypes.c_void_p(out.data_ptr()),
+                                           ctypes.c_void_p(st.cuda_stream)),
+              "xrp_render_proposal_device")
+        return out
+    if out is None:
+        out = np.empty((n, resolution, resolution), dtype=np.float32)
+    ptr = out.data_ptr() if hasattr(out, "data_ptr") else out.ctypes.data
+    check(L.xrp_render_proposal(scene.handle, ph, int(segment), cams, n, ctypes.byref(o),
+                                ctypes.c_void_p(ptr)), "xrp_render_proposal")
+    if stats:
+        c = (ctypes.c_uint64 * 10)()
+        L.xrp_proposal_last_stats(c)
+        return out, dict(zip(PROPOSAL_STATS, list(c)))
+    return out
+
+
+def mlp_grad(params, X_bf16_bits, y, pos_weight=1.0):
+    """The GPU training step's gradient (xrp_mlp_grad): returns
+    (grad [N] float32, loss, logits [rows])."""
+    L = _lib.load()
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X_bf16_bits, dtype=np.uint16)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    rows = X.shape[0]
+    grad = np.zeros_like(params)
+    loss = ctypes.c_float()
+    logits = np.zeros(rows, dtype=np.float32)
+    check(L.xrp_mlp_grad(params.ctypes.data, X.ctypes.data, y.ctypes.data, rows, float(pos_weight),
+                         grad.ctypes.data, ctypes.byref(loss), logits.ctypes.data), "xrp_mlp_grad")
+    return grad, float(loss.value), logits
+
+
 def xray_camera_params(angles, R=4.0, fov=40.0) -> np.ndarray:
     """The float32 XRayCameraParams rows the reference Go glue builds
     (cuda_path.go:61-77): eye, row-major camera-to-world, fov, R; shape [n,21]."""
