@@ -46,8 +46,13 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--workload", default="voxel", choices=["voxel", "cube", "lattice", "gyroid"],
-                   help="voxel (default, the headline) or one of the analytic scenes")
+    p.add_argument("--workload", default="voxel",
+                   choices=["voxel", "cube", "lattice", "gyroid", "batched"],
+                   help="voxel (default, the headline), one of the analytic scenes, or the batch "
+                        "of 64 uneven scenes (one persistent launch replayed from a CUDA graph)")
+    p.add_argument("--march", default="plain", choices=["plain", "certificate", "proposal"],
+                   help="analytic scenes: plain integrator, certificate march without the "
+                        "network, or the trained proposal")
     p.add_argument("--views", type=int, default=0, help="view count (0: the workload's)")
     p.add_argument("--res", type=int, default=0, help="resolution (0: the workload's)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -183,10 +188,16 @@ def run_reference(args):
     if rank != 0:
         return
     from xray_projection_render_gb300 import workloads as W
-    w = make_workload(args.workload, W, args.views, args.res)
+    if args.workload == "batched":
+        ws = W.batched_scenes(64)[:8]
+        w = W.Workload("batched_scenes_64", None, None, [], 0, 0.005)
+        measure = lambda sec: cpu_baseline_multi(ws, sec)  # noqa: E731
+    else:
+        w = make_workload(args.workload, W, args.views, args.res)
+        measure = lambda sec: cpu_baseline(w, sec)  # noqa: E731
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, max(2.0, args.cpu_seconds / max(1, args.steps)))
+        cb = measure(max(2.0, args.cpu_seconds / max(1, args.steps)))
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.median(vals))
@@ -240,10 +251,141 @@ def make_workload(name, W, views, res):
     return w
 
 
+def bench_batched(args):
+    """Config 4: 64 seeded scenes (1-200 primitives, resolution 256/512/1024,
+    8-128 views, ds 0.005) in one persistent launch per step, replayed from
+    the CUDA graph xrp_batch_create captured (autotuned tile shape and grid)."""
+    import torch
+    import __graft_entry__ as G
+    import xray_projection_render_gb300 as X
+    from xray_projection_render_gb300 import workloads as W
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    G.build()
+    ws = W.batched_scenes(64)[rank::world]  # ranks take disjoint scenes
+    ds = 0.005
+    scenes = [X.Scene(w.obj, w.deformation) for w in ws]
+    items = [(s, w.angles, w.res) for s, w in zip(scenes, ws)]
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)
+    b = X.Batch(items, ds=ds, autotune=True)
+    info = b.info()
+    for _ in range(args.warmup):
+        b.render(stream)
+    torch.cuda.synchronize()
+    # samples per step: each scene's counter pass on one view, scaled
+    samples = 0.0
+    for s, w in zip(scenes, ws):
+        _, n, _ = X.render(s, w.angles[:1], resolution=w.res, ds=ds, stats=True)
+        samples += n * len(w.angles)
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.render(stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    t_step = float(np.mean(times))
+    rays = info["rays"]
+    # the same work as one xrp_render_device call per scene (for comparison)
+    seq_out = torch.empty(max(len(w.angles) * w.res * w.res for w in ws), device=dev)
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s, w in zip(scenes, ws):
+            X.render(s, w.angles, resolution=w.res, ds=ds, out=seq_out, stream=stream)
+        torch.cuda.synchronize()
+        t_seq = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        t = torch.tensor([t_step, float(rays)], device=dev)
+        dist.all_reduce(t[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        t_step, rays = float(t[0].item()), int(t[1].item())
+    value = rays / t_step / 1e6
+    # end to end: a new batch through the public API (scene flattening and
+    # upload, batch creation without tuning, graph replay, every item's
+    # images copied to pinned host memory)
+    e2e_times, d2h = [], 0
+    if not args.no_e2e:
+        outs = [torch.empty((len(w.angles), w.res, w.res), dtype=torch.float32).pin_memory() for w in ws]
+        d2h = sum(o.numel() * 4 for o in outs)
+        objs = [(json.dumps(w.obj), json.dumps(w.deformation) if w.deformation else None) for w in ws]
+        h2d = sum(len(o) + (len(d) if d else 0) for o, d in objs) + sum(len(w.angles) * 192 for w in ws)
+        from xray_projection_render_gb300 import _lib as XL
+        for rep in range(1 + max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sc2 = [X.Scene(o, d) for o, d in objs]
+            with X.Batch([(s2, w.angles, w.res) for s2, w in zip(sc2, ws)], ds=ds, autotune=False) as b2:
+                b2.render()
+                for k, o in enumerate(outs):
+                    XL.check(XL.load().xrp_batch_copy_item(b2._h, k, ctypes_ptr(o)), "xrp_batch_copy_item")
+            for s2 in sc2:
+                s2.close()
+            if rep:
+                e2e_times.append(time.perf_counter() - t0)
+    t_e2e = float(np.mean(e2e_times)) if e2e_times else float("nan")
+    fp32_peak = fp32_peak_tflops(torch)
+    line = {
+        "metric": "Mrays/s on 1 GB300 (64 uneven scenes, one persistent launch per step)",
+        "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 4)",
+        "config": {"workload": "batched_scenes_64", "scenes": len(ws), "rays": rays, "ds": ds,
+                   "integrator": "simple", "R": 4.0, "fov": 40.0,
+                   "l2": "flushed before every timed step (256 MiB write); output > L2",
+                   "tile": f'{info["tile_w"]}x{info["tile_h"]}', "blocks_per_sm": info["blocks_per_sm"],
+                   "autotune_ms": info["tune_ms"], "graph": "one CUDA graph replay per step",
+                   "per_scene_calls_mrays": info["rays"] / t_seq / 1e6,
+                   "parallelism": f"scenes k mod {world}"},
+        "e2e": {"value": rays / t_e2e / 1e6 if e2e_times else None, "unit": "Mrays/s",
+                "h2d_bytes_per_step": h2d if e2e_times else 0, "d2h_bytes_per_step": d2h,
+                "path": "xrp_scene_create x64 + xrp_batch_create (no tuning) + xrp_batch_render + "
+                        "xrp_batch_copy_item into pinned host memory"},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": None, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": None, "traffic": None,
+                     "note": "per-sample work varies with each scene's candidate lists; "
+                             "samples per step reported instead",
+                     "samples_per_step": samples, "samples_per_s": samples / t_step},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_multi(ws[:8], args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    b.close()
+    for s in scenes:
+        s.close()
+
+
+def ctypes_ptr(t):
+    import ctypes
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def cpu_baseline_multi(ws, seconds):
+    """The oracle on seeded random rays spread over several scenes."""
+    parts = [cpu_baseline(w, seconds / len(ws)) for w in ws]
+    rays_s = len(ws) / sum(1.0 / p["value"] for p in parts)  # equal rays per scene
+    out = dict(parts[0])
+    out["value"] = rays_s
+    out["sample"] = f"{len(ws)} scenes of the batch, seeded random rays each ({seconds:.0f} s total)"
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return bench_batched(args)
     import torch
     import __graft_entry__ as G
     import xray_projection_render_gb300 as X
@@ -269,8 +411,16 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)  # 256 MiB > L2
     kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov, volume_path=args.volume_path)
 
+    prop = None
+    if args.march == "proposal":
+        prop = X.Proposal(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, segment=64)
+
     def step():
-        X.render(scene, my_angles, out=out, stream=stream, **kw)
+        if args.march == "plain":
+            X.render(scene, my_angles, out=out, stream=stream, **kw)
+        else:
+            X.render_proposal(scene, prop, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov,
+                              segment=64, refine=args.march == "proposal", out=out, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -321,7 +471,12 @@ def main():
 
         def e2e_call():
             with X.Scene(obj_json, def_json) as s2:
-                X.render(s2, my_angles, out=out_host, **kw)
+                if args.march == "plain":
+                    X.render(s2, my_angles, out=out_host, **kw)
+                else:  # the network trained on the resident scene applies to this copy
+                    X.render_proposal(s2, prop, my_angles, resolution=res, ds=w.ds, R=w.R,
+                                      fov=w.fov, segment=64, refine=args.march == "proposal",
+                                      out=out_host)
     if not args.no_e2e:
         e2e_call()  # warm
         for _ in range(max(1, min(args.steps, 3))):
@@ -348,6 +503,7 @@ def main():
         "data": "synthetic (seeded)",
         "config": {"workload": w.name, "views": len(w.angles), "res": res, "ds": w.ds,
                    "integrator": "simple", "R": w.R, "fov": w.fov,
+                   "march": None if is_voxel else args.march,
                    "l2": "flushed before every timed step (256 MiB write)",
                    "volume_path": args.volume_path if is_voxel else None,
                    "parallelism": f"views k mod {world}"},
@@ -368,6 +524,8 @@ def main():
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if prop is not None:
+        prop.close()
     scene.close()
     if world > 1:
         torch.distributed.destroy_process_group()

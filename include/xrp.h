@@ -183,6 +183,50 @@ XRP_API int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples);
 XRP_API void xrp_release_cache(void);
 
 /*
+ * Batched rendering (no counterpart in the reference, which renders one
+ * scene per process): many scenes, each with its own cameras and
+ * resolution, in one persistent launch that takes 256-pixel tiles from a
+ * global counter, so uneven items balance across the GPU.  xrp_batch_create
+ * flattens and uploads every scene once, picks the tile shape and grid with
+ * an autotuner (timed on a sample of the batch's tiles) and captures the
+ * launch in a CUDA graph; xrp_batch_render replays the graph.  Results are
+ * those of xrp_render for each item.  All items share the options (ds, R,
+ * integration, flat field, multiplier; opts->resolution is ignored).
+ */
+typedef struct {
+    xrp_scene* scene;
+    const xrp_camera* views;
+    int num_views;
+    int resolution;
+} xrp_batch_item;
+
+typedef struct xrp_batch xrp_batch;
+
+typedef struct {
+    long long rays, tiles;
+    int tile_w, tile_h;        /* chosen tile shape (tile_w * tile_h == 256) */
+    int blocks_per_sm, num_sms;
+    int tune_candidates;       /* autotuner: shapes x grids timed */
+    float tune_ms[8];          /* their times on the sampled tiles */
+    float build_ms;            /* flattening, upload, tuning, capture */
+} xrp_batch_info;
+
+/* autotune: 1 to time the candidates, 0 for 16x16 tiles at full occupancy. */
+XRP_API int xrp_batch_create(const xrp_batch_item* items, int num_items, const xrp_render_opts* opts,
+                             int autotune, xrp_batch** out);
+/* Replays the captured launch on `stream` (NULL: legacy stream) into the
+ * batch's device output; returns after queuing. */
+XRP_API int xrp_batch_render(xrp_batch* batch, void* stream);
+/* Device output: item k's images (num_views*res*res float32) start at
+ * xrp_batch_item_offset(batch, k) floats. */
+XRP_API const float* xrp_batch_output(const xrp_batch* batch);
+XRP_API long long xrp_batch_item_offset(const xrp_batch* batch, int k);
+/* Copies item k's images to host memory (synchronous). */
+XRP_API int xrp_batch_copy_item(const xrp_batch* batch, int k, float* out_host);
+XRP_API int xrp_batch_get_info(const xrp_batch* batch, xrp_batch_info* out);
+XRP_API void xrp_batch_destroy(xrp_batch* batch);
+
+/*
  * Proposal march (no counterpart in the reference, whose integrators are
  * main.go:144-199).  The plain integrator's samples are cut into segments.
  * A segment whose end densities agree and whose end-point distance

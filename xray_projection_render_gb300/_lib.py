@@ -51,6 +51,16 @@ class XrpProposalInfo(ctypes.Structure):
                 ("final_loss", c_float), ("train_ms", c_float)]
 
 
+class XrpBatchItem(ctypes.Structure):
+    _fields_ = [("scene", c_void_p), ("views", c_void_p), ("num_views", c_int), ("resolution", c_int)]
+
+
+class XrpBatchInfo(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_longlong), ("tiles", ctypes.c_longlong), ("tile_w", c_int),
+                ("tile_h", c_int), ("blocks_per_sm", c_int), ("num_sms", c_int),
+                ("tune_candidates", c_int), ("tune_ms", c_float * 8), ("build_ms", c_float)]
+
+
 XRP_INTEGRATE_SIMPLE = 0
 XRP_INTEGRATE_HIERARCHICAL = 1
 XRP_FLAG_STATS = 1
@@ -76,6 +86,13 @@ SIGNATURES = {
     "xrp_release_cache": (None, []),
     "xrp_render_volume_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int,
                                           c_float, c_float, c_void_p, c_void_p]),
+    "xrp_batch_create": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    "xrp_batch_render": (c_int, [c_void_p, c_void_p]),
+    "xrp_batch_output": (c_void_p, [c_void_p]),
+    "xrp_batch_item_offset": (ctypes.c_longlong, [c_void_p, c_int]),
+    "xrp_batch_copy_item": (c_int, [c_void_p, c_int, c_void_p]),
+    "xrp_batch_get_info": (c_int, [c_void_p, c_void_p]),
+    "xrp_batch_destroy": (None, [c_void_p]),
     "xrp_proposal_train": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "xrp_proposal_get_info": (c_int, [c_void_p, c_void_p]),
     "xrp_proposal_params": (c_int, [c_void_p, c_void_p, c_int]),

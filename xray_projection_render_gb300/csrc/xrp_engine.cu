@@ -520,7 +520,8 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     }
     const size_t img = (size_t)res * res;
     const int tpv = ((res + 15) / 16) * ((res + 15) / 16);
-    const int max_views_per_launch = std::max(1, (int)(0x7fffffffL / tpv));
+    int max_views_per_launch = std::max(1, (int)(0x7fffffffL / tpv));
+    if (pl) max_views_per_launch = std::max(1, std::min<int>(max_views_per_launch, (int)(pl->max_rays / (long long)img)));
     if (!out_host) {
         for (int v0 = 0; v0 < nviews; v0 += max_views_per_launch) {
             int n = std::min(max_views_per_launch, nviews - v0);
@@ -796,6 +797,300 @@ void xrp_release_cache(void) {
         cudaMemPoolTrimTo(kv.second->pool, 0);
     }
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batched rendering
+// ---------------------------------------------------------------------------
+
+struct xrp_batch {
+    int device = -1;
+    void* tables = nullptr;   // scenes, views, pixel tables, lattice, items (cudaMalloc)
+    float* out = nullptr;     // all items' images
+    unsigned long long* counter = nullptr;
+    std::vector<long long> offset;  // per item (caller's order)
+    std::vector<long long> size;
+    BatchLaunch bl;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    xrp_batch_info info;
+};
+
+static void batch_free(xrp_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->tables) cudaFree(b->tables);
+    if (b->out) cudaFree(b->out);
+    if (b->counter) cudaFree(b->counter);
+    delete b;
+}
+
+// Items' tiling for a tile shape, in work order; returns the tile count.
+static long long batch_tiling(std::vector<BatchItemDev>& items, int tw, int th) {
+    long long t0 = 0;
+    for (auto& it : items) {
+        const int res = it.P.res;
+        it.tiles_x = (res + tw - 1) / tw;
+        it.tiles_y = (res + th - 1) / th;
+        it.tile0 = t0;
+        t0 += (long long)it.nviews * it.tiles_x * it.tiles_y;
+    }
+    return t0;
+}
+
+extern "C" {
+
+int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* o, int autotune,
+                     xrp_batch** out) {
+    if (!items || !o || !out) return fail(1, "null pointer");
+    *out = nullptr;
+    if (n <= 0) return fail(2, "num_items must be > 0");
+    xrp_render_opts oo = *o;
+    for (int k = 0; k < n; k++) {
+        if (!items[k].scene || !items[k].views) return fail(1, "null pointer in item %d", k);
+        if (items[k].num_views <= 0 || items[k].resolution <= 0) return fail(2, "item %d: bad sizes", k);
+    }
+    oo.resolution = items[0].resolution;
+    std::string why;
+    if (!opts_ok(&oo, why)) return fail(2, "%s", why.c_str());
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    for (int k = 0; k < n; k++)
+        if (items[k].scene->device != E->device) return fail(2, "item %d: scene belongs to device %d", k, items[k].scene->device);
+    auto t_start = std::chrono::steady_clock::now();
+    std::unique_ptr<xrp_batch, void (*)(xrp_batch*)> B(new xrp_batch(), batch_free);
+    B->device = E->device;
+    memset(&B->info, 0, sizeof(B->info));
+    // work order: largest items first, so the tail of the launch is small
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (double)items[a].num_views * items[a].resolution * items[a].resolution >
+               (double)items[b].num_views * items[b].resolution * items[b].resolution;
+    });
+    // flatten every scene for its cameras; one sample lattice (shared ds, R)
+    std::vector<HostPrepared> hps(n);
+    std::vector<std::vector<ViewDev>> vws(n);
+    int depth = 0;
+    bool defs = false;
+    for (int q = 0; q < n; q++) {
+        const xrp_batch_item& it = items[order[q]];
+        double fov_max;
+        vws[q] = views_from(it.views, it.num_views, &fov_max);
+        try {
+            hps[q] = prepare_host(it.scene->hs, it.resolution, oo.integration, oo.ds, oo.R, oo.flat_field,
+                                  oo.density_multiplier, fov_max);
+        } catch (const std::exception& ex) {
+            return fail(2, "item %d: %s", order[q], ex.what());
+        }
+        for (size_t v = 0; v < hps[q].vols.size(); v++) {
+            hps[q].vols[v].data = it.scene->vdev[v];
+            hps[q].vols[v].data64 = it.scene->v64[v];
+        }
+        depth = std::max(depth, hps[q].fs.depth);
+        defs = defs || !hps[q].fs.defs.empty();
+    }
+    const HostLattice& hl = hps[0].hl;
+    // one upload: per item its scene tables, views and pixel table, then the
+    // lattice, the SceneDev array and the item array (patched with addresses)
+    Tables T;
+    struct Off { size_t nodes, n64, child, cells, items, defs, vols, xs; };
+    std::vector<Off> off(n);
+    std::vector<ViewDev> allv;  // every item's views, in work order
+    std::vector<int> view0(n);
+    for (int q = 0; q < n; q++) {
+        const FlatScene& fs = hps[q].fs;
+        off[q] = {T.add(fs.nodes), T.add(fs.nodes64), T.add(fs.child), T.add(fs.cells), T.add(fs.items),
+                  T.add(fs.defs), T.add(hps[q].vols), T.add(hps[q].xs)};
+        view0[q] = (int)allv.size();
+        allv.insert(allv.end(), vws[q].begin(), vws[q].end());
+    }
+    size_t o_views = T.add(allv);
+    size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
+    size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
+    std::vector<SceneDev> sdev(n);
+    std::vector<BatchItemDev> idev(n);
+    size_t o_scenes = T.add(sdev), o_items = T.add(idev);
+    cudaError_t e = cudaMalloc(&B->tables, T.host.size());
+    if (e != cudaSuccess) return cuda_fail(3, "batch tables", e);
+    unsigned char* base = (unsigned char*)B->tables;
+    long long out_total = 0;
+    std::vector<long long> out0(n);
+    for (int q = 0; q < n; q++) {
+        const xrp_batch_item& it = items[order[q]];
+        SceneDev S = hps[q].S;
+        S.nodes = (const Node*)(base + off[q].nodes);
+        S.nodes64 = (const Node64*)(base + off[q].n64);
+        S.child = (const int32_t*)(base + off[q].child);
+        S.cells = (const int32_t*)(base + off[q].cells);
+        S.items = (const int32_t*)(base + off[q].items);
+        S.defs = (const DefStep*)(base + off[q].defs);
+        S.vols = (const Volume*)(base + off[q].vols);
+        sdev[q] = S;
+        BatchItemDev& I = idev[q];
+        memset(&I, 0, sizeof(I));
+        I.scene = q;
+        I.view0 = view0[q];
+        I.nviews = it.num_views;
+        I.P = hps[q].P;
+        I.P.nviews = it.num_views;
+        I.P.xs = (const double*)(base + off[q].xs);
+        I.out0 = out_total;
+        out0[q] = out_total;
+        out_total += (long long)it.num_views * it.resolution * it.resolution;
+    }
+    const ViewDev* vbase = (const ViewDev*)(base + o_views);
+    memcpy(T.host.data() + o_scenes, sdev.data(), sdev.size() * sizeof(SceneDev));
+    Lattice L = hl.hdr;
+    L.s64 = (const double*)(base + o_s64);
+    L.t32 = (const float*)(base + o_t32);
+    L.fstart = (const int32_t*)(base + o_fs);
+    L.f64 = (const double*)(base + o_f64);
+    L.ft32 = (const float*)(base + o_ft32);
+    B->offset.resize(n);
+    B->size.resize(n);
+    for (int q = 0; q < n; q++) {
+        B->offset[order[q]] = out0[q];
+        B->size[order[q]] = (long long)items[order[q]].num_views * items[order[q]].resolution * items[order[q]].resolution;
+    }
+    if ((e = cudaMalloc(&B->out, (size_t)std::max<long long>(out_total, 1) * sizeof(float))) != cudaSuccess)
+        return cuda_fail(3, "batch output", e);
+    if ((e = cudaMalloc(&B->counter, sizeof(unsigned long long))) != cudaSuccess)
+        return cuda_fail(3, "batch counter", e);
+    if ((e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(3, "batch stream", e);
+    int sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
+    const bool hier = oo.integration == XRP_INTEGRATE_HIERARCHICAL;
+    const int kdepth = depth == 0 ? 0 : kMaxDepth;
+    if ((e = batch_blocks_per_sm(kdepth, defs, hier, &occ)) != cudaSuccess) return cuda_fail(7, "batch occupancy", e);
+    occ = std::max(occ, 1);
+    BatchLaunch bl;
+    memset(&bl, 0, sizeof(bl));
+    bl.scenes = (const SceneDev*)(base + o_scenes);
+    bl.items = (const BatchItemDev*)(base + o_items);
+    bl.nitems = n;
+    bl.views = vbase;
+    bl.L = L;
+    bl.depth = kdepth;
+    bl.defs = defs;
+    bl.hier = hier;
+    bl.counter = B->counter;
+    bl.out = B->out;
+    auto upload = [&](int tw, int th) -> cudaError_t {
+        bl.tw = tw;
+        bl.th = th;
+        bl.ntiles = batch_tiling(idev, tw, th);
+        memcpy(T.host.data() + o_items, idev.data(), idev.size() * sizeof(BatchItemDev));
+        cudaError_t ue = cudaMemcpyAsync(B->tables, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, B->cap);
+        if (ue == cudaSuccess) ue = cudaStreamSynchronize(B->cap);
+        return ue;
+    };
+    // autotuner: tile shapes x grid sizes, timed on the same sampled tiles
+    static const int shapes[3][2] = {{16, 16}, {32, 8}, {8, 32}};
+    int best_s = 0, best_b = occ;
+    const int grids[2] = {occ, std::max(1, occ / 2)};
+    int ncand = 0;
+    if (autotune && out_total > 0) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 3.0e38f;
+        for (int si = 0; si < 3; si++) {
+            if ((e = upload(shapes[si][0], shapes[si][1])) != cudaSuccess) return cuda_fail(4, "batch tables", e);
+            for (int gi = 0; gi < 2 && (gi == 0 || grids[1] != grids[0]); gi++) {
+                BatchLaunch t = bl;
+                t.blocks = grids[gi] * sms;
+                t.limit = std::min<long long>(t.ntiles, 16384);
+                t.stride = std::max<long long>(1, t.ntiles / t.limit);
+                float ms = 0;
+                for (int rep = 0; rep < 2; rep++) {
+                    cudaMemsetAsync(B->counter, 0, sizeof(unsigned long long), B->cap);
+                    cudaEventRecord(e0, B->cap);
+                    e = launch_batch(t, B->cap);
+                    cudaEventRecord(e1, B->cap);
+                    if (e != cudaSuccess) break;
+                    if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                }
+                if (e != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return cuda_fail(7, "batch autotune", e);
+                }
+                if (ncand < 8) B->info.tune_ms[ncand] = ms;
+                ncand++;
+                if (ms < best) {
+                    best = ms;
+                    best_s = si;
+                    best_b = grids[gi];
+                }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if ((e = upload(shapes[best_s][0], shapes[best_s][1])) != cudaSuccess) return cuda_fail(4, "batch tables", e);
+    bl.blocks = best_b * sms;
+    bl.stride = 1;
+    bl.limit = bl.ntiles;
+    B->bl = bl;
+    // capture: counter reset + persistent launch
+    if ((e = cudaStreamBeginCapture(B->cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cuda_fail(7, "graph capture", e);
+    cudaError_t e1 = cudaMemsetAsync(B->counter, 0, sizeof(unsigned long long), B->cap);
+    cudaError_t e2 = launch_batch(B->bl, B->cap);
+    e = cudaStreamEndCapture(B->cap, &B->graph);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e != cudaSuccess)
+        return cuda_fail(7, "graph capture", e != cudaSuccess ? e : (e1 != cudaSuccess ? e1 : e2));
+    if ((e = cudaGraphInstantiate(&B->exec, B->graph, 0)) != cudaSuccess) return cuda_fail(7, "graph instantiate", e);
+    B->info.rays = out_total;
+    B->info.tiles = bl.ntiles;
+    B->info.tile_w = shapes[best_s][0];
+    B->info.tile_h = shapes[best_s][1];
+    B->info.blocks_per_sm = best_b;
+    B->info.num_sms = sms;
+    B->info.tune_candidates = ncand;
+    B->info.build_ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    *out = B.release();
+    return 0;
+}
+
+int xrp_batch_render(xrp_batch* b, void* stream) {
+    if (!b) return fail(1, "null pointer");
+    cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(7, "graph launch", e);
+    return 0;
+}
+
+const float* xrp_batch_output(const xrp_batch* b) { return b ? b->out : nullptr; }
+
+long long xrp_batch_item_offset(const xrp_batch* b, int k) {
+    if (!b || k < 0 || k >= (int)b->offset.size()) return -1;
+    return b->offset[k];
+}
+
+int xrp_batch_copy_item(const xrp_batch* b, int k, float* out_host) {
+    if (!b || !out_host) return fail(1, "null pointer");
+    if (k < 0 || k >= (int)b->offset.size()) return fail(2, "item %d out of range", k);
+    cudaError_t e = cudaMemcpy(out_host, b->out + b->offset[k], (size_t)b->size[k] * sizeof(float),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(8, "batch copy", e);
+    return 0;
+}
+
+int xrp_batch_get_info(const xrp_batch* b, xrp_batch_info* out) {
+    if (!b || !out) return fail(1, "null pointer");
+    *out = b->info;
+    return 0;
+}
+
+void xrp_batch_destroy(xrp_batch* b) { batch_free(b); }
 
 }  // extern "C"
 
@@ -1162,8 +1457,9 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
             return cuda_fail(7, "stats reset", e);
         pl.Q.stats = (unsigned long long*)sb.p;
     }
-    // list of samples for FP64 re-evaluation (per launch; reused)
-    const unsigned fb_cap = 1u << 22;
+    // list of samples for FP64 re-evaluation (per launch of at most
+    // pl.max_rays rays; reused): half an entry per ray
+    const unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, pl.max_rays / 2);
     PoolBuf fb, fbc;
     if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
         (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)

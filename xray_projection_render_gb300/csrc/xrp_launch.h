@@ -47,11 +47,49 @@ struct Prepared {
 struct PropLaunch {
     PropParams Q;
     bool train = false;
+    long long max_rays = 1LL << 24;  // rays per launch (bounds the FP64 list)
 };
 
 // xrp_kern_scene.cu: k_render for general scenes.
 cudaError_t launch_scene(const Prepared& pr, int view0, int nviews, bool hier, float* dout,
                          unsigned long long* stats, cudaStream_t st);
+
+// One item of a batched render (several scenes, resolutions and view
+// counts in one persistent launch): its scene, views, tiling and output.
+struct BatchItemDev {
+    int scene;            // index into the batch's SceneDev array
+    int view0;            // first view in the batch's view array
+    int nviews;
+    int tiles_x, tiles_y; // tiles per view
+    int pad;
+    long long tile0;      // first global tile index
+    long long out0;       // first output element
+    RenderParams P;       // resolution, pixel table, flat field, multiplier
+};
+
+// Launch of the batch kernel: tiles of tw x th pixels (tw * th == 256),
+// taken from a global counter by a persistent grid; the tiles visited are
+// k * stride for k < limit (stride 1: all; larger strides sample the batch
+// for the autotuner).
+struct BatchLaunch {
+    const SceneDev* scenes;
+    const BatchItemDev* items;
+    int nitems;
+    const ViewDev* views;
+    Lattice L;
+    long long ntiles;
+    int tw, th;
+    int blocks;            // persistent grid size
+    int depth;             // 0: no tessellation in the batch, else up to kMaxDepth
+    bool defs, hier;
+    unsigned long long* counter;
+    long long stride, limit;
+    float* out;
+};
+
+// xrp_kern_scene.cu: the batch kernel and its occupancy.
+cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st);
+cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int* out);
 
 // xrp_kern_prop.cu: the proposal march (rendering).
 cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,

@@ -155,6 +155,63 @@ def render(scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, flat_field=
     return out
 
 
+class Batch:
+    """Many scenes rendered in one persistent, autotuned launch captured in a
+    CUDA graph (xrp_batch_create).  ``items``: (scene, angles, resolution)
+    triples; every item shares ds, R, fov and the other options."""
+
+    def __init__(self, items, *, ds, R=4.0, fov=40.0, flat_field=0.0, density_multiplier=1.0,
+                 integration="simple", autotune=True):
+        L = _lib.load()
+        self._keep = []
+        arr = (_lib.XrpBatchItem * len(items))()
+        self.shapes = []
+        for k, (scene, angles, res) in enumerate(items):
+            cams, n = cameras_from_angles(angles, R, fov)
+            self._keep.append((scene, cams))
+            arr[k] = _lib.XrpBatchItem(scene.handle, ctypes.cast(cams, ctypes.c_void_p), n, int(res))
+            self.shapes.append((n, int(res), int(res)))
+        o = _opts(items[0][2], ds, R, flat_field, density_multiplier, integration, False)
+        h = ctypes.c_void_p()
+        check(L.xrp_batch_create(arr, len(items), ctypes.byref(o), 1 if autotune else 0,
+                                 ctypes.byref(h)), "xrp_batch_create")
+        self._h = h
+
+    def render(self, stream=None):
+        """Queue one replay of the captured launch (torch stream or None)."""
+        st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(_lib.load().xrp_batch_render(self._h, st), "xrp_batch_render")
+
+    def item(self, k) -> np.ndarray:
+        out = np.empty(self.shapes[k], dtype=np.float32)
+        check(_lib.load().xrp_batch_copy_item(self._h, k, out.ctypes.data), "xrp_batch_copy_item")
+        return out
+
+    def info(self) -> dict:
+        i = _lib.XrpBatchInfo()
+        check(_lib.load().xrp_batch_get_info(self._h, ctypes.byref(i)), "xrp_batch_get_info")
+        d = {k: getattr(i, k) for k, _ in i._fields_}
+        d["tune_ms"] = list(i.tune_ms)[: i.tune_candidates]
+        return d
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().xrp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 PROPOSAL_STATS = ("segments", "certified", "refined", "dense", "dense_samples", "evaluations",
                   "fp64_samples", "mlp_rounds", "routed_dense", "subdivided")
 
