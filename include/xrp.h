@@ -183,6 +183,30 @@ XRP_API int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples);
 XRP_API void xrp_release_cache(void);
 
 /*
+ * Volume export of any scene (the CPU path of --export_volume,
+ * main.go:549-635; the reference GPU voxelizer covers cylinders only):
+ * density with the multiplier at x = i/res*2-1, y = j/res*2-1,
+ * z = k/res*2-1, layout [k][i][j] (res^3 values).  out_f32: the densities
+ * (FP32, equal to the reference's FP64 values rounded); out_u8: the
+ * exported bytes byte(v / max * 255) (0 where v <= 0 or max is 0).  Either
+ * may be NULL; host buffers; synchronous.
+ */
+XRP_API int xrp_voxelize_scene(xrp_scene* scene, int res, double density_multiplier, float* out_f32,
+                               unsigned char* out_u8);
+
+/*
+ * Image finishing on the device (main.go:482-506, cuda_path.go:104-130), so
+ * only 2 bytes per pixel cross to the host: for `num_views` images
+ * (device, [view][i][j] float32) writes gray = uint16(val * 0xffff) at PNG
+ * pixel (x = i, y = res-1-j) into d_gray ([view][y][x]), the alpha plane
+ * (0xffff, or with transparency 0xffff where val < 1 and 0 elsewhere) into
+ * d_alpha (may be NULL), and each image's (min, max) into d_minmax
+ * (2 floats per view).  Device buffers; queued on `stream`.
+ */
+XRP_API int xrp_finish_images(const float* d_images, int num_views, int res, int transparency,
+                              uint16_t* d_gray, uint16_t* d_alpha, float* d_minmax, void* stream);
+
+/*
  * Batched rendering (no counterpart in the reference, which renders one
  * scene per process): many scenes, each with its own cameras and
  * resolution, in one persistent launch that takes 256-pixel tiles from a

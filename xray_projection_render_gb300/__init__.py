@@ -9,8 +9,8 @@ front end (``engine.py``) and the seeded synthetic workloads
 """
 from .engine import (Batch, Proposal, Scene, assemble_voxel_grid, camera_arrays, cameras_from_angles,
                      mlp_grad, release_cache, render, render_proposal, render_volume_projections,
-                     xray_camera_params)
+                     finish_images, voxelize_scene, xray_camera_params)
 
 __all__ = ["Scene", "render", "render_volume_projections", "assemble_voxel_grid",
            "cameras_from_angles", "camera_arrays", "xray_camera_params", "release_cache",
-           "Proposal", "render_proposal", "mlp_grad", "Batch"]
+           "Proposal", "render_proposal", "mlp_grad", "Batch", "voxelize_scene", "finish_images"]

@@ -798,6 +798,50 @@ void xrp_release_cache(void) {
     }
 }
 
+int xrp_voxelize_scene(xrp_scene* s, int res, double dm, float* out_f32, unsigned char* out_u8) {
+    if (!s || (!out_f32 && !out_u8)) return fail(1, "null pointer");
+    if (res <= 0 || res > 2048) return fail(2, "res must be in [1, 2048]");
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
+    std::lock_guard<std::mutex> g(E->mtx);
+    cudaStream_t st = E->compute;
+    // the error analysis of the default camera (R 4, fov 40) covers grid
+    // points (|p| <= 1, one FP32 rounding)
+    std::vector<ViewDev> views(1);
+    memset(views.data(), 0, sizeof(ViewDev));
+    PoolBuf tab, vol, vmax, u8;
+    Prepared pr;
+    int rc = prepare(E, s->hs, s->vdev, s->v64, views, 8, XRP_INTEGRATE_SIMPLE, 0.01, 4.0, 0.0, 1.0, 40.0, st,
+                     tab, pr, 0);
+    if (rc) return rc;
+    const size_t nvox = (size_t)res * res * res;
+    cudaError_t e;
+    if ((e = vol.alloc(E, nvox * sizeof(float), st)) != cudaSuccess || (e = vmax.alloc(E, 16, st)) != cudaSuccess ||
+        (out_u8 && (e = u8.alloc(E, nvox, st)) != cudaSuccess))
+        return cuda_fail(3, "volume allocation", e);
+    e = launch_voxelize_scene(pr.S, pr.depth == 0 ? 0 : kMaxDepth, pr.defs, res, dm, (float*)vol.p,
+                              (unsigned*)vmax.p, out_u8 ? (unsigned char*)u8.p : nullptr, st);
+    if (e != cudaSuccess) return cuda_fail(5, "voxelizer kernel", e);
+    if (out_f32 && (e = cudaMemcpyAsync(out_f32, vol.p, nvox * sizeof(float), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(6, "volume copy", e);
+    if (out_u8 && (e = cudaMemcpyAsync(out_u8, u8.p, nvox, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(6, "volume copy", e);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(5, "voxelizer kernel", e);
+    return 0;
+}
+
+int xrp_finish_images(const float* d_images, int nviews, int res, int transparency, uint16_t* d_gray,
+                      uint16_t* d_alpha, float* d_minmax, void* stream) {
+    if (!d_images || !d_gray || !d_minmax) return fail(1, "null pointer");
+    if (nviews <= 0 || res <= 0) return fail(2, "bad sizes");
+    cudaError_t e = launch_finish(d_images, nviews, res, transparency, (unsigned short*)d_gray,
+                                  (unsigned short*)d_alpha, d_minmax, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(7, "finishing kernel", e);
+    return 0;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -91,6 +91,12 @@ struct BatchLaunch {
 cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st);
 cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int* out);
 
+// xrp_kern_scene.cu: volume export of a scene and device-side image finishing.
+cudaError_t launch_voxelize_scene(const SceneDev& S, int depth, bool defs, int res, double dm, float* out,
+                                  unsigned* vmax_bits, unsigned char* u8, cudaStream_t st);
+cudaError_t launch_finish(const float* img, int nviews, int res, int transparency, unsigned short* gray,
+                          unsigned short* alpha, float* minmax, cudaStream_t st);
+
 // xrp_kern_prop.cu: the proposal march (rendering).
 cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,
                                float* dout, cudaStream_t st);

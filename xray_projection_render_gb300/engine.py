@@ -155,6 +155,36 @@ def render(scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, flat_field=
     return out
 
 
+def voxelize_scene(scene: Scene, res, density_multiplier=1.0):
+    """Volume export of a scene (xrp_voxelize_scene): (float32 densities
+    [res][res][res] in [k][i][j] order, uint8 export bytes)."""
+    L = _lib.load()
+    f = np.empty((res, res, res), dtype=np.float32)
+    u = np.empty((res, res, res), dtype=np.uint8)
+    check(L.xrp_voxelize_scene(scene.handle, int(res), float(density_multiplier), f.ctypes.data,
+                               u.ctypes.data), "xrp_voxelize_scene")
+    return f, u
+
+
+def finish_images(images, transparency=False, stream=None):
+    """Device-side image finishing (xrp_finish_images) of a float32 CUDA
+    tensor [views, res, res]: returns (gray uint16-as-int16 tensor
+    [views, res, res] in PNG order, alpha, minmax [views, 2])."""
+    import torch
+    if not _is_torch_cuda(images) or images.dtype != torch.float32 or not images.is_contiguous():
+        raise ValueError("images must be a contiguous float32 CUDA tensor [views, res, res]")
+    n, res = images.shape[0], images.shape[-1]
+    gray = torch.empty((n, res, res), dtype=torch.int16, device=images.device)
+    alpha = torch.empty((n, res, res), dtype=torch.int16, device=images.device)
+    mm = torch.empty((n, 2), dtype=torch.float32, device=images.device)
+    st = stream if stream is not None else torch.cuda.current_stream(images.device)
+    check(_lib.load().xrp_finish_images(ctypes.c_void_p(images.data_ptr()), n, res,
+                                        1 if transparency else 0, ctypes.c_void_p(gray.data_ptr()),
+                                        ctypes.c_void_p(alpha.data_ptr()), ctypes.c_void_p(mm.data_ptr()),
+                                        ctypes.c_void_p(st.cuda_stream)), "xrp_finish_images")
+    return gray, alpha, mm
+
+
 class Batch:
     """Many scenes rendered in one persistent, autotuned launch captured in a
     CUDA graph (xrp_batch_create).  ``items``: (scene, angles, resolution)
