@@ -209,8 +209,8 @@ XRP_API int xrp_finish_images(const float* d_images, int num_views, int res, int
 /*
  * Batched rendering (no counterpart in the reference, which renders one
  * scene per process): many scenes, each with its own cameras and
- * resolution, in one persistent launch that takes 256-pixel tiles from a
- * global counter, so uneven items balance across the GPU.  xrp_batch_create
+ * resolution, in one persistent launch whose warps take 32-pixel tiles from
+ * a global counter, so uneven items balance across the GPU.  xrp_batch_create
  * flattens and uploads every scene once, picks the tile shape and grid with
  * an autotuner (timed on a sample of the batch's tiles) and captures the
  * launch in a CUDA graph; xrp_batch_render replays the graph.  Results are
@@ -228,7 +228,7 @@ typedef struct xrp_batch xrp_batch;
 
 typedef struct {
     long long rays, tiles;
-    int tile_w, tile_h;        /* chosen tile shape (tile_w * tile_h == 256) */
+    int tile_w, tile_h;        /* chosen warp tile shape (tile_w * tile_h == 32) */
     int blocks_per_sm, num_sms;
     int tune_candidates;       /* autotuner: shapes x grids timed */
     float tune_ms[8];          /* their times on the sampled tiles */

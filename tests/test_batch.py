@@ -41,10 +41,10 @@ def test_batch_equals_single_renders(X, integration, autotune):
             b.render()
             b.render()  # replay of the same graph
             info = b.info()
-            assert info["tile_w"] * info["tile_h"] == 256
+            assert info["tile_w"] * info["tile_h"] == 32
             assert info["rays"] == sum(len(w.angles) * w.res ** 2 for w in ws)
             if autotune:
-                assert info["tune_candidates"] >= 3
+                assert info["tune_candidates"] >= 4
             for k, (s, w) in enumerate(zip(scenes, ws)):
                 single = X.render(s, w.angles, resolution=w.res, ds=ds, integration=integration)
                 assert np.array_equal(b.item(k), single), w.name

@@ -1036,7 +1036,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         return ue;
     };
     // autotuner: tile shapes x grid sizes, timed on the same sampled tiles
-    static const int shapes[3][2] = {{16, 16}, {32, 8}, {8, 32}};
+    static const int shapes[4][2] = {{8, 4}, {4, 8}, {16, 2}, {32, 1}};  // warp tiles
     int best_s = 0, best_b = occ;
     const int grids[2] = {occ, std::max(1, occ / 2)};
     int ncand = 0;
@@ -1045,12 +1045,12 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         float best = 3.0e38f;
-        for (int si = 0; si < 3; si++) {
+        for (int si = 0; si < 4; si++) {
             if ((e = upload(shapes[si][0], shapes[si][1])) != cudaSuccess) return cuda_fail(4, "batch tables", e);
             for (int gi = 0; gi < 2 && (gi == 0 || grids[1] != grids[0]); gi++) {
                 BatchLaunch t = bl;
                 t.blocks = grids[gi] * sms;
-                t.limit = std::min<long long>(t.ntiles, 16384);
+                t.limit = std::min<long long>(t.ntiles, 131072);
                 t.stride = std::max<long long>(1, t.ntiles / t.limit);
                 float ms = 0;
                 for (int rep = 0; rep < 2; rep++) {

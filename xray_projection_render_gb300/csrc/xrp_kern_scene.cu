@@ -41,25 +41,39 @@ __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
     }
 }
 
-// Batches of scenes (general path): a persistent grid takes 256-pixel tiles
-// from a global counter, so scenes, resolutions and view counts of uneven
-// size share one launch and balance across SMs.  Items are ordered by
-// decreasing work and their tiles numbered consecutively; a tile's item is
-// found by binary search on the items' first tile.
+// Batches of scenes (general path): every warp of a persistent grid takes
+// 32-pixel tiles (tw x th) from a global counter, so scenes, resolutions
+// and view counts of uneven size share one launch and balance across SMs
+// without block barriers (rays differ in length; a block-wide tile would
+// hold finished warps at a barrier).  Items are ordered by decreasing work
+// and their tiles numbered consecutively; a tile's item is found by binary
+// search on the items' first tile.  The tile's scene header, item
+// parameters and view are staged in the warp's shared memory.
+static_assert(sizeof(SceneDev) % 4 == 0 && sizeof(RenderParams) % 4 == 0 && sizeof(ViewDev) % 4 == 0,
+              "staged structures are copied as 32-bit words");
+
+struct BatchStage {
+    SceneDev S;
+    RenderParams P;
+    ViewDev V;
+};
+
 template <bool HIER, int DEPTH, bool DEFS>
 __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
     k_batch(const SceneDev* __restrict__ scenes, const BatchItemDev* __restrict__ items, int nitems,
             const ViewDev* __restrict__ views, const __grid_constant__ Lattice L, long long ntiles, int tw,
             int th, unsigned long long* __restrict__ counter, long long stride, long long limit,
             float* __restrict__ out) {
-    __shared__ long long s_tile;
-    __shared__ int s_item;
+    __shared__ __align__(16) BatchStage stage[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    BatchStage& sg = stage[warp];
     for (;;) {
-        if (threadIdx.x == 0) {
+        long long t = -1;
+        int item = 0;
+        if (lane == 0) {
             unsigned long long k = atomicAdd(counter, 1ull);
-            long long t = (long long)k < limit ? (long long)k * stride : ntiles;
+            t = (long long)k < limit ? (long long)k * stride : ntiles;
             if (t >= ntiles) t = -1;
-            int item = 0;
             if (t >= 0) {
                 int lo = 0, hi = nitems - 1;
                 while (lo < hi) {  // last item with tile0 <= t
@@ -69,28 +83,40 @@ __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
                 }
                 item = lo;
             }
-            s_tile = t;
-            s_item = item;
         }
-        __syncthreads();
-        const long long t = s_tile;
-        const int it = s_item;
-        __syncthreads();
+        t = __shfl_sync(0xffffffffu, t, 0);
+        item = __shfl_sync(0xffffffffu, item, 0);
         if (t < 0) break;
-        const BatchItemDev& B = items[it];
+        const BatchItemDev& B = items[item];
         const int res = B.P.res;
         const long long local = t - B.tile0;
         const int tpv = B.tiles_x * B.tiles_y;
         const int v = (int)(local / tpv);
+        {
+            const unsigned* src_s = reinterpret_cast<const unsigned*>(scenes + B.scene);
+            const unsigned* src_p = reinterpret_cast<const unsigned*>(&B.P);
+            const unsigned* src_v = reinterpret_cast<const unsigned*>(views + B.view0 + v);
+            unsigned* ds_ = reinterpret_cast<unsigned*>(&sg.S);
+            unsigned* dp_ = reinterpret_cast<unsigned*>(&sg.P);
+            unsigned* dv_ = reinterpret_cast<unsigned*>(&sg.V);
+            constexpr int ns = sizeof(SceneDev) / 4, np = sizeof(RenderParams) / 4, nv = sizeof(ViewDev) / 4;
+            for (int q = lane; q < ns + np + nv; q += 32) {
+                if (q < ns) ds_[q] = src_s[q];
+                else if (q < ns + np) dp_[q - ns] = src_p[q - ns];
+                else dv_[q - ns - np] = src_v[q - ns - np];
+            }
+        }
+        __syncwarp();
         const int tt = (int)(local - (long long)v * tpv);
         const int ty = tt / B.tiles_x, tx = tt - ty * B.tiles_x;
-        const int i = ty * th + threadIdx.x / tw;
-        const int j = tx * tw + threadIdx.x % tw;
+        const int i = ty * th + lane / tw;
+        const int j = tx * tw + lane % tw;
         if (i < res && j < res) {
             RayStats st{0, 0};
-            float val = render_pixel<HIER, false, DEPTH, DEFS>(scenes[B.scene], L, B.P, views[B.view0 + v], i, j, st);
+            float val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);
             out[B.out0 + ((long long)v * res + i) * res + j] = val;
         }
+        __syncwarp();  // before the next tile overwrites the staged data
     }
 }
 
@@ -189,44 +215,68 @@ cudaError_t launch_voxelize_scene(const SceneDev& S, int depth, bool defs, int r
 // gray = uint16(val * 0xffff) stored at PNG pixel (x = i, y = res-1-j),
 // alpha = 0xffff, or with transparency 0xffff where val < 1 and 0 elsewhere,
 // and each image's min and max.  32x32 tiles through shared memory so both
-// the read (along j) and the flipped write (along x = i) are coalesced.
+// the read (along j) and the flipped write (along x = i) are coalesced; a
+// block walks a strip of kFinishTiles tiles along j and adds its min/max
+// with one atomic pair (per-view atomics from every warp contend in L2).
+constexpr int kFinishTiles = 8;
 __global__ void __launch_bounds__(256)
     k_finish(const float* __restrict__ img, int res, int transparency, unsigned short* __restrict__ gray,
              unsigned short* __restrict__ alpha, unsigned* __restrict__ minmax_bits) {
     __shared__ float tile[32][33];
+    __shared__ unsigned red[2][8];
     const int v = blockIdx.z;
-    const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+    const int i0 = blockIdx.y * 32;
     const float* src = img + (size_t)v * res * res;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
     unsigned lo = 0xffffffffu, hi = 0u;                       // ordered bits
-    for (int r = ty; r < 32; r += 8) {
-        const int i = i0 + r, j = j0 + tx;
-        float val = 0.0f;
-        if (i < res && j < res) {
-            val = src[(size_t)i * res + j];
-            const unsigned b = __float_as_uint(val);
-            const unsigned ob = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-            lo = ob < lo ? ob : lo;
-            hi = ob > hi ? ob : hi;
+    for (int tj = 0; tj < kFinishTiles; tj++) {
+        const int j0 = (blockIdx.x * kFinishTiles + tj) * 32;
+        if (j0 >= res) break;
+        for (int r = ty; r < 32; r += 8) {
+            const int i = i0 + r, j = j0 + tx;
+            float val = 0.0f;
+            if (i < res && j < res) {
+                val = src[(size_t)i * res + j];
+                const unsigned b = __float_as_uint(val);
+                const unsigned ob = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+                lo = ob < lo ? ob : lo;
+                hi = ob > hi ? ob : hi;
+            }
+            tile[r][tx] = val;
         }
-        tile[r][tx] = val;
-    }
-    __syncthreads();
-    // output row y = res-1-j (j = j0 + c), column x = i (i = i0 + tx)
-    for (int c = ty; c < 32; c += 8) {
-        const int j = j0 + c, i = i0 + tx;
-        if (i < res && j < res) {
-            const float val = tile[tx][c];
-            double t = (double)val * 65535.0;
-            t = t <= 0.0 ? 0.0 : (t >= 65535.0 ? 65535.0 : t);
-            const size_t o = (size_t)v * res * res + (size_t)(res - 1 - j) * res + i;
-            gray[o] = (unsigned short)t;
-            if (alpha) alpha[o] = transparency ? (val < 1.0f ? 0xffff : 0) : 0xffff;
+        __syncthreads();
+        // output row y = res-1-j (j = j0 + c), column x = i (i = i0 + tx)
+        for (int c = ty; c < 32; c += 8) {
+            const int j = j0 + c, i = i0 + tx;
+            if (i < res && j < res) {
+                const float val = tile[tx][c];
+                // uint16(float64(val) * 0xffff): the product is exact in FP64;
+                // in FP32 it is p + e exactly (e by FMA), and truncation of
+                // p + e is trunc(p), less one when p is whole and e < 0
+                const float p = val * 65535.0f;
+                const float e = fmaf(val, 65535.0f, -p);
+                float t = truncf(p);
+                if (t == p && e < 0.0f) t -= 1.0f;
+                t = t <= 0.0f ? 0.0f : (t >= 65535.0f ? 65535.0f : t);
+                const size_t o = (size_t)v * res * res + (size_t)(res - 1 - j) * res + i;
+                gray[o] = (unsigned short)t;
+                if (alpha) alpha[o] = transparency ? (val < 1.0f ? 0xffff : 0) : 0xffff;
+            }
         }
+        __syncthreads();
     }
     lo = __reduce_min_sync(0xffffffffu, lo);
     hi = __reduce_max_sync(0xffffffffu, hi);
     if (tx == 0) {
+        red[0][ty] = lo;
+        red[1][ty] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < 8; q++) {
+            lo = red[0][q] < lo ? red[0][q] : lo;
+            hi = red[1][q] > hi ? red[1][q] : hi;
+        }
         atomicMin(&minmax_bits[2 * v], lo);
         atomicMax(&minmax_bits[2 * v + 1], hi);
     }
@@ -253,7 +303,7 @@ cudaError_t launch_finish(const float* img, int nviews, int res, int transparenc
     unsigned* mm = reinterpret_cast<unsigned*>(minmax);
     int ib = (nviews + 255) / 256;
     k_minmax_init<<<ib, 256, 0, st>>>(mm, nviews);
-    dim3 grid((res + 31) / 32, (res + 31) / 32, nviews);
+    dim3 grid((res + 32 * kFinishTiles - 1) / (32 * kFinishTiles), (res + 31) / 32, nviews);
     k_finish<<<grid, 256, 0, st>>>(img, res, transparency, gray, alpha, mm);
     k_minmax_final<<<(2 * nviews + 255) / 256, 256, 0, st>>>(mm, nviews);
     return cudaGetLastError();

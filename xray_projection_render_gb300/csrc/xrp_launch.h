@@ -67,7 +67,7 @@ struct BatchItemDev {
     RenderParams P;       // resolution, pixel table, flat field, multiplier
 };
 
-// Launch of the batch kernel: tiles of tw x th pixels (tw * th == 256),
+// Launch of the batch kernel: warp tiles of tw x th pixels (tw * th == 32),
 // taken from a global counter by a persistent grid; the tiles visited are
 // k * stride for k < limit (stride 1: all; larger strides sample the batch
 // for the autotuner).
