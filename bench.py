@@ -47,9 +47,12 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
     p.add_argument("--workload", default="voxel",
-                   choices=["voxel", "cube", "lattice", "gyroid", "batched"],
-                   help="voxel (default, the headline), one of the analytic scenes, or the batch "
-                        "of 64 uneven scenes (one persistent launch replayed from a CUDA graph)")
+                   choices=["voxel", "cube", "lattice", "gyroid", "batched", "finish", "voxelize"],
+                   help="voxel (default, the headline), one of the analytic scenes, the batch "
+                        "of 64 uneven scenes (one persistent launch replayed from a CUDA graph), "
+                        "device-side image finishing of 64 images of 1024^2, or the volume "
+                        "export of the deformed lattice at 256^3")
+    p.add_argument("--scenes", type=int, default=64, help="batched: number of scenes")
     p.add_argument("--march", default="plain", choices=["plain", "certificate", "proposal"],
                    help="analytic scenes: plain integrator, certificate march without the "
                         "network, or the trained proposal")
@@ -188,6 +191,11 @@ def run_reference(args):
     if rank != 0:
         return
     from xray_projection_render_gb300 import workloads as W
+    if args.workload in ("finish", "voxelize"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the reference runs this step in Go on the host (PNG / raw writing); "
+                          "no CPU arm is timed for it here"}), flush=True)
+        return
     if args.workload == "batched":
         ws = W.batched_scenes(64)[:8]
         w = W.Workload("batched_scenes_64", None, None, [], 0, 0.005)
@@ -262,7 +270,9 @@ def bench_batched(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     G.build()
-    ws = W.batched_scenes(64)[rank::world]  # ranks take disjoint scenes
+    ws = W.batched_scenes(args.scenes)[rank::world]  # ranks take disjoint scenes
+    if args.res or args.views:  # reduced copies (profiling)
+        ws = [W.reduced(w, args.res or w.res, args.views or None) for w in ws]
     ds = 0.005
     scenes = [X.Scene(w.obj, w.deformation) for w in ws]
     items = [(s, w.angles, w.res) for s, w in zip(scenes, ws)]
@@ -365,6 +375,65 @@ def bench_batched(args):
         s.close()
 
 
+def bench_small_kernel(args):
+    """Device-side image finishing (64 images of 1024^2, 4 B read and 2 + 2 B
+    written per pixel: HBM-bound) or the volume export of the deformed
+    lattice at 256^3 (SM-bound), timed with CUDA events, inputs resident."""
+    import torch
+    import __graft_entry__ as G
+    import xray_projection_render_gb300 as X
+    from xray_projection_render_gb300 import workloads as W
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    G.build()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)
+    peaks = measured_peaks()
+    if args.workload == "finish":
+        n, res = 64, 1024
+        img = torch.rand((n, res, res), device=dev)
+        step = lambda: X.finish_images(img, stream=stream)  # noqa: E731
+        units, unit = n * res * res, "Mpixels/s"
+        bytes_per_unit = 4 + 2 + 2
+        metric = "Mpixels/s of device-side image finishing (64 images of 1024^2)"
+        cfg = {"workload": "finish_64x1024^2", "images": n, "res": res}
+    else:
+        w = W.deformed_lattice()
+        res = 256
+        scene = X.Scene(w.obj, w.deformation)
+        step = lambda: X.voxelize_scene(scene, res)  # noqa: E731  (host copies included)
+        units, unit = res ** 3, "Mvoxels/s"
+        bytes_per_unit = None
+        metric = "Mvoxels/s of the volume export (deformed lattice, 256^3, host copy included)"
+        cfg = {"workload": "voxelize_lattice_256^3", "res": res}
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    t = float(np.mean(times))
+    line = {"metric": metric, "value": units / t / 1e6, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": cfg,
+            "gpu_launches": args.steps, "clocks": clk.summary()}
+    if bytes_per_unit:
+        ach = units * bytes_per_unit / t / 1e9
+        pk = peaks.get("hbm_gbs")
+        line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": pk, "unit": "GB/s",
+                            "frac": ach / pk if pk else None, "traffic": None,
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_ptr(t):
     import ctypes
     return ctypes.c_void_p(t.data_ptr())
@@ -386,6 +455,8 @@ def main():
         return run_reference(args)
     if args.workload == "batched":
         return bench_batched(args)
+    if args.workload in ("finish", "voxelize"):
+        return bench_small_kernel(args)
     import torch
     import __graft_entry__ as G
     import xray_projection_render_gb300 as X
