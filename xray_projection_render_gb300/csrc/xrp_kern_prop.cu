@@ -7,7 +7,9 @@ namespace xrp {
 
 static cudaError_t march(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                          cudaStream_t st) {
-    XRP_PROP_DISPATCH(false, dout)
+    if (Q.mlp) return launch_prop_net(pr, view0, nviews, Q, dout, st);
+    if (Q.refine) { XRP_PROP_DISPATCH(kPropRefine, dout) }
+    XRP_PROP_DISPATCH(kPropDense, dout)
 }
 
 // March (optical depths), FP64 for the samples it left undecided, exp(-T).

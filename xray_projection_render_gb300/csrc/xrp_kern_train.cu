@@ -8,7 +8,7 @@ namespace xrp {
 
 cudaError_t launch_prop_train(const Prepared& pr, int view0, int nviews, const PropParams& Q,
                               cudaStream_t st) {
-    XRP_PROP_DISPATCH(true, nullptr)
+    XRP_PROP_DISPATCH(kPropTrain, nullptr)
 }
 
 cudaError_t mlp_kernel_attrs() {

@@ -12,6 +12,12 @@
 
 namespace xrp {
 
+// Minimum resident blocks per SM asked of the compiler (register budget)
+// for the general-scene and batch kernels, tuned on GB300.
+#ifndef XRP_SCENE_MIN_BLOCKS
+#define XRP_SCENE_MIN_BLOCKS 2
+#endif
+
 // Parameters of a voxel-grid root (no deformation), read by the voxel
 // kernels from their constant bank so the march keeps few live registers.
 struct VoxParams {
@@ -87,11 +93,11 @@ struct BatchLaunch {
     float* out;
 };
 
-// xrp_kern_scene.cu: the batch kernel and its occupancy.
+// xrp_kern_batch.cu: the batch kernel and its occupancy.
 cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st);
 cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int* out);
 
-// xrp_kern_scene.cu: volume export of a scene and device-side image finishing.
+// xrp_kern_export.cu: volume export of a scene and device-side image finishing.
 cudaError_t launch_voxelize_scene(const SceneDev& S, int depth, bool defs, int res, double dm, float* out,
                                   unsigned* vmax_bits, unsigned char* u8, cudaStream_t st);
 cudaError_t launch_finish(const float* img, int nviews, int res, int transparency, unsigned short* gray,
@@ -100,6 +106,10 @@ cudaError_t launch_finish(const float* img, int nviews, int res, int transparenc
 // xrp_kern_prop.cu: the proposal march (rendering).
 cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,
                                float* dout, cudaStream_t st);
+
+// xrp_kern_prop_net.cu: the march with the network routing candidates.
+cudaError_t launch_prop_net(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                            cudaStream_t st);
 
 // xrp_kern_train.cu: training-row generation and the network's kernels.
 cudaError_t launch_prop_train(const Prepared& pr, int view0, int nviews, const PropParams& Q,
@@ -129,10 +139,10 @@ cudaError_t persistent_grid(K kern, size_t smem, int block, int* out) {
 
 // One proposal-march launch, persistent grid (xrp_kern_prop.cu and
 // xrp_kern_train.cu instantiate it).
-template <int DEPTH, bool DEFS, bool TRAIN>
+template <int DEPTH, bool DEFS, int MODE>
 cudaError_t launch_prop_t(const Prepared& pr, int view0, int nviews, const PropParams& Q,
                           float* dout, cudaStream_t st) {
-    auto kern = k_propose<DEPTH, DEFS, TRAIN>;
+    auto kern = k_propose<DEPTH, DEFS, MODE>;
     static int grid_cache[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per device (first 8)
     const size_t smem = sizeof(PropShared);
     int dev = 0;

@@ -145,15 +145,23 @@ __device__ __forceinline__ void dense_pass(const WarpLists& ws, int nd, const Sm
     __syncwarp();
 }
 
-template <int DEPTH, bool DEFS, bool TRAIN>
+// MODE: kPropDense (certificate, else dense), kPropRefine (certificate,
+// else refinement), kPropNet (the network routes between the two),
+// kPropTrain (training rows).  Each mode is its own kernel so none carries
+// the others' code (instruction-cache pressure is this kernel's first stall).
+enum : int { kPropDense = 0, kPropRefine = 1, kPropNet = 2, kPropTrain = 3 };
+
+template <int DEPTH, bool DEFS, int MODE>
 __global__ void __launch_bounds__(32 * kPropWarps, 2)
     k_propose(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
               const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0,
               int nviews, const __grid_constant__ PropParams Q, float* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char prop_smem[];
     PropShared& sh = *reinterpret_cast<PropShared*>(prop_smem);
-    const bool use_mlp = !TRAIN && Q.mlp != nullptr;
-    if (use_mlp) load_mlp_shared(Q.mlp, sh.W);
+    constexpr bool TRAIN = MODE == kPropTrain;
+    constexpr bool REFINE = MODE == kPropRefine || MODE == kPropNet;
+    constexpr bool use_mlp = MODE == kPropNet;
+    if constexpr (use_mlp) load_mlp_shared(Q.mlp, sh.W);
     if (threadIdx.x < kStatCount) sh.stats[threadIdx.x] = 0;
     __syncthreads();
     const unsigned FULL = 0xffffffffu;
@@ -282,14 +290,16 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
                 } else {
                     // the network routes candidates: likely transitions -> dense,
                     // the rest -> refinement by certificates
-                    bool to_dense = cand && !Q.refine;
-                    if (use_mlp && Q.refine && __any_sync(FULL, cand)) {
-                        write_features(Q, pa, pe, xrow + lane * kMlpLd);
-                        __syncwarp();
-                        float logit = mlp_forward_warp(sh.W, xrow);
-                        __syncwarp();
-                        to_dense = cand && logit > Q.tau;
-                        count(kStatMlpRounds, 1);
+                    bool to_dense = cand && !REFINE;
+                    if constexpr (use_mlp) {
+                        if (__any_sync(FULL, cand)) {
+                            write_features(Q, pa, pe, xrow + lane * kMlpLd);
+                            __syncwarp();
+                            float logit = mlp_forward_warp(sh.W, xrow);
+                            __syncwarp();
+                            to_dense = cand && logit > Q.tau;
+                            count(kStatMlpRounds, 1);
+                        }
                     }
                     if (cert) acc.add(rho_a * (float)(e - a));
                     count(kStatCertified, __popc(__ballot_sync(FULL, cert)));
@@ -315,11 +325,11 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
                         ws.da[q2] = a;
                         ws.dn[q2] = e - a;
                     }
-                    int sp = __popc(smask), nd = __popc(dmask);
+                    int sp = REFINE ? __popc(smask) : 0, nd = __popc(dmask);
                     __syncwarp();
                     // refinement waves: split each piece at its middle sample,
                     // certify the halves, push the rest (dense below min_piece)
-                    while (sp > 0) {
+                    while (REFINE && sp > 0) {
                         if (nd > kDenseCap - 64) {
                             dense_pass(ws, nd, smp, L, Q, rb + q, acc, count);
                             nd = 0;
