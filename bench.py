@@ -11,10 +11,13 @@ value     : device throughput, volume resident in HBM, output to a device
 e2e       : the same metric through the reference ABI call
             RenderVolumeProjectionsCUDA with pinned host buffers (volume
             upload and image download inside the timed region).
-roofline  : the render kernel against the FP32 FMA peak measured in this run
-            by a CUDA-core SGEMM (TF32 off); the algorithmic work is the
-            exact count of lattice samples the kernel evaluates (a counter
-            pass) times 58 FLOPs per trilinear sample.
+roofline  : the voxel kernel is bound by its texture gathers (two tld4 of
+            16 B per sample, the exact sample count from a counter pass):
+            achieved gathered bytes/s against the gather throughput measured
+            in this run (xrp_probe_gather_rate, L1-resident texture).  The
+            FP32 view (58 FLOPs per sample against a CUDA-core SGEMM with
+            TF32 off, measured in this run) is kept under "fp32"; the
+            analytic workloads report the FP32 view.
 cpu_baseline / --impl reference: the FP64 CPU restatement of the reference
             path (oracle/), on all host cores, on a seeded ray subset.
 
@@ -566,6 +569,25 @@ def main():
     fp32_peak = fp32_peak_tflops(torch)
     fps = FLOPS[args.workload]
     achieved = samples_step * fps / t_step / 1e12
+    fp32_roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                 "frac": achieved / fp32_peak if fp32_peak else None,
+                 "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
+                 "flops_per_sample": fps}
+    roof = dict(fp32_roof)
+    if is_voxel and args.volume_path == "gather":
+        # the voxel kernel's binding unit is the texture path: two tld4
+        # gathers (16 B each) per evaluated sample, against the gather rate
+        # measured in this run by xrp_probe_gather_rate
+        import ctypes
+        from xray_projection_render_gb300 import _lib as XL
+        gr = ctypes.c_double(0.0)
+        XL.check(XL.load().xrp_probe_gather_rate(ctypes.byref(gr)), "xrp_probe_gather_rate")
+        g_ach = 2.0 * samples_step / t_step
+        roof = {"bound": "tex", "achieved": g_ach * 16 / 1e9, "peak": gr.value * 16 / 1e9, "unit": "GB/s",
+                "frac": g_ach / gr.value if gr.value else None,
+                "peak_source": "measured in this run: tld4 gathers on an L1-resident layered texture",
+                "note": "gathered bytes (2 x 16 B per sample) vs the measured gather throughput",
+                "fp32": fp32_roof}
     line = {
         "metric": METRIC if args.workload == "voxel" else f"Mrays/s on 1 GB300 ({w.name})",
         "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -581,14 +603,12 @@ def main():
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
         "gpu_launches": args.steps,  # one render launch per step (all views)
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak if fp32_peak else None,
+        "roofline": dict(roof, **{
                      "traffic": TRAFFIC.get(args.workload, {}).get("bytes_per_view", 0) * n_my or None,
                      "traffic_source": TRAFFIC.get(args.workload, {}).get("source"),
-                     "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
-                     "samples_per_step": samples_step, "flops_per_sample": fps,
+                     "samples_per_step": samples_step,
                      "fp64_fallback_fraction": fp64 / max(samples, 1),
-                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
+                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")}),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -182,6 +182,12 @@ XRP_API int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples);
 /* Frees the device buffers the library caches between calls. */
 XRP_API void xrp_release_cache(void);
 
+/* Measured throughput of the texture gathers the voxel kernel issues
+ * (tld4 on a layered texture resident in L1), gathers per second on the
+ * current device: the peak the voxel kernel's binding unit can reach.  A
+ * measurement hook for benchmarks; no counterpart in the reference. */
+XRP_API int xrp_probe_gather_rate(double* gathers_per_s);
+
 /*
  * Volume export of any scene (the CPU path of --export_volume,
  * main.go:549-635; the reference GPU voxelizer covers cylinders only):

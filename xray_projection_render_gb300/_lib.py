@@ -86,6 +86,7 @@ SIGNATURES = {
     "xrp_release_cache": (None, []),
     "xrp_render_volume_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int,
                                           c_float, c_float, c_void_p, c_void_p]),
+    "xrp_probe_gather_rate": (c_int, [c_void_p]),
     "xrp_voxelize_scene": (c_int, [c_void_p, c_int, c_double, c_void_p, c_void_p]),
     "xrp_finish_images": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),

@@ -68,6 +68,29 @@ __device__ __forceinline__ float4 gather_a2d(cudaTextureObject_t tex, int layer,
 
 // FP64 density of sample s of pixel (i, j) (VoxelGrid.Density at the
 // reference's own position, objects.go:789-855, main.go:148-150).
+// Throughput probe of the texture path: every thread issues `iters` tld4
+// gathers on a small layered texture (resident in L1), so the rate measures
+// the TEX unit, the binding unit of the voxel kernel.  Coordinates cycle
+// over texel-quad centres in bounds.
+__global__ void __launch_bounds__(256) k_gather_probe(cudaTextureObject_t tex, int iters, float* sink) {
+    // four independent chains per thread; each coordinate depends on the
+    // previous gather of its chain (times 0, which is not folded without
+    // fast math), so no gather can be hoisted or merged
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    const float u0 = 1.0f + (float)(threadIdx.x & 7), v0 = 1.0f + (float)((threadIdx.x >> 3) & 7);
+    for (int k = 0; k < iters; k += 4) {
+        const float4 g0 = gather_a2d(tex, 0, u0 + a0 * 0.0f, v0);
+        const float4 g1 = gather_a2d(tex, 1, u0 + 1.0f + a1 * 0.0f, v0);
+        const float4 g2 = gather_a2d(tex, 0, u0 + 2.0f + a2 * 0.0f, v0 + 1.0f);
+        const float4 g3 = gather_a2d(tex, 1, u0 + 3.0f + a3 * 0.0f, v0 + 1.0f);
+        a0 += g0.x + g0.w;
+        a1 += g1.x + g1.w;
+        a2 += g2.x + g2.w;
+        a3 += g3.x + g3.w;
+    }
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3;
+}
+
 __device__ __forceinline__ double vox_sample64_inl(const VoxParams& Q, const ViewDev& V,
                                                    const double* xs, int i, int j, double s) {
     Ray64 r;
@@ -839,6 +862,45 @@ int xrp_finish_images(const float* d_images, int nviews, int res, int transparen
     cudaError_t e = launch_finish(d_images, nviews, res, transparency, (unsigned short*)d_gray,
                                   (unsigned short*)d_alpha, d_minmax, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(7, "finishing kernel", e);
+    return 0;
+}
+
+int xrp_probe_gather_rate(double* gathers_per_s) {
+    if (!gathers_per_s) return fail(1, "null pointer");
+    int code = 0;
+    Engine* E = engine_for_current(&code);
+    if (!E) return code;
+    std::lock_guard<std::mutex> g(E->mtx);
+    cudaStream_t st = E->compute;
+    std::vector<float> host(32 * 32 * 2);
+    for (size_t k = 0; k < host.size(); k++) host[k] = (float)(k % 7);
+    PoolBuf dv, sink;
+    cudaError_t e;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
+    const int blocks = sms * 8, iters = 8192;
+    if ((e = dv.alloc(E, host.size() * sizeof(float), st)) != cudaSuccess ||
+        (e = sink.alloc(E, (size_t)blocks * 256 * sizeof(float), st)) != cudaSuccess)
+        return cuda_fail(3, "probe buffers", e);
+    if ((e = cudaMemcpyAsync(dv.p, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(4, "probe upload", e);
+    LayeredTex t;
+    if ((e = t.create((const float*)dv.p, 32, 32, 2, st)) != cudaSuccess || !t.tex) return cuda_fail(3, "probe texture", e);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float ms = 0.0f;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(e0, st);
+        k_gather_probe<<<blocks, 256, 0, st>>>(t.tex, iters, (float*)sink.p);
+        cudaEventRecord(e1, st);
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        cudaEventElapsedTime(&ms, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return cuda_fail(7, "probe kernel", e);
+    *gathers_per_s = (double)blocks * 256 * iters / (ms * 1e-3);
     return 0;
 }
 
