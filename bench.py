@@ -270,10 +270,14 @@ def bench_batched(args):
     import __graft_entry__ as G
     import xray_projection_render_gb300 as X
     from xray_projection_render_gb300 import workloads as W
+    from xray_projection_render_gb300.sharding import job_time, shard
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     G.build()
-    ws = W.batched_scenes(args.scenes)[rank::world]  # ranks take disjoint scenes
+    ws = shard(W.batched_scenes(args.scenes), rank, world)  # scene k on rank k mod N
     if args.res or args.views:  # reduced copies (profiling)
         ws = [W.reduced(w, args.res or w.res, args.views or None) for w in ws]
     ds = 0.005
@@ -292,6 +296,9 @@ def bench_batched(args):
     for s, w in zip(scenes, ws):
         _, n, _ = X.render(s, w.angles[:1], resolution=w.res, ds=ds, stats=True)
         samples += n * len(w.angles)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     times = []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -313,13 +320,8 @@ def bench_batched(args):
             X.render(s, w.angles, resolution=w.res, ds=ds, out=seq_out, stream=stream)
         torch.cuda.synchronize()
         t_seq = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-        t = torch.tensor([t_step, float(rays)], device=dev)
-        dist.all_reduce(t[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        t_step, rays = float(t[0].item()), int(t[1].item())
+    t_step, rays = job_time(t_step, rays, dev)
+    rays = int(rays)
     value = rays / t_step / 1e6
     # end to end: a new batch through the public API (scene flattening and
     # upload, batch creation without tuning, graph replay, every item's
@@ -376,6 +378,8 @@ def bench_batched(args):
     b.close()
     for s in scenes:
         s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def bench_small_kernel(args):
@@ -471,9 +475,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     G.build()
+    from xray_projection_render_gb300.sharding import job_time, shard
     w = make_workload(args.workload, W, args.views, args.res)
     is_voxel = w.volume is not None
-    my_angles = w.angles[rank::world]
+    my_angles = shard(w.angles, rank, world)  # view k on rank k mod N, no exchange
     n_my = len(my_angles)
     res = w.res
     img = res * res
@@ -516,12 +521,7 @@ def main():
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1) * 1e-3)
-    t_step = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([t_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
-    rays_total = len(w.angles) * img
+    t_step, rays_total = job_time(float(np.mean(times)), n_my * img, dev)
     value = rays_total / t_step / 1e6
 
     # end to end through the host-facing C ABI, pinned host buffers, inputs
@@ -558,11 +558,7 @@ def main():
             t0 = time.perf_counter()
             e2e_call()
             e2e_times.append(time.perf_counter() - t0)
-    t_e2e = float(np.mean(e2e_times)) if e2e_times else float("nan")
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e, _ = job_time(float(np.mean(e2e_times)) if e2e_times else float("nan"), 0, dev)
     e2e_value = rays_total / t_e2e / 1e6
 
     peaks = measured_peaks()
