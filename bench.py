@@ -56,9 +56,9 @@ def parse():
                         "device-side image finishing of 64 images of 1024^2, or the volume "
                         "export of the deformed lattice at 256^3")
     p.add_argument("--scenes", type=int, default=64, help="batched: number of scenes")
-    p.add_argument("--march", default="plain", choices=["plain", "certificate", "proposal"],
-                   help="analytic scenes: plain integrator, certificate march without the "
-                        "network, or the trained proposal")
+    p.add_argument("--march", default="plain", choices=["plain", "trace", "certificate", "proposal"],
+                   help="analytic scenes: plain integrator, per-ray certificate tracing, "
+                        "segment march with certificates and no network, or the trained proposal")
     p.add_argument("--views", type=int, default=0, help="view count (0: the workload's)")
     p.add_argument("--res", type=int, default=0, help="resolution (0: the workload's)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -499,7 +499,8 @@ def main():
             X.render(scene, my_angles, out=out, stream=stream, **kw)
         else:
             X.render_proposal(scene, prop, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov,
-                              segment=64, refine=args.march == "proposal", out=out, stream=stream)
+                              segment=64, refine=args.march == "proposal",
+                              trace=args.march == "trace", out=out, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -508,6 +509,14 @@ def main():
     nstat = max(1, min(8, n_my))
     _, samples, fp64 = X.render(scene, my_angles[:nstat], stats=True, **kw)
     samples_step = samples * n_my / nstat
+    evals_step = None
+    if args.march != "plain" and not is_voxel:
+        # evaluations the march actually makes (density + certificate radius
+        # per evaluation, or one density per dense sample)
+        _, pst = X.render_proposal(scene, prop, my_angles[:nstat], resolution=res, ds=w.ds, R=w.R,
+                                   fov=w.fov, segment=64, refine=args.march == "proposal",
+                                   trace=args.march == "trace", stats=True)
+        evals_step = (pst["evaluations"] + pst["dense_samples"]) * n_my / nstat
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -550,7 +559,7 @@ def main():
                 else:  # the network trained on the resident scene applies to this copy
                     X.render_proposal(s2, prop, my_angles, resolution=res, ds=w.ds, R=w.R,
                                       fov=w.fov, segment=64, refine=args.march == "proposal",
-                                      out=out_host)
+                                      trace=args.march == "trace", out=out_host)
     if not args.no_e2e:
         e2e_call()  # warm
         for _ in range(max(1, min(args.steps, 3))):
@@ -564,11 +573,19 @@ def main():
     peaks = measured_peaks()
     fp32_peak = fp32_peak_tflops(torch)
     fps = FLOPS[args.workload]
-    achieved = samples_step * fps / t_step / 1e12
+    if evals_step is None:
+        achieved = samples_step * fps / t_step / 1e12
+        work = "lattice samples evaluated x FLOPs per sample"
+    else:
+        # a certificate evaluation adds the radius (about 12 FLOPs beyond
+        # the density, sharing its deformation and geometry)
+        achieved = evals_step * (fps + 12) / t_step / 1e12
+        work = ("evaluations the march makes (counter pass) x (FLOPs per sample + 12 for the "
+                "certificate radius); the plain integrator would evaluate samples_per_step")
     fp32_roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                  "frac": achieved / fp32_peak if fp32_peak else None,
                  "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
-                 "flops_per_sample": fps}
+                 "flops_per_sample": fps, "work": work, "evaluations_per_step": evals_step}
     roof = dict(fp32_roof)
     if is_voxel and args.volume_path == "gather":
         # the voxel kernel's binding unit is the texture path: two tld4

@@ -114,7 +114,8 @@ enum { XRP_INTEGRATE_SIMPLE = 0, XRP_INTEGRATE_HIERARCHICAL = 1 };
 enum {
     XRP_FLAG_STATS = 1,        /* count evaluated and FP64-re-evaluated samples */
     XRP_FLAG_VOLUME_LOADS = 2, /* voxel-grid roots: per-tap loads instead of texture gathers */
-    XRP_FLAG_NO_REFINE = 4     /* proposal march: no certificate refinement of segments */
+    XRP_FLAG_NO_REFINE = 4,    /* proposal march: no certificate refinement of segments */
+    XRP_FLAG_TRACE = 8         /* proposal march: per-ray certificate tracing (no network) */
 };
 
 /* Per-call options: the globals and flags of the reference CLI
@@ -308,7 +309,10 @@ XRP_API void xrp_proposal_destroy(xrp_proposal* p);
 
 /* Renders like xrp_render with the proposal march.  `proposal` NULL: every
  * candidate is refined (or, with XRP_FLAG_NO_REFINE, integrated densely);
- * segment: samples per segment, 0 for the proposal's own or 64.  The device variant queues the work on `stream`
+ * segment: samples per segment, 0 for the proposal's own or 64.  With
+ * XRP_FLAG_TRACE (proposal NULL) each ray is traced on its own: at every
+ * evaluated sample the certificate radius says how many following samples
+ * share its density, and the march jumps past them.  The device variant queues the work on `stream`
  * and then waits for it (it reads back whether the list of samples left to
  * FP64 overflowed, in which case the plain integrator renders the call). */
 XRP_API int xrp_render_proposal(xrp_scene* scene, const xrp_proposal* proposal, int segment,

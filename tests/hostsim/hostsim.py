@@ -42,25 +42,26 @@ def lib():
         L.hs_render.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, I, I, I, P, I, I, I, D, D, D,
                                 D, P, P, I, P, L_, I, ctypes.c_char_p, I]
         L.hs_margin.restype = I
-        L.hs_margin.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, L_, D, D, D, P, P,
+        L.hs_margin.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, L_, D, D, D, P, P, P, P,
                                 ctypes.c_char_p, I]
         _lib = L
     return _lib
 
 
-def margin(obj, points, *, deformation=None, R=4.0, fov=40.0, ds=0.01):
-    """(density, certificate radius) of the engine's FP32 code at points [n,3]."""
+def margin(obj, points, *, deformation=None, R=4.0, fov=40.0, ds=0.01, fused=False):
+    """(density, certificate radius) of the engine's FP32 code at points [n,3];
+    with ``fused`` also the fused evaluator's (density, radius)."""
     pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
     n = pts.shape[0]
-    rho = np.zeros(n, np.float32)
-    m = np.zeros(n, np.float32)
+    rho, m, rho2, m2 = (np.zeros(n, np.float32) for _ in range(4))
     err = ctypes.create_string_buffer(512)
     rc = lib().hs_margin(json.dumps(obj).encode(),
                          json.dumps(deformation).encode() if deformation else None,
-                         pts.ctypes.data, n, R, fov, ds, rho.ctypes.data, m.ctypes.data, err, 512)
+                         pts.ctypes.data, n, R, fov, ds, rho.ctypes.data, m.ctypes.data,
+                         rho2.ctypes.data, m2.ctypes.data, err, 512)
     if rc != 0:
         raise ValueError(err.value.decode())
-    return rho, m
+    return (rho, m, rho2, m2) if fused else (rho, m)
 
 
 def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integration="simple",

@@ -108,11 +108,12 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
 
 // Density (FP32 guarded; NaN when uncertain) and distance certificate
 // (margin32, world units) at FP64 points rounded to FP32, for the soundness
-// tests of the certificates.  R and fov enter the error analysis as for a
+// tests of the certificates; also the fused evaluator's pair, which must be
+// identical.  R and fov enter the error analysis as for a
 // render with those cameras.
 extern "C" __attribute__((visibility("default"))) int hs_margin(
     const char* obj_json, const char* def_json, const double* pts, long n, double R, double fov,
-    double ds, float* rho_out, float* m_out, char* err, int errlen) {
+    double ds, float* rho_out, float* m_out, float* rho2_out, float* m2_out, char* err, int errlen) {
     try {
         HostScene hs = load_scene(obj_json, def_json, {});
         HostPrepared hp = prepare_host(hs, 8, 0, ds, R, 0.0, 1.0, fov);
@@ -128,6 +129,7 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
             float x = (float)pts[3 * q], y = (float)pts[3 * q + 1], z = (float)pts[3 * q + 2];
             rho_out[q] = density32<kMaxDepth, true>(S, x, y, z);
             m_out[q] = margin32<kMaxDepth, true>(S, x, y, z);
+            rho2_out[q] = dens_margin32<kMaxDepth, true>(S, x, y, z, m2_out[q]);
         }
         return 0;
     } catch (const std::exception& ex) {

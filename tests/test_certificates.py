@@ -23,7 +23,12 @@ from xray_projection_render_gb300 import workloads as W  # noqa: E402
 def check_scene(obj, deformation=None, n=1500, per=6, seed=0, lo=-1.1, hi=1.1, ds=0.002):
     rng = np.random.default_rng(seed)
     P = rng.uniform(lo, hi, (n, 3))
-    rho, m = hostsim.margin(obj, P, deformation=deformation, ds=ds)
+    rho, m, rho2, m2 = hostsim.margin(obj, P, deformation=deformation, ds=ds, fused=True)
+    # the fused evaluator (certificate tracing) decides and bounds identically
+    assert np.array_equal(np.isnan(rho), np.isnan(rho2))
+    ok = ~np.isnan(rho)
+    assert np.array_equal(rho[ok], rho2[ok])
+    assert np.array_equal(m[ok], m2[ok])
     sc = O.Scene(obj, deformation)
     certified = 0
     for k in range(n):

@@ -71,6 +71,17 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
+def test_certificate_tracing_matches_oracle(X, name):
+    w = CASES[name]()
+    ref = _oracle(w)
+    with X.Scene(w.obj, w.deformation) as s:
+        img, st = X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                                    trace=True, stats=True)
+    assert np.max(np.abs(img - ref) / ref) <= REL_TOL
+    assert st["evaluations"] > 0
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
 @pytest.mark.parametrize("segment,refine", [(32, False), (128, False), (64, True), (256, True)])
 def test_certificate_march_matches_oracle(X, name, segment, refine):
     w = CASES[name]()

@@ -66,6 +66,7 @@ XRP_INTEGRATE_HIERARCHICAL = 1
 XRP_FLAG_STATS = 1
 XRP_FLAG_VOLUME_LOADS = 2
 XRP_FLAG_NO_REFINE = 4
+XRP_FLAG_TRACE = 8
 
 # Every symbol include/xrp.h declares, with (restype, argtypes).
 SIGNATURES = {

@@ -607,6 +607,195 @@ XRP_HD float margin32(const SceneDev& S, float x, float y, float z) {
 }
 
 // ---------------------------------------------------------------------------
+// Density and certificate radius in one traversal (certificate tracing):
+// the same decisions as density32 and the same radius as margin32, with the
+// deformation, folds and leaf geometry computed once.
+// ---------------------------------------------------------------------------
+
+XRP_HD float leaf_dm(const Node& n, float x, float y, float z, float& m) {
+    const float* f = n.f;
+    switch (n.type) {
+    case N_SPHERE: {
+        float dx = x - f[0], dy = y - f[1], dz = z - f[2];
+        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        m = fabsf(sqrtf(d2) - sqrtf(f[3]));
+        float q = d2 - f[3];
+        if (q < -f[F_BAND]) return f[F_RHO];
+        if (q > f[F_BAND]) return 0.0f;
+        return xnan();
+    }
+    case N_BOX: {
+        float mx = f[3] - fabsf(x - f[0]);
+        float my = f[4] - fabsf(y - f[1]);
+        float mz = f[5] - fabsf(z - f[2]);
+        float mn = fminf(mx, fminf(my, mz));
+        m = fabsf(mn);
+        float b = f[F_BAND];
+        if (mn > b) return f[F_RHO];
+        if (mn < -b) return 0.0f;
+        return xnan();
+    }
+    case N_CYL: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
+        float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
+        float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
+        float len = sqrtf(1.0f / f[6]);
+        m = fabsf(fmaxf(sqrtf(p2) - sqrtf(f[7]), fmaxf(-c * len, (c - 1.0f) * len)));
+        float bc = f[F_BAND2];
+        if (c < -bc || c > 1.0f + bc) return 0.0f;
+        float q = p2 - f[7];
+        float bd = f[F_BAND];
+        if (q > bd) return 0.0f;
+        if (q < -bd && c > bc && c < 1.0f - bc) return f[F_RHO];
+        return xnan();
+    }
+    case N_PPD: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float sd = -3.0e38f, mn = 3.0e38f;
+        for (int a = 0; a < 3; a++) {
+            const float* r = f + 3 + 3 * a;
+            float q = fmaf(r[2], wz, fmaf(r[1], wy, r[0] * wx));
+            float nrm = sqrtf(fmaf(r[2], r[2], fmaf(r[1], r[1], r[0] * r[0])));
+            sd = fmaxf(sd, fmaxf(-q, q - 1.0f) / nrm);
+            mn = fminf(mn, fminf(q, 1.0f - q));
+        }
+        m = fabsf(sd);
+        float b = f[F_BAND];
+        if (mn > b) return f[F_RHO];
+        if (mn < -b) return 0.0f;
+        return xnan();
+    }
+    case N_GYROID: {
+        float X = (x - f[0]) * f[3], Y = (y - f[1]) * f[3], Z = (z - f[2]) * f[3];
+        float sx, cx, sy, cy, sz, cz;
+        f_sincos(X, &sx, &cx);
+        f_sincos(Y, &sy, &cy);
+        f_sincos(Z, &sz, &cz);
+        float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
+        float q = f[4] - fabsf(g);
+        m = fmaxf(fabsf(q) - f[F_BAND], 0.0f) / (2.4494898f * fabsf(f[3]));
+        if (q > f[F_BAND]) return f[F_RHO];
+        if (q < -f[F_BAND]) return 0.0f;
+        return xnan();
+    }
+    default: m = 0.0f; return xnan();
+    }
+}
+
+template <int D>
+XRP_HD float coll_dm(const SceneDev& S, const Node& c, float x, float y, float z, float& m);
+
+template <int D>
+XRP_HD float item_dm(const SceneDev& S, int id, float x, float y, float z, float& m) {
+    const Node& n = S.nodes[id];
+    if (n.type <= N_GYROID) return leaf_dm(n, x, y, z, m);
+    if (n.type == N_TESS) {
+        if constexpr (D > 0) {
+            const float* f = n.f;
+            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
+                             fminf(z - f[4], f[5] - z));
+            if (mo <= 0.0f) m = -mo;
+            if (mo < -f[6]) return 0.0f;
+            if (!(mo > f[6])) { m = 0.0f; return xnan(); }
+            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
+            float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
+            float bq = f[23];
+            float fr = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)), fminf(qy - ny, 1.0f - (qy - ny))),
+                             fminf(qz - nz, 1.0f - (qz - nz)));
+            if (!(fr > bq)) { m = 0.0f; return xnan(); }
+            float fc = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)) * fabsf(f[14]),
+                                   fminf(qy - ny, 1.0f - (qy - ny)) * fabsf(f[15])),
+                             fminf(qz - nz, 1.0f - (qz - nz)) * fabsf(f[16]));
+            float mm = fminf(mo, fc);
+            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
+            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
+                             fminf(fz - f[11], f[12] - fz));
+            if (mu < -f[13]) { m = fminf(mm, -mu); return 0.0f; }
+            if (!(mu > f[13])) { m = 0.0f; return xnan(); }
+            float mc;
+            float r = coll_dm<D - 1>(S, S.nodes[n.a], fx, fy, fz, mc);
+            m = fminf(fminf(mm, mu), mc);
+            return r;
+        }
+    }
+    m = 0.0f;  // voxel grids and anything deeper: density by the plain path
+    if (n.type == N_VOXEL) return voxel32(S.vols[n.a], n.f[0], x, y, z, S.hier_zero_guard);
+    return xnan();
+}
+
+template <int D>
+XRP_HD float coll_dm(const SceneDev& S, const Node& c, float x, float y, float z, float& m) {
+    const int32_t* kids = S.child + c.a;
+    int cnt = c.b;
+    const int32_t* list = nullptr;
+    m = 3.0e38f;
+    if (c.flags & C_ACCEL) {
+        int G = (c.flags >> 16) & 0xff;
+        float ux = (x - c.f[0]) * c.f[3], uy = (y - c.f[1]) * c.f[4], uz = (z - c.f[2]) * c.f[5];
+        int ix = (int)floorf(ux), iy = (int)floorf(uy), iz = (int)floorf(uz);
+        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
+        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
+        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
+        if (ix > 0) m = fminf(m, (ux - (float)ix) / c.f[3]);
+        if (ix < G - 1) m = fminf(m, ((float)(ix + 1) - ux) / c.f[3]);
+        if (iy > 0) m = fminf(m, (uy - (float)iy) / c.f[4]);
+        if (iy < G - 1) m = fminf(m, ((float)(iy + 1) - uy) / c.f[4]);
+        if (iz > 0) m = fminf(m, (uz - (float)iz) / c.f[5]);
+        if (iz < G - 1) m = fminf(m, ((float)(iz + 1) - uz) / c.f[5]);
+        m = fmaxf(m, 0.0f);
+        int cell_base = f2i(c.f[6]);
+        const int32_t* off = S.cells + cell_base + (iz * G + iy) * G + ix;
+        int s0 = off[0], s1 = off[1];
+        list = S.items + s0;
+        cnt = s1 - s0;
+    }
+    const bool greedy = (c.flags & C_GREEDY) != 0;
+    float sum = 0.0f, sabs = 0.0f;
+    bool unc = false, done = false;
+    for (int k = 0; k < cnt; k++) {
+        int slot = list ? list[k] : k;
+        float mk;
+        float r = item_dm<D>(S, kids[slot], x, y, z, mk);
+        m = fminf(m, mk);
+        if (done) continue;  // greedy value fixed; radii of the rest still count
+        if (isunc(r)) {
+            unc = true;
+            done = true;
+            continue;
+        }
+        if (greedy && r > 0.0f) {
+            sum = r;
+            sabs = fabsf(r);
+            done = true;
+            continue;
+        }
+        sum += r;
+        sabs += fabsf(r);
+    }
+    if (unc) return xnan();
+    if (greedy && done) return sum;
+    if (!(c.flags & C_EXACT_SUM) && sabs > 0.0f && fabsf(sum) <= c.f[7] * sabs) return xnan();
+    if (c.flags & C_CLIP) sum = fminf(fmaxf(sum, 0.0f), 1.0f);
+    return sum;
+}
+
+// density32 and margin32 at one point: returns the density (NaN when
+// uncertain) and sets `m` to the world-space certificate radius.
+template <int DEPTH, bool DEFS>
+XRP_HD float dens_margin32(const SceneDev& S, float x, float y, float z, float& m) {
+    if constexpr (DEFS) deform32(S, x, y, z);
+    const Node& r = S.nodes[S.root];
+    float rho;
+    if (r.type <= N_GYROID) rho = leaf_dm(r, x, y, z, m);
+    else if (r.type == N_COLL) rho = coll_dm<DEPTH>(S, r, x, y, z, m);
+    else rho = item_dm<DEPTH>(S, S.root, x, y, z, m);
+    m = fmaf(m, 0.9999f, -S.m_slack);
+    m = m > 0.0f ? m * S.inv_lip : 0.0f;
+    return rho;
+}
+
+// ---------------------------------------------------------------------------
 // FP64 exact evaluation (reference arithmetic, operation by operation)
 // ---------------------------------------------------------------------------
 

@@ -1535,6 +1535,7 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     if (!E) return code;
     if (E->device != s->device) return fail(2, "scene belongs to device %d", s->device);
     if (prop && prop->device != s->device) return fail(2, "proposal belongs to device %d", prop->device);
+    if (prop && (o->flags & XRP_FLAG_TRACE)) return fail(2, "certificate tracing takes no proposal network");
     double fov_max;
     std::vector<ViewDev> v = views_from(views, nviews, &fov_max);
     std::unique_lock<std::mutex> g(E->mtx, std::defer_lock);
@@ -1546,6 +1547,7 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     memset(&pl.Q, 0, sizeof(pl.Q));
     pl.Q.mc = segment;
     pl.Q.refine = (o->flags & XRP_FLAG_NO_REFINE) ? 0 : 1;
+    pl.Q.trace = (o->flags & XRP_FLAG_TRACE) ? 1 : 0;
     pl.Q.min_piece = 8;
     if (prop) {
         pl.Q.mlp = prop->params;

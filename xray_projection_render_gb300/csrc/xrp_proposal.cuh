@@ -31,6 +31,7 @@ struct PropParams {
     int mc;                        // samples per segment (multiple of 32)
     float tau;                     // logits above tau send a candidate to dense integration
     int refine;                    // 1: refine candidates by certificates; 0: dense
+    int trace;                     // 1: per-ray certificate tracing (k_trace) instead
     int min_piece;                 // pieces of at most this many samples go dense
     float fc[3], fs[3];            // feature normalisation (p - fc) * fs
     const int* rays;               // optional ray list: (view, i, j) triples, views absolute
@@ -119,7 +120,9 @@ __device__ __forceinline__ void write_features(const PropParams& Q, const float*
 // cache; the hot dense loop keeps its own inlined density evaluation.
 template <int DEPTH, bool DEFS>
 __device__ __noinline__ float2 eval_dm(const SceneDev& S, float x, float y, float z) {
-    return make_float2(density32<DEPTH, DEFS>(S, x, y, z), margin32<DEPTH, DEFS>(S, x, y, z));
+    float m;
+    const float rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+    return make_float2(rho, m);
 }
 
 // Dense integration of the listed pieces, the warp's lanes over each
@@ -425,6 +428,72 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 }
 
 #if defined(XRP_PROP_RENDER_KERNELS)
+// Certificate tracing: one thread per ray (16x16 pixel tiles, warps of 8x4
+// pixels like k_render, so neighbouring rays stay coherent).  At sample k
+// the density and the certificate radius m are evaluated; samples k .. k+j
+// with j*ds <= m lie inside the ball around sample k, so they all have its
+// density and are counted at once, and the march jumps to k+j+1.  Far from
+// any boundary the jumps are long; approaching one they shrink
+// geometrically; next to it the march steps sample by sample.  Samples FP32
+// cannot decide go to the FP64 list like the other march modes.
+template <int DEPTH, bool DEFS>
+__global__ void __launch_bounds__(256, 2)
+    k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
+            const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
+            const __grid_constant__ PropParams Q, float* __restrict__ out) {
+    const int res = P.res;
+    const int tpr = (res + 15) >> 4;
+    const int tpv = tpr * tpr;
+    const int b = blockIdx.x;
+    const int v = b / tpv;
+    const int t = b - v * tpv;
+    const int ti = t / tpr, tj = t - ti * tpr;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = (ti << 4) + ((warp >> 1) << 2) + (lane >> 3);
+    const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
+    unsigned evals = 0;
+    if (v < nviews && i < res && j < res) {
+        const long r = ((long)v * res + i) * res + j;
+        Ray ray;
+        {
+            Ray64 r64;
+            setup_ray64(views[view0 + v], P.xs, i, j, r64);
+            setup_ray32(r64, L.s_c, ray);
+        }
+        float t0, t1;
+        clip_ray(S.sup_lo, S.sup_hi, ray, t0, t1);
+        int k0, k1;
+        KahanF acc;
+        if (sample_range(L, t0, t1, L.K, k0, k1)) {
+            const float step = L.ds32 * 1.00001f;  // world distance between samples, rounded up
+            int k = k0;
+            while (k <= k1) {
+                const float tk = lattice_t(L, k);
+                const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
+                const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
+                const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
+                float m;
+                const float rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+                evals++;
+                if (isunc(rho)) {
+                    unsigned slot = atomicAdd(Q.fb_count, 1u);
+                    if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);
+                    k++;
+                    continue;
+                }
+                int jmp = (int)fminf(floorf(m / step), (float)(k1 - k));
+                acc.add(rho * (float)(jmp + 1));
+                k += jmp + 1;
+            }
+        }
+        out[r] = fmaf(P.density_multiplier * L.ds32, acc.s - acc.c, P.flat_field);
+    }
+    if (Q.stats) {
+        unsigned s = __reduce_add_sync(0xffffffffu, evals);
+        if (lane == 0 && s) atomicAdd(&Q.stats[kStatEvaluations], (unsigned long long)s);
+    }
+}
+
 // FP64 re-evaluation of the samples the march left undecided: adds
 // w * density (reference arithmetic at the reference's position) to the
 // ray's optical depth.  Rays are numbered within the launch (view0 first).

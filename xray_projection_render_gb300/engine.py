@@ -303,10 +303,11 @@ class Proposal:
 
 def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resolution, ds, R=4.0,
                     fov=40.0, flat_field=0.0, density_multiplier=1.0, segment=0, refine=True,
-                    out=None, stream=None, stats=False):
+                    trace=False, out=None, stream=None, stats=False):
     """Render with the proposal march (xrp_render_proposal).  ``proposal``
     None: no network (every candidate refined, or integrated densely with
-    ``refine=False``).  Host path returns a float32 array [views, res, res]
+    ``refine=False``; ``trace=True``: per-ray certificate tracing).  Host path
+    returns a float32 array [views, res, res]
     (with ``stats``: (images, dict)); a contiguous float32 CUDA tensor as
     ``out`` selects the device path."""
     L = _lib.load()
@@ -314,6 +315,8 @@ def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resoluti
     o = _opts(resolution, ds, R, flat_field, density_multiplier, "simple", stats)
     if not refine:
         o.flags |= _lib.XRP_FLAG_NO_REFINE
+    if trace:
+        o.flags |= _lib.XRP_FLAG_TRACE
     ph = proposal.handle if proposal is not None else None
     if out is not None and _is_torch_cuda(out):
         import torch
