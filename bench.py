@@ -286,7 +286,8 @@ def bench_batched(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)
-    b = X.Batch(items, ds=ds, autotune=True)
+    trace = args.march == "trace"
+    b = X.Batch(items, ds=ds, autotune=True, trace=trace)
     info = b.info()
     for _ in range(args.warmup):
         b.render(stream)
@@ -337,7 +338,8 @@ def bench_batched(args):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             sc2 = [X.Scene(o, d) for o, d in objs]
-            with X.Batch([(s2, w.angles, w.res) for s2, w in zip(sc2, ws)], ds=ds, autotune=False) as b2:
+            with X.Batch([(s2, w.angles, w.res) for s2, w in zip(sc2, ws)], ds=ds, autotune=False,
+                         trace=trace) as b2:
                 b2.render()
                 for k, o in enumerate(outs):
                     XL.check(XL.load().xrp_batch_copy_item(b2._h, k, ctypes_ptr(o)), "xrp_batch_copy_item")
@@ -357,6 +359,7 @@ def bench_batched(args):
                    "l2": "flushed before every timed step (256 MiB write); output > L2",
                    "tile": f'{info["tile_w"]}x{info["tile_h"]}', "blocks_per_sm": info["blocks_per_sm"],
                    "autotune_ms": info["tune_ms"], "graph": "one CUDA graph replay per step",
+                   "march": "certificate tracing" if trace else "plain",
                    "per_scene_calls_mrays": info["rays"] / t_seq / 1e6,
                    "parallelism": f"scenes k mod {world}"},
         "e2e": {"value": rays / t_e2e / 1e6 if e2e_times else None, "unit": "Mrays/s",

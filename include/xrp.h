@@ -222,7 +222,9 @@ XRP_API int xrp_finish_images(const float* d_images, int num_views, int res, int
  * an autotuner (timed on a sample of the batch's tiles) and captures the
  * launch in a CUDA graph; xrp_batch_render replays the graph.  Results are
  * those of xrp_render for each item.  All items share the options (ds, R,
- * integration, flat field, multiplier; opts->resolution is ignored).
+ * integration, flat field, multiplier; opts->resolution is ignored); with
+ * XRP_FLAG_TRACE in opts->flags (simple integrator) every ray is rendered
+ * by certificate tracing, which gives the same results.
  */
 typedef struct {
     xrp_scene* scene;

@@ -15,7 +15,7 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
     const char* obj_json, const char* def_json, const float* vol, int nx, int ny, int nz,
     const double* cams, int ncams, int res, int integration, double ds, double R, double ff,
     double dm, float* out, unsigned long long* stats, int nthreads, const int* rays, long nrays,
-    int force_general, char* err, int errlen) {
+    int force_general, int trace, char* err, int errlen) {
     try {
         std::vector<HVolume> ext;
         if (vol) {
@@ -45,6 +45,7 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
         S.child = hp.fs.child.data();
         S.cells = hp.fs.cells.data();
         S.items = hp.fs.items.data();
+        S.clear = hp.fs.clear.data();
         S.defs = hp.fs.defs.data();
         S.vols = hp.vols.data();
         Lattice L = hp.hl.hdr;
@@ -74,7 +75,11 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
                 RayStats st{0, 0};
                 float val;
                 bool hier = integration == 1;
-                if (hier)
+                if (trace && !hier) {
+                    unsigned ev = 0;
+                    val = trace_pixel<kMaxDepth, true>(S, L, P, views[v], i, j, ev);
+                    st.samples = ev;
+                } else if (hier)
                     val = vf ? render_pixel<true, true>(S, L, P, views[v], i, j, st)
                              : render_pixel<true, false>(S, L, P, views[v], i, j, st);
                 else
@@ -123,6 +128,7 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
         S.child = hp.fs.child.data();
         S.cells = hp.fs.cells.data();
         S.items = hp.fs.items.data();
+        S.clear = hp.fs.clear.data();
         S.defs = hp.fs.defs.data();
         S.vols = hp.vols.data();
         for (long q = 0; q < n; q++) {

@@ -77,3 +77,25 @@ def test_batch_rejects_bad_items(X):
             X.Batch([(s, w.angles, 0)], ds=0.01)
         with pytest.raises(EngineError):
             X.Batch([(s, w.angles, 16)], ds=-1.0)
+
+
+def test_batch_with_certificate_tracing(X):
+    ws = _items()
+    ds = 0.005
+    scenes = [X.Scene(w.obj, w.deformation) for w in ws]
+    try:
+        with X.Batch([(s, w.angles, w.res) for s, w in zip(scenes, ws)], ds=ds, trace=True) as b:
+            b.render()
+            for k, (s, w) in enumerate(zip(scenes, ws)):
+                single = X.render(s, w.angles, resolution=w.res, ds=ds)
+                # same samples, summed in another order (runs of equal density)
+                assert np.max(np.abs(b.item(k) - single) / single) <= 2 * REL_TOL, w.name
+            w = ws[4]
+            ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, ds, R=w.R, fov=w.fov)
+            assert np.max(np.abs(b.item(4) - ref) / ref) <= REL_TOL
+        from xray_projection_render_gb300._lib import EngineError
+        with pytest.raises(EngineError):
+            X.Batch([(scenes[0], ws[0].angles, ws[0].res)], ds=ds, trace=True, integration="hierarchical")
+    finally:
+        for s in scenes:
+            s.close()

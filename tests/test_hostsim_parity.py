@@ -116,3 +116,27 @@ def test_greedy_sum_and_cancellation():
         w = W.Workload("g", c, None, [(0.0, 90.0), (70.0, 60.0)], 96, 0.004)
         check(w)
         check(w, "hierarchical")
+
+
+@pytest.mark.parametrize("name", ["gyroid", "lattice", "config1", "batched", "coll_defs"])
+def test_certificate_tracing(name):
+    """Certificate tracing (trace_pixel, the algorithm of k_trace and the
+    tracing batch kernel) against the FP64 oracle on the CPU build."""
+    if name == "gyroid":
+        w = W.reduced(W.gyroid_sigmoid(), 128, 4)
+    elif name == "lattice":
+        w = W.reduced(W.deformed_lattice(), 128, 3)
+    elif name == "config1":
+        w = W.cube_minus_sphere_cylinder(128)
+    elif name == "batched":
+        w = W.reduced(W.batched_scenes(3)[2], 128, 3)
+    else:
+        coll = {"type": "object_collection", "objects": [
+            {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+            {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+            {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0}]}
+        w = W.Workload("c", coll, {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02],
+                                   "sigmas": [0.3, 0.3, 0.5], "centers": [0.0, 0.1, 0.0]},
+                       [(10.0, 80.0), (200.0, 120.0)], 64, 0.01)
+    st = check(w, nrays=1500, trace=True)
+    assert st[0] > 0

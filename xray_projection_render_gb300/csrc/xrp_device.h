@@ -145,6 +145,7 @@ struct SceneDev {
     const int32_t* child;   // child node ids of collections
     const int32_t* cells;   // accel: per collection, (G^3 + 1) offsets into items
     const int32_t* items;   // accel: child slots (positions within the collection)
+    const float* clear;     // accel: per cell, distance to the nearest child not listed
     const Volume* vols;
     const DefStep* defs;
     int32_t root;
@@ -578,9 +579,11 @@ XRP_HD float collm32(const SceneDev& S, const Node& c, float x, float y, float z
         if (iy < G - 1) m = fminf(m, ((float)(iy + 1) - uy) / c.f[4]);
         if (iz > 0) m = fminf(m, (uz - (float)iz) / c.f[5]);
         if (iz < G - 1) m = fminf(m, ((float)(iz + 1) - uz) / c.f[5]);
-        m = fmaxf(m, 0.0f);
         int cell_base = f2i(c.f[6]);
-        const int32_t* off = S.cells + cell_base + (iz * G + iy) * G + ix;
+        const int cell = cell_base + (iz * G + iy) * G + ix;
+        // unlisted children are beyond the cell's faces and beyond its clearance
+        m = fmaxf(fmaxf(m, 0.0f), S.clear[cell]);
+        const int32_t* off = S.cells + cell;
         int s0 = off[0], s1 = off[1];
         list = S.items + s0;
         cnt = s1 - s0;
@@ -743,9 +746,11 @@ XRP_HD float coll_dm(const SceneDev& S, const Node& c, float x, float y, float z
         if (iy < G - 1) m = fminf(m, ((float)(iy + 1) - uy) / c.f[4]);
         if (iz > 0) m = fminf(m, (uz - (float)iz) / c.f[5]);
         if (iz < G - 1) m = fminf(m, ((float)(iz + 1) - uz) / c.f[5]);
-        m = fmaxf(m, 0.0f);
         int cell_base = f2i(c.f[6]);
-        const int32_t* off = S.cells + cell_base + (iz * G + iy) * G + ix;
+        const int cell = cell_base + (iz * G + iy) * G + ix;
+        // unlisted children are beyond the cell's faces and beyond its clearance
+        m = fmaxf(fmaxf(m, 0.0f), S.clear[cell]);
+        const int32_t* off = S.cells + cell;
         int s0 = off[0], s1 = off[1];
         list = S.items + s0;
         cnt = s1 - s0;
@@ -1481,6 +1486,63 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
         prev_zero = zero;
     }
     return acc.s;
+}
+
+// Certificate tracing of one ray over lattice samples [k0, k1]: at sample k
+// the density and the certificate radius m (dens_margin32); the samples
+// k..k+j with j*ds <= m lie inside the ball around sample k, so they share
+// its density and are counted at once.  `unc(k)` returns the value of a
+// sample FP32 cannot decide (its FP64 density, or 0 when the caller
+// re-evaluates it later).  Returns the Kahan-compensated sum of densities,
+// the same terms as march_simple.
+template <int DEPTH, bool DEFS, class Unc>
+XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
+                       unsigned& evals) {
+    KahanF acc;
+    const float step = L.ds32 * 1.00001f;  // world distance between samples, rounded up
+    int k = k0;
+    while (k <= k1) {
+        const float tk = lattice_t(L, k);
+        const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
+        const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
+        const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
+        float m;
+        const float rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+        evals++;
+        if (isunc(rho)) {
+            acc.add(unc(k));
+            k++;
+            continue;
+        }
+        const int jmp = (int)fminf(floorf(m / step), (float)(k1 - k));
+        acc.add(rho * (float)(jmp + 1));
+        k += jmp + 1;
+    }
+    return acc.s - acc.c;
+}
+
+// One pixel by certificate tracing (simple integrator), FP64 for undecided
+// samples in place.
+template <int DEPTH, bool DEFS>
+XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P, const ViewDev& V,
+                         int i, int j, unsigned& evals) {
+    Ray r;
+    {
+        Ray64 r64;
+        setup_ray64(V, P.xs, i, j, r64);
+        setup_ray32(r64, L.s_c, r);
+    }
+    float t0, t1;
+    clip_ray(S.sup_lo, S.sup_hi, r, t0, t1);
+    int k0, k1;
+    float acc = 0.0f;
+    if (sample_range(L, t0, t1, L.K, k0, k1)) {
+        acc = trace_sum<DEPTH, DEFS>(
+            S, L, r, k0, k1,
+            [&](int k) { return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[k]); }, evals);
+    }
+    float T = fmaf(P.density_multiplier * L.ds32, acc, P.flat_field);
+    return expf(-T);
 }
 
 // One pixel: optical depth T = flat_field + multiplier * (sum), as

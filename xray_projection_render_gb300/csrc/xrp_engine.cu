@@ -446,6 +446,7 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     Tables T;
     size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
     size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
+    size_t o_clear = T.add(fs.clear);
     size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs);
     size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
     size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
@@ -461,6 +462,7 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     S.child = (const int32_t*)(base + o_child);
     S.cells = (const int32_t*)(base + o_cells);
     S.items = (const int32_t*)(base + o_items);
+    S.clear = (const float*)(base + o_clear);
     S.defs = (const DefStep*)(base + o_defs);
     S.vols = (const Volume*)(base + o_vols);
     out.L = hl.hdr;
@@ -1005,14 +1007,14 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     // one upload: per item its scene tables, views and pixel table, then the
     // lattice, the SceneDev array and the item array (patched with addresses)
     Tables T;
-    struct Off { size_t nodes, n64, child, cells, items, defs, vols, xs; };
+    struct Off { size_t nodes, n64, child, cells, items, defs, vols, xs, clear; };
     std::vector<Off> off(n);
     std::vector<ViewDev> allv;  // every item's views, in work order
     std::vector<int> view0(n);
     for (int q = 0; q < n; q++) {
         const FlatScene& fs = hps[q].fs;
         off[q] = {T.add(fs.nodes), T.add(fs.nodes64), T.add(fs.child), T.add(fs.cells), T.add(fs.items),
-                  T.add(fs.defs), T.add(hps[q].vols), T.add(hps[q].xs)};
+                  T.add(fs.defs), T.add(hps[q].vols), T.add(hps[q].xs), T.add(fs.clear)};
         view0[q] = (int)allv.size();
         allv.insert(allv.end(), vws[q].begin(), vws[q].end());
     }
@@ -1035,6 +1037,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         S.child = (const int32_t*)(base + off[q].child);
         S.cells = (const int32_t*)(base + off[q].cells);
         S.items = (const int32_t*)(base + off[q].items);
+        S.clear = (const float*)(base + off[q].clear);
         S.defs = (const DefStep*)(base + off[q].defs);
         S.vols = (const Volume*)(base + off[q].vols);
         sdev[q] = S;
@@ -1073,8 +1076,11 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
     const bool hier = oo.integration == XRP_INTEGRATE_HIERARCHICAL;
+    const bool trace = (oo.flags & XRP_FLAG_TRACE) != 0;
+    if (trace && hier) return fail(2, "certificate tracing needs the simple integrator");
     const int kdepth = depth == 0 ? 0 : kMaxDepth;
-    if ((e = batch_blocks_per_sm(kdepth, defs, hier, &occ)) != cudaSuccess) return cuda_fail(7, "batch occupancy", e);
+    if ((e = batch_blocks_per_sm(kdepth, defs, hier, trace, &occ)) != cudaSuccess)
+        return cuda_fail(7, "batch occupancy", e);
     occ = std::max(occ, 1);
     BatchLaunch bl;
     memset(&bl, 0, sizeof(bl));
@@ -1086,6 +1092,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     bl.depth = kdepth;
     bl.defs = defs;
     bl.hier = hier;
+    bl.trace = trace;
     bl.counter = B->counter;
     bl.out = B->out;
     auto upload = [&](int tw, int th) -> cudaError_t {
@@ -1760,6 +1767,7 @@ extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, 
     Tables T;
     size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
     size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
+    size_t o_clear = T.add(fs.clear);
     size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs);
     size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
     size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
@@ -1777,6 +1785,7 @@ extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, 
     pr.S.child = (const int32_t*)(base + o_child);
     pr.S.cells = (const int32_t*)(base + o_cells);
     pr.S.items = (const int32_t*)(base + o_items);
+    pr.S.clear = (const float*)(base + o_clear);
     pr.S.defs = (const DefStep*)(base + o_defs);
     pr.S.vols = (const Volume*)(base + o_vols);
     pr.L = hl.hdr;

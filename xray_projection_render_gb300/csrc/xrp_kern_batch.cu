@@ -21,7 +21,7 @@ struct BatchStage {
     ViewDev V;
 };
 
-template <bool HIER, int DEPTH, bool DEFS>
+template <bool HIER, int DEPTH, bool DEFS, bool TRACE>
 __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
     k_batch(const SceneDev* __restrict__ scenes, const BatchItemDev* __restrict__ items, int nitems,
             const ViewDev* __restrict__ views, const __grid_constant__ Lattice L, long long ntiles, int tw,
@@ -75,40 +75,51 @@ __global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
         const int i = ty * th + lane / tw;
         const int j = tx * tw + lane % tw;
         if (i < res && j < res) {
-            RayStats st{0, 0};
-            float val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);
+            float val;
+            if constexpr (TRACE) {
+                unsigned ev = 0;
+                val = trace_pixel<DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, ev);
+            } else {
+                RayStats st{0, 0};
+                val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);
+            }
             out[B.out0 + ((long long)v * res + i) * res + j] = val;
         }
         __syncwarp();  // before the next tile overwrites the staged data
     }
 }
 
-template <bool HIER, int DEPTH, bool DEFS>
+template <bool HIER, int DEPTH, bool DEFS, bool TRACE>
 static cudaError_t launch_batch_t(const BatchLaunch& b, cudaStream_t st) {
-    k_batch<HIER, DEPTH, DEFS><<<b.blocks, 256, 0, st>>>(b.scenes, b.items, b.nitems, b.views, b.L, b.ntiles,
-                                                         b.tw, b.th, b.counter, b.stride, b.limit, b.out);
+    k_batch<HIER, DEPTH, DEFS, TRACE><<<b.blocks, 256, 0, st>>>(b.scenes, b.items, b.nitems, b.views, b.L,
+                                                                b.ntiles, b.tw, b.th, b.counter, b.stride,
+                                                                b.limit, b.out);
     return cudaGetLastError();
+}
+
+template <int DEPTH, bool DEFS>
+static cudaError_t launch_batch_d(const BatchLaunch& b, cudaStream_t st) {
+    if (b.trace) return launch_batch_t<false, DEPTH, DEFS, true>(b, st);
+    if (b.hier) return launch_batch_t<true, DEPTH, DEFS, false>(b, st);
+    return launch_batch_t<false, DEPTH, DEFS, false>(b, st);
 }
 
 cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st) {
     if (b.blocks <= 0 || b.ntiles <= 0) return cudaSuccess;
-    if (b.hier) {
-        if (b.depth == 0) return b.defs ? launch_batch_t<true, 0, true>(b, st) : launch_batch_t<true, 0, false>(b, st);
-        return b.defs ? launch_batch_t<true, 3, true>(b, st) : launch_batch_t<true, 3, false>(b, st);
-    }
-    if (b.depth == 0) return b.defs ? launch_batch_t<false, 0, true>(b, st) : launch_batch_t<false, 0, false>(b, st);
-    return b.defs ? launch_batch_t<false, 3, true>(b, st) : launch_batch_t<false, 3, false>(b, st);
+    if (b.depth == 0) return b.defs ? launch_batch_d<0, true>(b, st) : launch_batch_d<0, false>(b, st);
+    return b.defs ? launch_batch_d<3, true>(b, st) : launch_batch_d<3, false>(b, st);
 }
 
-cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int* out) {
-    const void* f;
-    if (hier) {
-        if (depth == 0) f = defs ? (const void*)k_batch<true, 0, true> : (const void*)k_batch<true, 0, false>;
-        else f = defs ? (const void*)k_batch<true, 3, true> : (const void*)k_batch<true, 3, false>;
-    } else {
-        if (depth == 0) f = defs ? (const void*)k_batch<false, 0, true> : (const void*)k_batch<false, 0, false>;
-        else f = defs ? (const void*)k_batch<false, 3, true> : (const void*)k_batch<false, 3, false>;
-    }
+template <int DEPTH, bool DEFS>
+static const void* batch_fn(bool hier, bool trace) {
+    if (trace) return (const void*)k_batch<false, DEPTH, DEFS, true>;
+    if (hier) return (const void*)k_batch<true, DEPTH, DEFS, false>;
+    return (const void*)k_batch<false, DEPTH, DEFS, false>;
+}
+
+cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, bool trace, int* out) {
+    const void* f = depth == 0 ? (defs ? batch_fn<0, true>(hier, trace) : batch_fn<0, false>(hier, trace))
+                               : (defs ? batch_fn<3, true>(hier, trace) : batch_fn<3, false>(hier, trace));
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, f, 256, 0);
 }
 

@@ -88,6 +88,7 @@ struct BatchLaunch {
     int blocks;            // persistent grid size
     int depth;             // 0: no tessellation in the batch, else up to kMaxDepth
     bool defs, hier;
+    bool trace;            // certificate tracing (simple integrator)
     unsigned long long* counter;
     long long stride, limit;
     float* out;
@@ -95,7 +96,7 @@ struct BatchLaunch {
 
 // xrp_kern_batch.cu: the batch kernel and its occupancy.
 cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st);
-cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int* out);
+cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, bool trace, int* out);
 
 // xrp_kern_export.cu: volume export of a scene and device-side image finishing.
 cudaError_t launch_voxelize_scene(const SceneDev& S, int depth, bool defs, int res, double dm, float* out,

@@ -463,30 +463,18 @@ __global__ void __launch_bounds__(256, 2)
         float t0, t1;
         clip_ray(S.sup_lo, S.sup_hi, ray, t0, t1);
         int k0, k1;
-        KahanF acc;
+        float sum = 0.0f;
         if (sample_range(L, t0, t1, L.K, k0, k1)) {
-            const float step = L.ds32 * 1.00001f;  // world distance between samples, rounded up
-            int k = k0;
-            while (k <= k1) {
-                const float tk = lattice_t(L, k);
-                const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
-                const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
-                const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
-                float m;
-                const float rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
-                evals++;
-                if (isunc(rho)) {
+            sum = trace_sum<DEPTH, DEFS>(
+                S, L, ray, k0, k1,
+                [&](int k) {
                     unsigned slot = atomicAdd(Q.fb_count, 1u);
                     if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);
-                    k++;
-                    continue;
-                }
-                int jmp = (int)fminf(floorf(m / step), (float)(k1 - k));
-                acc.add(rho * (float)(jmp + 1));
-                k += jmp + 1;
-            }
+                    return 0.0f;
+                },
+                evals);
         }
-        out[r] = fmaf(P.density_multiplier * L.ds32, acc.s - acc.c, P.flat_field);
+        out[r] = fmaf(P.density_multiplier * L.ds32, sum, P.flat_field);
     }
     if (Q.stats) {
         unsigned s = __reduce_add_sync(0xffffffffu, evals);

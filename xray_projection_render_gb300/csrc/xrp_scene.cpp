@@ -843,15 +843,29 @@ struct Flattener {
                         if (ix == G - 1) hi[0] = kInf;
                         if (iy == G - 1) hi[1] = kInf;
                         if (iz == G - 1) hi[2] = kInf;
+                        // clearance: distance from the (dilated) cell to the
+                        // nearest child that is not listed (certificate radii)
+                        double clear2 = kInf;
                         for (size_t k = 0; k < kids.size(); k++) {
                             const Box3& b = infos[k].box;
                             if (b.empty()) continue;
                             bool hit = true;
                             for (int a = 0; a < 3; a++) hit = hit && b.lo[a] <= hi[a] && b.hi[a] >= lo[a];
-                            if (hit) fs.items.push_back((int32_t)k);
+                            if (hit) {
+                                fs.items.push_back((int32_t)k);
+                            } else {
+                                double d2 = 0;
+                                for (int a = 0; a < 3; a++) {
+                                    double gap = std::max(b.lo[a] - hi[a], lo[a] - b.hi[a]);
+                                    if (gap > 0) d2 += gap * gap;
+                                }
+                                clear2 = std::min(clear2, d2);
+                            }
                         }
+                        fs.clear.push_back(clear2 >= kInf ? 3.0e38f : (float)(std::sqrt(clear2) * (1.0 - 1e-6)));
                     }
             fs.cells.push_back((int32_t)fs.items.size());
+            fs.clear.push_back(0.0f);
             flags |= C_ACCEL | (G << 16);
         }
         flags |= homo << 8;

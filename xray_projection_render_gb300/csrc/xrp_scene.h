@@ -72,6 +72,7 @@ struct FlatScene {
     std::vector<int32_t> child;
     std::vector<int32_t> cells;
     std::vector<int32_t> items;
+    std::vector<float> clear;  // per cell of `cells`: distance to the nearest unlisted child
     std::vector<DefStep> defs;
     int root = 0;
     bool bounded = true;

@@ -191,7 +191,7 @@ class Batch:
     triples; every item shares ds, R, fov and the other options."""
 
     def __init__(self, items, *, ds, R=4.0, fov=40.0, flat_field=0.0, density_multiplier=1.0,
-                 integration="simple", autotune=True):
+                 integration="simple", autotune=True, trace=False):
         L = _lib.load()
         self._keep = []
         arr = (_lib.XrpBatchItem * len(items))()
@@ -202,6 +202,8 @@ class Batch:
             arr[k] = _lib.XrpBatchItem(scene.handle, ctypes.cast(cams, ctypes.c_void_p), n, int(res))
             self.shapes.append((n, int(res), int(res)))
         o = _opts(items[0][2], ds, R, flat_field, density_multiplier, integration, False)
+        if trace:
+            o.flags |= _lib.XRP_FLAG_TRACE
         h = ctypes.c_void_p()
         check(L.xrp_batch_create(arr, len(items), ctypes.byref(o), 1 if autotune else 0,
                                  ctypes.byref(h)), "xrp_batch_create")
