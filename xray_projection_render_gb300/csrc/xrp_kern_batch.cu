@@ -22,7 +22,7 @@ struct BatchStage {
 };
 
 template <bool HIER, int DEPTH, bool DEFS, bool TRACE>
-__global__ void __launch_bounds__(256, XRP_SCENE_MIN_BLOCKS)
+__global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 3 : XRP_SCENE_MIN_BLOCKS)
     k_batch(const SceneDev* __restrict__ scenes, const BatchItemDev* __restrict__ items, int nitems,
             const ViewDev* __restrict__ views, const __grid_constant__ Lattice L, long long ntiles, int tw,
             int th, unsigned long long* __restrict__ counter, long long stride, long long limit,

@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // geometrically; next to it the march steps sample by sample.  Samples FP32
 // cannot decide go to the FP64 list like the other march modes.
 template <int DEPTH, bool DEFS>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
