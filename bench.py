@@ -619,10 +619,10 @@ def main():
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
         # plain: one render launch per step (all views); march modes: per
-        # launch group of at most 16 M rays, the march, its FP64 pass and
+        # launch group of at most 8 M rays, the march, its FP64 pass and
         # the exp pass
         "gpu_launches": args.steps * (1 if (args.march == "plain" or is_voxel)
-                                      else 3 * -(-n_my * img // (1 << 24))),
+                                      else 3 * -(-n_my * img // (1 << 23))),
         "roofline": dict(roof, **{
                      "traffic": TRAFFIC.get(args.workload, {}).get("bytes_per_view", 0) * n_my or None,
                      "traffic_source": TRAFFIC.get(args.workload, {}).get("source"),

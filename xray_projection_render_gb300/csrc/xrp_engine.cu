@@ -1573,8 +1573,10 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
         pl.Q.stats = (unsigned long long*)sb.p;
     }
     // list of samples for FP64 re-evaluation (per launch of at most
-    // pl.max_rays rays; reused): half an entry per ray
-    const unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, pl.max_rays / 2);
+    // pl.max_rays rays; reused): four entries per ray (the deformed lattice
+    // leaves about one undecided sample per ray; an overflow costs a plain
+    // re-render of the whole call)
+    const unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, pl.max_rays * 4);
     PoolBuf fb, fbc;
     if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
         (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)

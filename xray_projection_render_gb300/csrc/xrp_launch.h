@@ -53,7 +53,7 @@ struct Prepared {
 struct PropLaunch {
     PropParams Q;
     bool train = false;
-    long long max_rays = 1LL << 24;  // rays per launch (bounds the FP64 list)
+    long long max_rays = 1LL << 23;  // rays per launch (bounds the FP64 list: 4 entries per ray)
 };
 
 // xrp_kern_scene.cu: k_render for general scenes.
