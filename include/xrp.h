@@ -327,8 +327,9 @@ XRP_API int xrp_render_proposal_device(xrp_scene* scene, const xrp_proposal* pro
  * XRP_FLAG_STATS: segments, segments certified, pieces certified in
  * refinement, pieces integrated densely, dense samples, certificate
  * evaluations, FP64 re-evaluations, network rounds, candidates routed to
- * dense integration, candidates refined. */
-XRP_API int xrp_proposal_last_stats(uint64_t out[10]);
+ * dense integration, candidates refined, and 1 when the list of samples left
+ * to FP64 overflowed (the call was then rendered by the plain integrator). */
+XRP_API int xrp_proposal_last_stats(uint64_t out[11]);
 
 /* The network's training step on the GPU, exposed for gradient checks:
  * for `rows` BF16 feature rows X (uint16 bit patterns, [rows][64]) and 0/1

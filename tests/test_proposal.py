@@ -78,7 +78,7 @@ def test_certificate_tracing_matches_oracle(X, name):
         img, st = X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
                                     trace=True, stats=True)
     assert np.max(np.abs(img - ref) / ref) <= REL_TOL
-    assert st["evaluations"] > 0
+    assert st["evaluations"] > 0 and st["fp64_list_overflow"] == 0
 
 
 @pytest.mark.parametrize("name", sorted(CASES))

@@ -1608,6 +1608,7 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
             (e = cudaStreamSynchronize(st)) != cudaSuccess)
             return cuda_fail(7, "stats read", e);
         for (int q = 0; q < kStatCount; q++) t_prop_stats[q] = h[q];
+        t_prop_stats[kStatOverflows] = ovf ? 1 : 0;
     }
     return 0;
 }
@@ -1622,7 +1623,7 @@ int xrp_render_proposal_device(xrp_scene* s, const xrp_proposal* prop, int segme
     return render_proposal(s, prop, segment, views, nviews, o, out_device, false, stream);
 }
 
-int xrp_proposal_last_stats(uint64_t out[10]) {
+int xrp_proposal_last_stats(uint64_t out[11]) {
     if (!out) return fail(1, "null pointer");
     for (int q = 0; q < kStatCount; q++) out[q] = t_prop_stats[q];
     return 0;

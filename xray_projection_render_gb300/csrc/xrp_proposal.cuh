@@ -61,6 +61,7 @@ enum : int {
     kStatMlpRounds,     // warp-wide network evaluations (32 rows each)
     kStatRoutedDense,   // candidates the network sent to dense integration
     kStatSubdivided,    // candidates refined by certificates
+    kStatOverflows,     // launches whose FP64 list overflowed (host; the call re-rendered plainly)
     kStatCount
 };
 

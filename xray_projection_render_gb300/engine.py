@@ -245,7 +245,7 @@ class Batch:
 
 
 PROPOSAL_STATS = ("segments", "certified", "refined", "dense", "dense_samples", "evaluations",
-                  "fp64_samples", "mlp_rounds", "routed_dense", "subdivided")
+                  "fp64_samples", "mlp_rounds", "routed_dense", "subdivided", "fp64_list_overflow")
 
 
 class Proposal:
@@ -336,7 +336,7 @@ def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resoluti
     check(L.xrp_render_proposal(scene.handle, ph, int(segment), cams, n, ctypes.byref(o),
                                 ctypes.c_void_p(ptr)), "xrp_render_proposal")
     if stats:
-        c = (ctypes.c_uint64 * 10)()
+        c = (ctypes.c_uint64 * 11)()
         L.xrp_proposal_last_stats(c)
         return out, dict(zip(PROPOSAL_STATS, list(c)))
     return out
