@@ -479,7 +479,7 @@ XRP_HD float leaf_margin(const Node& n, float x, float y, float z) {
     case N_SPHERE: {
         float dx = x - f[0], dy = y - f[1], dz = z - f[2];
         float d = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
-        return fabsf(d - sqrtf(f[3]));
+        return fabsf(d - f[4]);
     }
     case N_BOX: {
         float mx = f[3] - fabsf(x - f[0]);
@@ -492,8 +492,8 @@ XRP_HD float leaf_margin(const Node& n, float x, float y, float z) {
         float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
         float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
         float pr = sqrtf(fmaf(pz, pz, fmaf(py, py, px * px)));
-        float len = sqrtf(1.0f / f[6]);
-        float sd = fmaxf(pr - sqrtf(f[7]), fmaxf(-c * len, (c - 1.0f) * len));
+        float len = f[9];
+        float sd = fmaxf(pr - f[8], fmaxf(-c * len, (c - 1.0f) * len));
         return fabsf(sd);
     }
     case N_PPD: {
@@ -621,7 +621,7 @@ XRP_HD float leaf_dm(const Node& n, float x, float y, float z, float& m) {
     case N_SPHERE: {
         float dx = x - f[0], dy = y - f[1], dz = z - f[2];
         float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        m = fabsf(sqrtf(d2) - sqrtf(f[3]));
+        m = fabsf(sqrtf(d2) - f[4]);
         float q = d2 - f[3];
         if (q < -f[F_BAND]) return f[F_RHO];
         if (q > f[F_BAND]) return 0.0f;
@@ -643,8 +643,8 @@ XRP_HD float leaf_dm(const Node& n, float x, float y, float z, float& m) {
         float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
         float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
         float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
-        float len = sqrtf(1.0f / f[6]);
-        m = fabsf(fmaxf(sqrtf(p2) - sqrtf(f[7]), fmaxf(-c * len, (c - 1.0f) * len)));
+        float len = f[9];
+        m = fabsf(fmaxf(sqrtf(p2) - f[8], fmaxf(-c * len, (c - 1.0f) * len)));
         float bc = f[F_BAND2];
         if (c < -bc || c > 1.0f + bc) return 0.0f;
         float q = p2 - f[7];

@@ -537,6 +537,7 @@ struct Flattener {
             double band = 2 * r * dist + dist * dist + 8 * kU * (r + dist) * (r + dist) + 2 * kU * r * r;
             for (int a = 0; a < 3; a++) n.f[a] = (float)d[a];
             n.f[3] = (float)(d[3] * d[3]);
+            n.f[4] = (float)r;  // certificate radii
             n.f[F_BAND] = (float)(kSafety * band);
             rho = d[4];
             double reff = std::sqrt(r * r + kSafety * band) + E;
@@ -589,6 +590,8 @@ struct Flattener {
             }
             n.f[6] = (float)(1.0 / vv);
             n.f[7] = (float)(r * r);
+            n.f[8] = (float)r;   // certificate radii: radius and axis length
+            n.f[9] = (float)vl;
             n.f[F_BAND2] = (float)(kSafety * band_c);
             n.f[F_BAND] = (float)(kSafety * band_d);
             double reff = std::sqrt(r * r + kSafety * band_d) + vl * kSafety * band_c + E;
