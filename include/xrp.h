@@ -115,7 +115,7 @@ enum {
     XRP_FLAG_STATS = 1,        /* count evaluated and FP64-re-evaluated samples */
     XRP_FLAG_VOLUME_LOADS = 2, /* voxel-grid roots: per-tap loads instead of texture gathers */
     XRP_FLAG_NO_REFINE = 4,    /* proposal march: no certificate refinement of segments */
-    XRP_FLAG_TRACE = 8         /* proposal march: per-ray certificate tracing (no network) */
+    XRP_FLAG_TRACE = 8         /* per-ray certificate tracing (proposal march without network, batches) */
 };
 
 /* Per-call options: the globals and flags of the reference CLI
@@ -223,8 +223,8 @@ XRP_API int xrp_finish_images(const float* d_images, int num_views, int res, int
  * launch in a CUDA graph; xrp_batch_render replays the graph.  Results are
  * those of xrp_render for each item.  All items share the options (ds, R,
  * integration, flat field, multiplier; opts->resolution is ignored); with
- * XRP_FLAG_TRACE in opts->flags (simple integrator) every ray is rendered
- * by certificate tracing, which gives the same results.
+ * XRP_FLAG_TRACE in opts->flags every ray is rendered by certificate
+ * tracing (either integrator), which gives the same results.
  */
 typedef struct {
     xrp_scene* scene;
@@ -312,9 +312,11 @@ XRP_API void xrp_proposal_destroy(xrp_proposal* p);
 /* Renders like xrp_render with the proposal march.  `proposal` NULL: every
  * candidate is refined (or, with XRP_FLAG_NO_REFINE, integrated densely);
  * segment: samples per segment, 0 for the proposal's own or 64.  With
- * XRP_FLAG_TRACE (proposal NULL) each ray is traced on its own: at every
- * evaluated sample the certificate radius says how many following samples
- * share its density, and the march jumps past them.  The device variant queues the work on `stream`
+ * XRP_FLAG_TRACE (proposal NULL; simple or hierarchical integrator) each ray
+ * is traced on its own: at every evaluated sample the certificate radius
+ * says how many following samples share its density, and the march jumps
+ * past them (the hierarchical integrator still refines every coarse sample
+ * whose zero-ness changes).  The device variant queues the work on `stream`
  * and then waits for it (it reads back whether the list of samples left to
  * FP64 overflowed, in which case the plain integrator renders the call). */
 XRP_API int xrp_render_proposal(xrp_scene* scene, const xrp_proposal* proposal, int segment,

@@ -75,9 +75,10 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
                 RayStats st{0, 0};
                 float val;
                 bool hier = integration == 1;
-                if (trace && !hier) {
+                if (trace) {
                     unsigned ev = 0;
-                    val = trace_pixel<kMaxDepth, true>(S, L, P, views[v], i, j, ev);
+                    val = hier ? trace_pixel<true, kMaxDepth, true>(S, L, P, views[v], i, j, ev)
+                               : trace_pixel<false, kMaxDepth, true>(S, L, P, views[v], i, j, ev);
                     st.samples = ev;
                 } else if (hier)
                     val = vf ? render_pixel<true, true>(S, L, P, views[v], i, j, st)

@@ -93,9 +93,12 @@ def test_batch_with_certificate_tracing(X):
             w = ws[4]
             ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, ds, R=w.R, fov=w.fov)
             assert np.max(np.abs(b.item(4) - ref) / ref) <= REL_TOL
-        from xray_projection_render_gb300._lib import EngineError
-        with pytest.raises(EngineError):
-            X.Batch([(scenes[0], ws[0].angles, ws[0].res)], ds=ds, trace=True, integration="hierarchical")
+        with X.Batch([(s, w.angles, w.res) for s, w in zip(scenes, ws)], ds=ds, trace=True,
+                     integration="hierarchical") as bh:
+            bh.render()
+            for k, (s, w) in enumerate(zip(scenes, ws)):
+                single = X.render(s, w.angles, resolution=w.res, ds=ds, integration="hierarchical")
+                assert np.max(np.abs(bh.item(k) - single) / single) <= 2 * REL_TOL, w.name
     finally:
         for s in scenes:
             s.close()

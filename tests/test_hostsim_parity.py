@@ -118,10 +118,12 @@ def test_greedy_sum_and_cancellation():
         check(w, "hierarchical")
 
 
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 @pytest.mark.parametrize("name", ["gyroid", "lattice", "config1", "batched", "coll_defs"])
-def test_certificate_tracing(name):
+def test_certificate_tracing(name, integration):
     """Certificate tracing (trace_pixel, the algorithm of k_trace and the
-    tracing batch kernel) against the FP64 oracle on the CPU build."""
+    tracing batch kernel), both integrators, against the FP64 oracle on the
+    CPU build."""
     if name == "gyroid":
         w = W.reduced(W.gyroid_sigmoid(), 128, 4)
     elif name == "lattice":
@@ -138,5 +140,5 @@ def test_certificate_tracing(name):
         w = W.Workload("c", coll, {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02],
                                    "sigmas": [0.3, 0.3, 0.5], "centers": [0.0, 0.1, 0.0]},
                        [(10.0, 80.0), (200.0, 120.0)], 64, 0.01)
-    st = check(w, nrays=1500, trace=True)
+    st = check(w, integration, nrays=1500, trace=True)
     assert st[0] > 0

@@ -70,13 +70,15 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_certificate_tracing_matches_oracle(X, name):
+def test_certificate_tracing_matches_oracle(X, name, integration):
     w = CASES[name]()
-    ref = _oracle(w)
+    ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                   integration=integration)
     with X.Scene(w.obj, w.deformation) as s:
         img, st = X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
-                                    trace=True, stats=True)
+                                    trace=True, stats=True, integration=integration)
     assert np.max(np.abs(img - ref) / ref) <= REL_TOL
     assert st["evaluations"] > 0 and st["fp64_list_overflow"] == 0
 
@@ -193,3 +195,20 @@ def test_proposal_speed_against_plain_and_without_network(X, gyroid_trained):
     a, b, c = (o.cpu().numpy() for o in outs)
     assert np.max(np.abs(b - a) / a) <= 2 * REL_TOL
     assert np.max(np.abs(c - a) / a) <= 2 * REL_TOL
+
+
+def test_certificate_tracing_options(X):
+    # multiplier and flat field, device output, both integrators
+    import torch
+    w = W.reduced(W.gyroid_sigmoid(), 40, 2)
+    for integration in ("simple", "hierarchical"):
+        ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                       density_multiplier=1.7, flat_field=0.3, integration=integration)
+        with X.Scene(w.obj, w.deformation) as s:
+            out = torch.empty(len(w.angles) * w.res * w.res, device="cuda", dtype=torch.float32)
+            X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                              density_multiplier=1.7, flat_field=0.3, trace=True,
+                              integration=integration, out=out)
+            torch.cuda.synchronize()
+            img = out.cpu().numpy().reshape(ref.shape)
+        assert np.max(np.abs(img - ref) / ref) <= REL_TOL

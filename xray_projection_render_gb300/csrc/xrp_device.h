@@ -1521,9 +1521,59 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
     return acc.s - acc.c;
 }
 
-// One pixel by certificate tracing (simple integrator), FP64 for undecided
-// samples in place.
-template <int DEPTH, bool DEFS>
+// Certificate tracing of the hierarchical integrator (main.go:159-199):
+// coarse samples k0..k1 (right ends, spacing DS).  A coarse sample whose
+// zero-ness differs from its predecessor's is refined over its fine samples
+// exactly as march_hier does; the coarse samples a certificate covers share
+// the evaluated density, so none of them flips and each adds rho*DS.
+// `unc(index, fine)` gives the value of an undecided coarse (fine = false,
+// index into s64) or fine (fine = true, index into f64) sample.  Returns
+// sum(w * rho) with w in {DS, DS/10}.
+template <int DEPTH, bool DEFS, class Unc>
+XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
+                            unsigned& evals) {
+    KahanF acc;
+    const float step = L.ds32 * 1.00001f;
+    bool prev_zero = true;  // coarse samples before k0 are outside the support
+    int k = k0;
+    while (k <= k1) {
+        const float tk = lattice_t(L, k);
+        float m;
+        float rho = dens_margin32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tk, ray.pc[0]),
+                                               fmaf(ray.d32[1], tk, ray.pc[1]),
+                                               fmaf(ray.d32[2], tk, ray.pc[2]), m);
+        evals++;
+        int jmp = 0;
+        if (isunc(rho)) {
+            rho = unc(k, false);
+        } else {
+            jmp = (int)fminf(floorf(m / step), (float)(k1 - k));
+        }
+        const bool zero = (rho == 0.0f);
+        if (zero != prev_zero) {
+            const int f0 = L.fstart[k], f1 = L.fstart[k + 1];
+            for (int q = f0; q < f1; q++) {
+                const float tf = L.ft32[q];
+                float rf = density32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tf, ray.pc[0]),
+                                                  fmaf(ray.d32[1], tf, ray.pc[1]),
+                                                  fmaf(ray.d32[2], tf, ray.pc[2]));
+                evals++;
+                if (isunc(rf)) rf = unc(q, true);
+                acc.add(rf * L.dsf32);
+            }
+            acc.add(rho * L.dsf32);
+        } else {
+            acc.add(rho * L.ds32);
+        }
+        if (jmp > 0) acc.add(rho * L.ds32 * (float)jmp);
+        prev_zero = zero;
+        k += jmp + 1;
+    }
+    return acc.s - acc.c;
+}
+
+// One pixel by certificate tracing, FP64 for undecided samples in place.
+template <bool HIER, int DEPTH, bool DEFS>
 XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P, const ViewDev& V,
                          int i, int j, unsigned& evals) {
     Ray r;
@@ -1537,11 +1587,21 @@ XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams
     int k0, k1;
     float acc = 0.0f;
     if (sample_range(L, t0, t1, L.K, k0, k1)) {
-        acc = trace_sum<DEPTH, DEFS>(
-            S, L, r, k0, k1,
-            [&](int k) { return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[k]); }, evals);
+        if constexpr (HIER) {
+            acc = trace_sum_hier<DEPTH, DEFS>(
+                S, L, r, k0, k1,
+                [&](int q, bool fine) {
+                    return (float)sample64_pixel(S, V, P.xs, i, j, fine ? L.f64[q] : L.s64[q]);
+                },
+                evals);
+        } else {
+            acc = trace_sum<DEPTH, DEFS>(
+                S, L, r, k0, k1,
+                [&](int k) { return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[k]); }, evals);
+        }
     }
-    float T = fmaf(P.density_multiplier * L.ds32, acc, P.flat_field);
+    float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+    float T = fmaf(w, acc, P.flat_field);
     return expf(-T);
 }
 

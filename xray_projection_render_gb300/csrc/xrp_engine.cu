@@ -1077,7 +1077,6 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
     const bool hier = oo.integration == XRP_INTEGRATE_HIERARCHICAL;
     const bool trace = (oo.flags & XRP_FLAG_TRACE) != 0;
-    if (trace && hier) return fail(2, "certificate tracing needs the simple integrator");
     const int kdepth = depth == 0 ? 0 : kMaxDepth;
     if ((e = batch_blocks_per_sm(kdepth, defs, hier, trace, &occ)) != cudaSuccess)
         return cuda_fail(7, "batch occupancy", e);
@@ -1234,8 +1233,8 @@ uint64_t splitmix(uint64_t& s) {
 double unit_rand(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
 
 bool proposal_scene_ok(const xrp_scene* s, const xrp_render_opts* o, std::string& why) {
-    if (o->integration != XRP_INTEGRATE_SIMPLE) {
-        why = "the proposal march supports the simple integrator only";
+    if (o->integration != XRP_INTEGRATE_SIMPLE && !(o->flags & XRP_FLAG_TRACE)) {
+        why = "the segment march supports the simple integrator only (certificate tracing both)";
         return false;
     }
     for (const HNode& n : s->hs.nodes)

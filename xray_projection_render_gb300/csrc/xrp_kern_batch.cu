@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 3 : XRP_SCENE_MIN_
             float val;
             if constexpr (TRACE) {
                 unsigned ev = 0;
-                val = trace_pixel<DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, ev);
+                val = trace_pixel<HIER, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, ev);
             } else {
                 RayStats st{0, 0};
                 val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);
@@ -99,7 +99,8 @@ static cudaError_t launch_batch_t(const BatchLaunch& b, cudaStream_t st) {
 
 template <int DEPTH, bool DEFS>
 static cudaError_t launch_batch_d(const BatchLaunch& b, cudaStream_t st) {
-    if (b.trace) return launch_batch_t<false, DEPTH, DEFS, true>(b, st);
+    if (b.trace) return b.hier ? launch_batch_t<true, DEPTH, DEFS, true>(b, st)
+                               : launch_batch_t<false, DEPTH, DEFS, true>(b, st);
     if (b.hier) return launch_batch_t<true, DEPTH, DEFS, false>(b, st);
     return launch_batch_t<false, DEPTH, DEFS, false>(b, st);
 }
@@ -112,7 +113,7 @@ cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st) {
 
 template <int DEPTH, bool DEFS>
 static const void* batch_fn(bool hier, bool trace) {
-    if (trace) return (const void*)k_batch<false, DEPTH, DEFS, true>;
+    if (trace) return hier ? (const void*)k_batch<true, DEPTH, DEFS, true> : (const void*)k_batch<false, DEPTH, DEFS, true>;
     if (hier) return (const void*)k_batch<true, DEPTH, DEFS, false>;
     return (const void*)k_batch<false, DEPTH, DEFS, false>;
 }

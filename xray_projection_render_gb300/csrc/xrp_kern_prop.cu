@@ -12,7 +12,10 @@ static cudaError_t trace_t(const Prepared& pr, int view0, int nviews, const Prop
     long blocks = (long)nviews * tpr * tpr;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
-    k_trace<DEPTH, DEFS><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, nviews, Q, dout);
+    if (pr.L.hierarchical)
+        k_trace<DEPTH, DEFS, true><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, nviews, Q, dout);
+    else
+        k_trace<DEPTH, DEFS, false><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, nviews, Q, dout);
     return cudaGetLastError();
 }
 

@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // any boundary the jumps are long; approaching one they shrink
 // geometrically; next to it the march steps sample by sample.  Samples FP32
 // cannot decide go to the FP64 list like the other march modes.
-template <int DEPTH, bool DEFS>
+template <int DEPTH, bool DEFS, bool HIER>
 __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
@@ -466,16 +466,32 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
         int k0, k1;
         float sum = 0.0f;
         if (sample_range(L, t0, t1, L.K, k0, k1)) {
-            sum = trace_sum<DEPTH, DEFS>(
-                S, L, ray, k0, k1,
-                [&](int k) {
-                    unsigned slot = atomicAdd(Q.fb_count, 1u);
-                    if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);
-                    return 0.0f;
-                },
-                evals);
+            if constexpr (HIER) {
+                // a coarse sample's value decides refinement: FP64 in place;
+                // fine samples only add, so they go to the list (high bit)
+                const ViewDev& V = views[view0 + v];
+                sum = trace_sum_hier<DEPTH, DEFS>(
+                    S, L, ray, k0, k1,
+                    [&](int q, bool fine) {
+                        if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
+                        unsigned slot = atomicAdd(Q.fb_count, 1u);
+                        if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)q | 0x80000000u);
+                        return 0.0f;
+                    },
+                    evals);
+            } else {
+                sum = trace_sum<DEPTH, DEFS>(
+                    S, L, ray, k0, k1,
+                    [&](int k) {
+                        unsigned slot = atomicAdd(Q.fb_count, 1u);
+                        if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);
+                        return 0.0f;
+                    },
+                    evals);
+            }
         }
-        out[r] = fmaf(P.density_multiplier * L.ds32, sum, P.flat_field);
+        const float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+        out[r] = fmaf(w, sum, P.flat_field);
     }
     if (Q.stats) {
         unsigned s = __reduce_add_sync(0xffffffffu, evals);
@@ -497,14 +513,17 @@ __global__ void __launch_bounds__(256)
     if (blockIdx.x == 0 && threadIdx.x == 0 && total > fb_cap) atomicOr(overflow, 1u);
     const long img = (long)P.res * P.res;
     const float w = P.density_multiplier * L.ds32;
+    const float wf = P.density_multiplier * L.dsf32;  // fine samples (hierarchical)
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const uint2 e = fb[q];
         const long r = e.x;
         const int v = view0 + (int)(r / img);
         const long pix = r % img;
         const int i = (int)(pix / P.res), j = (int)(pix % P.res);
-        double rho = sample64_pixel_inl(S, views[v], P.xs, i, j, L.s64[e.y]);
-        atomicAdd(&T[r], w * (float)rho);
+        const bool fine = (e.y & 0x80000000u) != 0;
+        const unsigned idx = e.y & 0x7fffffffu;
+        double rho = sample64_pixel_inl(S, views[v], P.xs, i, j, fine ? L.f64[idx] : L.s64[idx]);
+        atomicAdd(&T[r], (fine ? wf : w) * (float)rho);
     }
     if (stats && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[kStatFallbacks], (unsigned long long)n);
 }

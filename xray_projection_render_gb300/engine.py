@@ -305,16 +305,17 @@ class Proposal:
 
 def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resolution, ds, R=4.0,
                     fov=40.0, flat_field=0.0, density_multiplier=1.0, segment=0, refine=True,
-                    trace=False, out=None, stream=None, stats=False):
+                    trace=False, integration="simple", out=None, stream=None, stats=False):
     """Render with the proposal march (xrp_render_proposal).  ``proposal``
     None: no network (every candidate refined, or integrated densely with
-    ``refine=False``; ``trace=True``: per-ray certificate tracing).  Host path
+    ``refine=False``; ``trace=True``: per-ray certificate tracing, either
+    ``integration``; the segment march needs "simple").  Host path
     returns a float32 array [views, res, res]
     (with ``stats``: (images, dict)); a contiguous float32 CUDA tensor as
     ``out`` selects the device path."""
     L = _lib.load()
     cams, n = cameras_from_angles(angles, R, fov)
-    o = _opts(resolution, ds, R, flat_field, density_multiplier, "simple", stats)
+    o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats)
     if not refine:
         o.flags |= _lib.XRP_FLAG_NO_REFINE
     if trace:
