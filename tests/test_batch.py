@@ -102,3 +102,22 @@ def test_batch_with_certificate_tracing(X):
     finally:
         for s in scenes:
             s.close()
+
+
+def test_batch_with_empty_and_outside_scenes(X):
+    objs = [{"type": "object_collection", "objects": []},
+            {"type": "sphere", "center": [9.0, 9.0, 9.0], "radius": 0.5, "rho": 1.0},
+            W.cube_minus_sphere_cylinder(8).obj]
+    angles = [(0.0, 90.0), (40.0, 60.0)]
+    scenes = [X.Scene(o) for o in objs]
+    try:
+        for trace in (False, True):
+            with X.Batch([(s, angles, r) for s, r in zip(scenes, (16, 20, 24))], ds=0.01,
+                         flat_field=0.25, trace=trace) as b:
+                b.render()
+                for k, (o, r) in enumerate(zip(objs, (16, 20, 24))):
+                    ref = O.render(O.Scene(o), angles, r, 0.01, flat_field=0.25)
+                    assert np.max(np.abs(b.item(k) - ref) / ref) <= REL_TOL
+    finally:
+        for s in scenes:
+            s.close()

@@ -212,3 +212,29 @@ def test_certificate_tracing_options(X):
             torch.cuda.synchronize()
             img = out.cpu().numpy().reshape(ref.shape)
         assert np.max(np.abs(img - ref) / ref) <= REL_TOL
+
+
+@pytest.mark.parametrize("obj", [
+    {"type": "object_collection", "objects": []},
+    {"type": "sphere", "center": [9.0, 9.0, 9.0], "radius": 0.5, "rho": 1.0},
+    {"type": "sphere", "center": [0.0, 0.0, 0.0], "radius": 0.5, "rho": 0.0},
+], ids=["empty", "outside", "zero_rho"])
+def test_tracing_and_march_on_empty_support(X, obj):
+    # nothing to integrate: every pixel is exp(-flat_field), as the oracle says
+    angles = [(0.0, 90.0), (40.0, 60.0)]
+    ref = O.render(O.Scene(obj), angles, 24, 0.01, flat_field=0.25)
+    assert np.allclose(ref, np.exp(-0.25))
+    with X.Scene(obj) as s:
+        for kw in (dict(trace=True), dict(refine=False, segment=32), dict(refine=True)):
+            img = X.render_proposal(s, None, angles, resolution=24, ds=0.01, flat_field=0.25, **kw)
+            assert np.max(np.abs(img - ref) / ref) <= REL_TOL, kw
+
+
+def test_tracing_coarse_step(X):
+    # ds comparable to the object: few samples, long certificate jumps clamp at k1
+    w = W.cube_minus_sphere_cylinder(32)
+    for ds in (0.05, 0.2):
+        ref = O.render(O.Scene(w.obj), w.angles, 32, ds)
+        with X.Scene(w.obj) as s:
+            img = X.render_proposal(s, None, w.angles, resolution=32, ds=ds, trace=True)
+        assert np.max(np.abs(img - ref) / ref) <= REL_TOL

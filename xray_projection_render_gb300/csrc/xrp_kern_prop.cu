@@ -1,6 +1,8 @@
 // xrp_kern_prop.cu -- the proposal march's rendering kernels
 // (xrp_proposal.cuh), specialised like the general-scene kernel.
 #define XRP_PROP_RENDER_KERNELS
+#include <algorithm>
+
 #include "xrp_launch.h"
 
 namespace xrp {
@@ -44,14 +46,16 @@ cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const 
     cudaError_t e = cudaMemsetAsync(Q.fb_count, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     if ((e = march(pr, view0, nviews, Q, dout, st)) != cudaSuccess) return e;
-    static int fb_grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    static std::atomic<int> fb_grid[kMaxDevices];
     int dev = 0;
     cudaGetDevice(&dev);
-    int& g = fb_grid[dev & 7];
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    int g = fb_grid[dev].load(std::memory_order_relaxed);
     if (!g) {
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        g = sms * 4;
+        g = std::max(1, sms * 4);
+        fb_grid[dev].store(g, std::memory_order_relaxed);
     }
     k_prop_fallback<<<g, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, Q.fb, Q.fb_count, Q.fb_cap,
                                       dout, Q.stats, Q.fb_overflow);

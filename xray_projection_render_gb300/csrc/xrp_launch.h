@@ -7,6 +7,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "xrp_device.h"
 #include "xrp_proposal.cuh"
 
@@ -124,6 +126,8 @@ cudaError_t mlp_adam_launch(cudaStream_t st, float* params, float* grad, float* 
 cudaError_t mlp_logits_launch(cudaStream_t st, const float* params, const __nv_bfloat16* X, int rows,
                               float* logits);
 
+constexpr int kMaxDevices = 64;  // per-device launch caches
+
 // Grid of a persistent proposal launch: resident blocks x SMs (cached per
 // kernel and device).
 template <class K>
@@ -144,14 +148,16 @@ template <int DEPTH, bool DEFS, int MODE>
 cudaError_t launch_prop_t(const Prepared& pr, int view0, int nviews, const PropParams& Q,
                           float* dout, cudaStream_t st) {
     auto kern = k_propose<DEPTH, DEFS, MODE>;
-    static int grid_cache[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per device (first 8)
+    static std::atomic<int> grid_cache[kMaxDevices];  // per device; 0 until measured
     const size_t smem = sizeof(PropShared);
     int dev = 0;
     cudaGetDevice(&dev);
-    int& gmax = grid_cache[dev & 7];
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    int gmax = grid_cache[dev].load(std::memory_order_relaxed);
     if (!gmax) {
         cudaError_t e = persistent_grid(kern, smem, 32 * kPropWarps, &gmax);
         if (e != cudaSuccess) return e;
+        grid_cache[dev].store(gmax, std::memory_order_relaxed);
     }
     long rays = Q.rays ? (long)Q.nrays : (long)nviews * pr.P.res * pr.P.res;
     long need = (rays + 32 * kPropWarps - 1) / (32 * kPropWarps);  // 32 rays per warp batch
