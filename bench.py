@@ -263,7 +263,7 @@ def make_workload(name, W, views, res):
 
 
 def bench_batched(args):
-    """Config 4: 64 seeded scenes (1-200 primitives, resolution 256/512/1024,
+    """The batch of 64 seeded scenes (1-200 primitives, resolution 256/512/1024,
     8-128 views, ds 0.005) in one persistent launch per step, replayed from
     the CUDA graph xrp_batch_create captured (autotuned tile shape and grid)."""
     import torch

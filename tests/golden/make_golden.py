@@ -22,10 +22,10 @@ from xray_projection_render_gb300 import workloads as W  # noqa: E402
 
 def scene_cases():
     out = {
-        "config1_cube_minus_sphere_cylinder": W.cube_minus_sphere_cylinder(48),
-        "config3_deformed_lattice": W.reduced(W.deformed_lattice(), 40, 2),
-        "config5_gyroid_sigmoid": W.reduced(W.gyroid_sigmoid(), 40, 2),
-        "config4_batched_scene0": W.reduced(W.batched_scenes(1)[0], 40, 2),
+        "scene_cube_minus_sphere_cylinder": W.cube_minus_sphere_cylinder(48),
+        "scene_deformed_lattice": W.reduced(W.deformed_lattice(), 40, 2),
+        "scene_gyroid_sigmoid": W.reduced(W.gyroid_sigmoid(), 40, 2),
+        "scene_batched_scene0": W.reduced(W.batched_scenes(1)[0], 40, 2),
     }
     return out
 
@@ -59,7 +59,7 @@ def main():
                                 angles=np.asarray(w.angles), res=w.res, ds=w.ds, R=w.R, fov=w.fov,
                                 integration=integ)
     vol = W.gaussian_blob_volume(24, 8, seed=2)
-    for name, (v, ds) in dict(cuda_test_volumes(), config2_voxel_blobs=(vol, 2.0 / 24 / 2)).items():
+    for name, (v, ds) in dict(cuda_test_volumes(), voxel_blobs=(vol, 2.0 / 24 / 2)).items():
         angles = [(0.0, 90.0), (75.0, 90.0)]
         cams = O.xray_camera_params(angles, 4.0, 40.0)
         img = O.render_volume_abi(v, cams, 32, np.float32(ds))

@@ -45,7 +45,7 @@ def check_scene(obj, deformation=None, n=1500, per=6, seed=0, lo=-1.1, hi=1.1, d
     return certified, n
 
 
-def test_config1_collection():
+def test_cube_minus_sphere_cylinder_collection():
     c, n = check_scene(W.cube_minus_sphere_cylinder(8).obj)
     assert c > n // 2
 

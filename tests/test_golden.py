@@ -16,7 +16,7 @@ GOLD = os.path.join(HERE, "golden")
 sys.path.insert(0, os.path.join(HERE, "hostsim"))
 
 REL_TOL = 1e-5
-SCENES = sorted(f for f in glob.glob(os.path.join(GOLD, "config*_*.npz")) if "_abi" not in f)
+SCENES = sorted(glob.glob(os.path.join(GOLD, "scene_*.npz")))
 ABI = sorted(glob.glob(os.path.join(GOLD, "*_abi.npz")))
 
 

@@ -56,7 +56,7 @@ def _render_both(X, w, integration="simple", stats=False, **kw):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-def test_config1_full_size(X, integration):
+def test_cube_minus_sphere_cylinder_full_size(X, integration):
     w = W().cube_minus_sphere_cylinder(512)
     (got, ns, nf), ref = _render_both(X, w, integration, stats=True)
     _compare(got, ref)

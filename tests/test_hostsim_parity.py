@@ -43,7 +43,7 @@ def check(w, integration="simple", nrays=2500, seed=0, **kw):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-def test_config1(integration):
+def test_cube_minus_sphere_cylinder(integration):
     st = check(W.cube_minus_sphere_cylinder(256), integration)
     assert st[1] < 0.01 * st[0]
 
@@ -119,7 +119,7 @@ def test_greedy_sum_and_cancellation():
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-@pytest.mark.parametrize("name", ["gyroid", "lattice", "config1", "batched", "coll_defs"])
+@pytest.mark.parametrize("name", ["gyroid", "lattice", "cube", "batched", "coll_defs"])
 def test_certificate_tracing(name, integration):
     """Certificate tracing (trace_pixel, the algorithm of k_trace and the
     tracing batch kernel), both integrators, against the FP64 oracle on the
@@ -128,7 +128,7 @@ def test_certificate_tracing(name, integration):
         w = W.reduced(W.gyroid_sigmoid(), 128, 4)
     elif name == "lattice":
         w = W.reduced(W.deformed_lattice(), 128, 3)
-    elif name == "config1":
+    elif name == "cube":
         w = W.cube_minus_sphere_cylinder(128)
     elif name == "batched":
         w = W.reduced(W.batched_scenes(3)[2], 128, 3)

@@ -36,7 +36,7 @@ class Workload:
 
 
 def cube_minus_sphere_cylinder(res=512) -> Workload:
-    """Config 1: cube (side 1, rho 1) minus a sphere (r 0.3) and a cylinder
+    """Cube (side 1, rho 1) minus a sphere (r 0.3) and a cylinder
     (r 0.2, z from -0.6 to 0.6); one view at azimuth 0, polar 90; ds 0.005."""
     obj = {"type": "object_collection", "objects": [
         {"type": "cube", "side": 1.0, "center": [0.0, 0.0, 0.0], "rho": 1.0},
@@ -64,7 +64,7 @@ def gaussian_blob_volume(n=256, blobs=64, seed=2) -> np.ndarray:
 
 
 def voxel_blobs(res=1024, views=180, n=256, seed=2) -> Workload:
-    """Config 2: 256^3 FP32 grid of 64 Gaussians, 180 views evenly spaced in
+    """Voxel grid: 256^3 FP32 grid of 64 Gaussians, 180 views evenly spaced in
     azimuth (0, 2, ..., 358) at polar 90, 1024^2, ds = half a voxel."""
     vol = gaussian_blob_volume(n, 64, seed)
     angles = [(360.0 * k / views, 90.0) for k in range(views)]
@@ -90,7 +90,7 @@ def lattice_unit_cell(a=0.2, r=0.03):
 
 
 def deformed_lattice(res=1024, views=360, seed=3) -> Workload:
-    """Config 3: 16-cylinder cell tessellated 10x10x10 over [-1,1]^3 with 5 %
+    """Deformed lattice: 16-cylinder cell tessellated 10x10x10 over [-1,1]^3 with 5 %
     axial (zz) strain; seeded random azimuth U[0,360) and polar U[30,150]."""
     rng = np.random.default_rng(seed)
     az = rng.uniform(0.0, 360.0, size=views)
@@ -133,7 +133,7 @@ def random_scene(rng) -> dict:
 
 
 def batched_scenes(count=64, seed=4) -> list:
-    """Config 4: 64 collections of 1-200 random primitives with uneven
+    """Batch: 64 collections of 1-200 random primitives with uneven
     resolutions {256, 512, 1024} and 8-128 evenly spaced views each; ds 0.005."""
     rng = np.random.default_rng(seed)
     out = []
@@ -147,7 +147,7 @@ def batched_scenes(count=64, seed=4) -> list:
 
 
 def gyroid_sigmoid(res=2048, views=720) -> Workload:
-    """Config 5: gyroid (scale 8, thickness 0.1) tessellated with outer and
+    """Gyroid (scale 8, thickness 0.1) tessellated with outer and
     unit-cell bounds [-1,1]^3, sigmoid deformation (A 0.1, L 0.2, along z);
     720 views evenly spaced in azimuth; 2048^2; ds 0.001."""
     obj = {"type": "tessellated_obj_coll",
@@ -168,13 +168,13 @@ def reduced(w: Workload, res: int, views: int | None = None) -> Workload:
     return dataclasses.replace(w, res=res, angles=list(ang))
 
 
-CONFIGS = {
-    1: cube_minus_sphere_cylinder,
-    2: voxel_blobs,
-    3: deformed_lattice,
-    5: gyroid_sigmoid,
+WORKLOADS = {
+    "cube_minus_sphere_cylinder": cube_minus_sphere_cylinder,
+    "voxel_blobs": voxel_blobs,
+    "deformed_lattice": deformed_lattice,
+    "gyroid_sigmoid": gyroid_sigmoid,
 }
 
 __all__ = ["Workload", "cube_minus_sphere_cylinder", "gaussian_blob_volume", "voxel_blobs",
            "lattice_unit_cell", "deformed_lattice", "random_scene", "batched_scenes",
-           "gyroid_sigmoid", "reduced", "CONFIGS", "math"]
+           "gyroid_sigmoid", "reduced", "WORKLOADS", "math"]
