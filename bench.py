@@ -56,8 +56,10 @@ def parse():
                         "device-side image finishing of 64 images of 1024^2, or the volume "
                         "export of the deformed lattice at 256^3")
     p.add_argument("--scenes", type=int, default=64, help="batched: number of scenes")
-    p.add_argument("--march", default="plain", choices=["plain", "trace", "certificate", "proposal"],
-                   help="analytic scenes: plain integrator, per-ray certificate tracing, "
+    p.add_argument("--march", default="plain",
+                   choices=["plain", "trace", "ball", "certificate", "proposal"],
+                   help="analytic scenes: plain integrator, per-ray certificate tracing (ray bounds "
+                        "for affine deformation chains), tracing with ball certificates only, "
                         "segment march with certificates and no network, or the trained proposal")
     p.add_argument("--views", type=int, default=0, help="view count (0: the workload's)")
     p.add_argument("--res", type=int, default=0, help="resolution (0: the workload's)")
@@ -286,7 +288,7 @@ def bench_batched(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)
-    trace = args.march == "trace"
+    trace = _trace_mode(args)
     b = X.Batch(items, ds=ds, autotune=True, trace=trace)
     info = b.info()
     for _ in range(args.warmup):
@@ -359,7 +361,8 @@ def bench_batched(args):
                    "l2": "flushed before every timed step (256 MiB write); output > L2",
                    "tile": f'{info["tile_w"]}x{info["tile_h"]}', "blocks_per_sm": info["blocks_per_sm"],
                    "autotune_ms": info["tune_ms"], "graph": "one CUDA graph replay per step",
-                   "march": "certificate tracing" if trace else "plain",
+                   "march": {"trace": "certificate tracing (ray bounds: every scene is affine)",
+                             "ball": "certificate tracing (ball certificates)"}.get(args.march, "plain"),
                    "per_scene_calls_mrays": info["rays"] / t_seq / 1e6,
                    "parallelism": f"scenes k mod {world}"},
         "e2e": {"value": rays / t_e2e / 1e6 if e2e_times else None, "unit": "Mrays/s",
@@ -459,6 +462,11 @@ def cpu_baseline_multi(ws, seconds):
     return out
 
 
+def _trace_mode(args):
+    """render_proposal / Batch `trace` argument of a --march choice."""
+    return {"trace": True, "ball": "ball"}.get(args.march, False)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -503,7 +511,7 @@ def main():
         else:
             X.render_proposal(scene, prop, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov,
                               segment=64, refine=args.march == "proposal",
-                              trace=args.march == "trace", out=out, stream=stream)
+                              trace=_trace_mode(args), out=out, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -518,7 +526,7 @@ def main():
         # per evaluation, or one density per dense sample)
         _, pst = X.render_proposal(scene, prop, my_angles[:nstat], resolution=res, ds=w.ds, R=w.R,
                                    fov=w.fov, segment=64, refine=args.march == "proposal",
-                                   trace=args.march == "trace", stats=True)
+                                   trace=_trace_mode(args), stats=True)
         evals_step = (pst["evaluations"] + pst["dense_samples"]) * n_my / nstat
     if world > 1:
         torch.distributed.barrier()
@@ -562,7 +570,7 @@ def main():
                 else:  # the network trained on the resident scene applies to this copy
                     X.render_proposal(s2, prop, my_angles, resolution=res, ds=w.ds, R=w.R,
                                       fov=w.fov, segment=64, refine=args.march == "proposal",
-                                      trace=args.march == "trace", out=out_host)
+                                      trace=_trace_mode(args), out=out_host)
     if not args.no_e2e:
         e2e_call()  # warm
         for _ in range(max(1, min(args.steps, 3))):

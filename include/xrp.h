@@ -115,7 +115,8 @@ enum {
     XRP_FLAG_STATS = 1,        /* count evaluated and FP64-re-evaluated samples */
     XRP_FLAG_VOLUME_LOADS = 2, /* voxel-grid roots: per-tap loads instead of texture gathers */
     XRP_FLAG_NO_REFINE = 4,    /* proposal march: no certificate refinement of segments */
-    XRP_FLAG_TRACE = 8         /* per-ray certificate tracing (proposal march without network, batches) */
+    XRP_FLAG_TRACE = 8,        /* per-ray certificate tracing (proposal march without network, batches) */
+    XRP_FLAG_BALL = 16         /* tracing: ball certificates only, even for affine deformation chains */
 };
 
 /* Per-call options: the globals and flags of the reference CLI
@@ -224,7 +225,8 @@ XRP_API int xrp_finish_images(const float* d_images, int num_views, int res, int
  * those of xrp_render for each item.  All items share the options (ds, R,
  * integration, flat field, multiplier; opts->resolution is ignored); with
  * XRP_FLAG_TRACE in opts->flags every ray is rendered by certificate
- * tracing (either integrator), which gives the same results.
+ * tracing (either integrator), which gives the same results (ray bounds
+ * when every scene's deformation chain is affine, unless XRP_FLAG_BALL).
  */
 typedef struct {
     xrp_scene* scene;
@@ -316,7 +318,11 @@ XRP_API void xrp_proposal_destroy(xrp_proposal* p);
  * is traced on its own: at every evaluated sample the certificate radius
  * says how many following samples share its density, and the march jumps
  * past them (the hierarchical integrator still refines every coarse sample
- * whose zero-ness changes).  The device variant queues the work on `stream`
+ * whose zero-ness changes).  When the deformation chain is affine (linear,
+ * affine, rigid or none) the certificate is a ray bound, the distance along
+ * the ray to the next place where the density can change (the samples lie
+ * on a line in object coordinates); otherwise, or with XRP_FLAG_BALL, it is
+ * the radius of a ball around the sample.  The device variant queues the work on `stream`
  * and then waits for it (it reads back whether the list of samples left to
  * FP64 overflowed, in which case the plain integrator renders the call). */
 XRP_API int xrp_render_proposal(xrp_scene* scene, const xrp_proposal* proposal, int segment,

@@ -43,7 +43,7 @@ def lib():
                                 D, P, P, I, P, L_, I, I, ctypes.c_char_p, I]
         L.hs_margin.restype = I
         L.hs_margin.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, L_, D, D, D, P, P, P, P,
-                                ctypes.c_char_p, I]
+                                P, P, P, P, ctypes.c_char_p, I]
         _lib = L
     return _lib
 
@@ -58,10 +58,31 @@ def margin(obj, points, *, deformation=None, R=4.0, fov=40.0, ds=0.01, fused=Fal
     rc = lib().hs_margin(json.dumps(obj).encode(),
                          json.dumps(deformation).encode() if deformation else None,
                          pts.ctypes.data, n, R, fov, ds, rho.ctypes.data, m.ctypes.data,
-                         rho2.ctypes.data, m2.ctypes.data, err, 512)
+                         rho2.ctypes.data, m2.ctypes.data, None, None, None, None, err, 512)
     if rc != 0:
         raise ValueError(err.value.decode())
     return (rho, m, rho2, m2) if fused else (rho, m)
+
+
+def ray_bound(obj, points, dirs, *, deformation=None, R=4.0, fov=40.0, ds=0.01):
+    """Ray evaluator at points [n,3] along world directions [n,3]: (density,
+    ray bound t, affine).  Every sample at parameter s in [0, t] must have
+    the density of the point; ``affine`` False means the chain is not affine
+    (no ray certificates; density and t are then not computed)."""
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    d = np.ascontiguousarray(dirs, dtype=np.float64).reshape(-1, 3)
+    n = pts.shape[0]
+    rho, m, rho2, m2, rho3, t = (np.zeros(n, np.float32) for _ in range(6))
+    aff = ctypes.c_int(0)
+    err = ctypes.create_string_buffer(512)
+    rc = lib().hs_margin(json.dumps(obj).encode(),
+                         json.dumps(deformation).encode() if deformation else None,
+                         pts.ctypes.data, n, R, fov, ds, rho.ctypes.data, m.ctypes.data,
+                         rho2.ctypes.data, m2.ctypes.data, d.ctypes.data, rho3.ctypes.data,
+                         t.ctypes.data, ctypes.byref(aff), err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return rho3, t, bool(aff.value)
 
 
 def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integration="simple",

@@ -77,8 +77,12 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
                 bool hier = integration == 1;
                 if (trace) {
                     unsigned ev = 0;
-                    val = hier ? trace_pixel<true, kMaxDepth, true>(S, L, P, views[v], i, j, ev)
-                               : trace_pixel<false, kMaxDepth, true>(S, L, P, views[v], i, j, ev);
+                    if (S.affine)
+                        val = hier ? trace_pixel<true, kMaxDepth, true, true>(S, L, P, views[v], i, j, ev)
+                                   : trace_pixel<false, kMaxDepth, true, true>(S, L, P, views[v], i, j, ev);
+                    else
+                        val = hier ? trace_pixel<true, kMaxDepth, true, false>(S, L, P, views[v], i, j, ev)
+                                   : trace_pixel<false, kMaxDepth, true, false>(S, L, P, views[v], i, j, ev);
                     st.samples = ev;
                 } else if (hier)
                     val = vf ? render_pixel<true, true>(S, L, P, views[v], i, j, st)
@@ -115,11 +119,13 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
 // Density (FP32 guarded; NaN when uncertain) and distance certificate
 // (margin32, world units) at FP64 points rounded to FP32, for the soundness
 // tests of the certificates; also the fused evaluator's pair, which must be
-// identical.  R and fov enter the error analysis as for a
+// identical, and with `dirs` (affine chains) the ray evaluator's density and
+// ray bound along each direction.  R and fov enter the error analysis as for a
 // render with those cameras.
 extern "C" __attribute__((visibility("default"))) int hs_margin(
     const char* obj_json, const char* def_json, const double* pts, long n, double R, double fov,
-    double ds, float* rho_out, float* m_out, float* rho2_out, float* m2_out, char* err, int errlen) {
+    double ds, float* rho_out, float* m_out, float* rho2_out, float* m2_out, const double* dirs,
+    float* rho3_out, float* t_out, int* affine_out, char* err, int errlen) {
     try {
         HostScene hs = load_scene(obj_json, def_json, {});
         HostPrepared hp = prepare_host(hs, 8, 0, ds, R, 0.0, 1.0, fov);
@@ -137,7 +143,13 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
             rho_out[q] = density32<kMaxDepth, true>(S, x, y, z);
             m_out[q] = margin32<kMaxDepth, true>(S, x, y, z);
             rho2_out[q] = dens_margin32<kMaxDepth, true>(S, x, y, z, m2_out[q]);
+            if (dirs && S.affine) {
+                float d[3] = {(float)dirs[3 * q], (float)dirs[3 * q + 1], (float)dirs[3 * q + 2]};
+                RayDir u = ray_dir32(S, d);
+                rho3_out[q] = dens_ray32<kMaxDepth, true>(S, x, y, z, u, t_out[q]);
+            }
         }
+        if (affine_out) *affine_out = S.affine;
         return 0;
     } catch (const std::exception& ex) {
         if (err && errlen > 0) {

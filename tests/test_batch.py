@@ -93,6 +93,17 @@ def test_batch_with_certificate_tracing(X):
             w = ws[4]
             ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, ds, R=w.R, fov=w.fov)
             assert np.max(np.abs(b.item(4) - ref) / ref) <= REL_TOL
+        # without the gyroid (sigmoid chain) every scene is affine: ray bounds
+        with X.Batch([(s, w.angles, w.res) for s, w in zip(scenes[:6], ws[:6])], ds=ds, trace=True) as br:
+            br.render()
+            for k, (s, w) in enumerate(zip(scenes[:6], ws[:6])):
+                single = X.render(s, w.angles, resolution=w.res, ds=ds)
+                assert np.max(np.abs(br.item(k) - single) / single) <= 2 * REL_TOL, w.name
+        with X.Batch([(s, w.angles, w.res) for s, w in zip(scenes, ws)], ds=ds, trace="ball") as bb:
+            bb.render()
+            for k, (s, w) in enumerate(zip(scenes, ws)):
+                single = X.render(s, w.angles, resolution=w.res, ds=ds)
+                assert np.max(np.abs(bb.item(k) - single) / single) <= 2 * REL_TOL, w.name
         with X.Batch([(s, w.angles, w.res) for s, w in zip(scenes, ws)], ds=ds, trace=True,
                      integration="hierarchical") as bh:
             bh.render()

@@ -97,3 +97,102 @@ def test_every_primitive_under_every_deformation():
     coll = {"type": "object_collection", "objects": prims}
     for d in defs:
         check_scene(coll, d, n=300, per=4)
+
+
+# ---------------------------------------------------------------------------
+# Ray certificates (affine chains): along a direction D the density must
+# stay that of the point for every ray parameter in [0, t].
+# ---------------------------------------------------------------------------
+
+def check_ray(obj, deformation=None, n=1200, per=8, seed=0, lo=-1.1, hi=1.1, ds=0.002, span=4.0):
+    rng = np.random.default_rng(seed)
+    P = rng.uniform(lo, hi, (n, 3))
+    D = rng.normal(size=(n, 3))
+    D /= np.linalg.norm(D, axis=1, keepdims=True)
+    rho, t, affine = hostsim.ray_bound(obj, P, D, deformation=deformation, ds=ds)
+    assert affine
+    # the ray evaluator decides exactly as the point evaluators
+    rho_pt, _ = hostsim.margin(obj, P, deformation=deformation, ds=ds)
+    assert np.array_equal(np.isnan(rho), np.isnan(rho_pt))
+    ok = ~np.isnan(rho)
+    assert np.array_equal(rho[ok], rho_pt[ok])
+    sc = O.Scene(obj, deformation)
+    certified, far = 0, 0
+    for k in range(n):
+        if not (t[k] > 0) or np.isnan(rho[k]):
+            continue
+        r0 = sc.density(*P[k])
+        assert np.float32(r0) == rho[k], (k, P[k], r0, rho[k])
+        tk = min(float(t[k]), span)
+        far += t[k] > span
+        taus = np.concatenate([[tk, 0.999 * tk, 0.5 * tk], rng.uniform(0, tk, per - 3)])
+        for tau in taus:
+            q = P[k] + D[k] * tau
+            assert sc.density(*q) == r0, (k, P[k], D[k], float(t[k]), tau)
+        certified += 1
+    return certified, far, n
+
+
+def test_ray_cube_minus_sphere_cylinder():
+    c, far, n = check_ray(W.cube_minus_sphere_cylinder(8).obj)
+    assert c > n // 2
+
+
+def test_ray_deformed_lattice():
+    w = W.deformed_lattice()
+    c, far, n = check_ray(w.obj, w.deformation, n=800)
+    assert c > n // 3
+
+
+@pytest.mark.parametrize("k", [0, 3, 7])
+def test_ray_batched_scene_with_candidate_lists(k):
+    w = W.batched_scenes(8)[k]
+    check_ray(w.obj, n=800, seed=k)
+
+
+def test_ray_every_primitive_under_affine_deformations():
+    prims = [
+        {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+        {"type": "box", "center": [0.0, 0.2, 0.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5},
+        {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+        {"type": "cylinder", "p0": [0.0, 0.0, -0.6], "p1": [0.0, 0.0, 0.6], "radius": 0.3},
+        {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+         "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9},
+        {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0},
+    ]
+    defs = [None,
+            {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]},
+            {"type": "rigid", "displacements": [0.05, -0.1, 0.02]},
+            {"type": "affine", "matrix": [[1.1, 0.0, 0.1], [0.0, 0.9, 0.0], [0.05, 0.0, 1.0]]}]
+    for p in prims:
+        for d in defs:
+            check_ray(p, d, n=250, per=6)
+    coll = {"type": "object_collection", "objects": prims}
+    for d in defs:
+        check_ray(coll, d, n=300, per=6)
+
+
+def test_ray_axis_aligned_directions():
+    # directions along the axes and along a cylinder axis: zero components,
+    # rays parallel to faces and to the axis
+    obj = {"type": "object_collection", "objects": [
+        {"type": "box", "center": [0.0, 0.0, 0.0], "sides": [0.6, 0.6, 0.6], "rho": 0.5},
+        {"type": "cylinder", "p0": [0.0, 0.0, -0.8], "p1": [0.0, 0.0, 0.8], "radius": 0.2}]}
+    rng = np.random.default_rng(5)
+    P = rng.uniform(-1, 1, (600, 3))
+    axes = np.eye(3)[rng.integers(0, 3, 600)] * rng.choice([-1.0, 1.0], (600, 1))
+    rho, t, _ = hostsim.ray_bound(obj, P, axes)
+    sc = O.Scene(obj)
+    for k in range(600):
+        if not (t[k] > 0) or np.isnan(rho[k]):
+            continue
+        r0 = sc.density(*P[k])
+        for tau in np.linspace(0, min(float(t[k]), 4.0), 9):
+            assert sc.density(*(P[k] + axes[k] * tau)) == r0
+
+
+def test_non_affine_chain_has_no_ray_certificates():
+    w = W.gyroid_sigmoid()
+    _, _, affine = hostsim.ray_bound(w.obj, np.zeros((1, 3)), np.array([[1.0, 0, 0]]),
+                                     deformation=w.deformation)
+    assert not affine

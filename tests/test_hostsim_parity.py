@@ -119,7 +119,7 @@ def test_greedy_sum_and_cancellation():
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-@pytest.mark.parametrize("name", ["gyroid", "lattice", "cube", "batched", "coll_defs"])
+@pytest.mark.parametrize("name", ["gyroid", "lattice", "cube", "batched", "coll_defs", "coll_affine"])
 def test_certificate_tracing(name, integration):
     """Certificate tracing (trace_pixel, the algorithm of k_trace and the
     tracing batch kernel), both integrators, against the FP64 oracle on the
@@ -132,6 +132,20 @@ def test_certificate_tracing(name, integration):
         w = W.cube_minus_sphere_cylinder(128)
     elif name == "batched":
         w = W.reduced(W.batched_scenes(3)[2], 128, 3)
+    elif name == "coll_affine":
+        # ray certificates of every primitive under a chain of affine steps
+        coll = {"type": "object_collection", "objects": [
+            {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+            {"type": "box", "center": [0.0, 0.2, 0.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5},
+            {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+            {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+             "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9},
+            {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0}]}
+        deform = {"type": "composed", "deformations": [
+            {"type": "affine", "matrix": [[1.1, 0.0, 0.1], [0.0, 0.9, 0.0], [0.05, 0.0, 1.0]]},
+            {"type": "rigid", "displacements": [0.05, -0.1, 0.02]},
+            {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]}]}
+        w = W.Workload("c", coll, deform, [(10.0, 80.0), (200.0, 120.0), (95.0, 40.0)], 96, 0.004)
     else:
         coll = {"type": "object_collection", "objects": [
             {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},

@@ -70,17 +70,52 @@ CASES = {
 }
 
 
+def _affine_collection():
+    # every primitive under a chain of affine steps (ray certificates)
+    coll = {"type": "object_collection", "objects": [
+        {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+        {"type": "box", "center": [0.0, 0.2, 0.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5},
+        {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+        {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+         "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9},
+        {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0}]}
+    deform = {"type": "composed", "deformations": [
+        {"type": "affine", "matrix": [[1.1, 0.0, 0.1], [0.0, 0.9, 0.0], [0.05, 0.0, 1.0]]},
+        {"type": "rigid", "displacements": [0.05, -0.1, 0.02]},
+        {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]}]}
+    return W.Workload("affine_collection", coll, deform, [(10.0, 80.0), (200.0, 120.0)], 48, 0.004)
+
+
+TRACE_CASES = dict(CASES, affine_collection=_affine_collection)
+
+
+@pytest.mark.parametrize("mode", [True, "ball"])
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-@pytest.mark.parametrize("name", sorted(CASES))
-def test_certificate_tracing_matches_oracle(X, name, integration):
-    w = CASES[name]()
+@pytest.mark.parametrize("name", sorted(TRACE_CASES))
+def test_certificate_tracing_matches_oracle(X, name, integration, mode):
+    """Tracing with ray bounds (affine chains; the gyroid's sigmoid chain
+    falls back to balls) and with ball certificates only."""
+    w = TRACE_CASES[name]()
     ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
                    integration=integration)
     with X.Scene(w.obj, w.deformation) as s:
         img, st = X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
-                                    trace=True, stats=True, integration=integration)
+                                    trace=mode, stats=True, integration=integration)
     assert np.max(np.abs(img - ref) / ref) <= REL_TOL
     assert st["evaluations"] > 0 and st["fp64_list_overflow"] == 0
+
+
+def test_ray_certificates_evaluate_less_than_balls(X):
+    # the lattice (linear strain): the ray bound jumps straight to the next
+    # strut or cell face instead of approaching it geometrically
+    w = W.reduced(W.deformed_lattice(), 64, 2)
+    with X.Scene(w.obj, w.deformation) as s:
+        kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, stats=True)
+        a, st_ray = X.render_proposal(s, None, w.angles, trace=True, **kw)
+        b, st_ball = X.render_proposal(s, None, w.angles, trace="ball", **kw)
+    assert np.max(np.abs(a - b) / b) <= 2 * REL_TOL
+    assert 2 * st_ray["evaluations"] < st_ball["evaluations"]
+    print(f"\nevaluations: ray {st_ray['evaluations']}, ball {st_ball['evaluations']}")
 
 
 @pytest.mark.parametrize("name", sorted(CASES))

@@ -67,6 +67,7 @@ XRP_FLAG_STATS = 1
 XRP_FLAG_VOLUME_LOADS = 2
 XRP_FLAG_NO_REFINE = 4
 XRP_FLAG_TRACE = 8
+XRP_FLAG_BALL = 16
 
 # Every symbol include/xrp.h declares, with (restype, argtypes).
 SIGNATURES = {

@@ -151,13 +151,17 @@ struct SceneDev {
     int32_t root;
     int32_t ndefs;
     int32_t hier_zero_guard;  // 1: flag near-zero voxel values (hierarchical zero test)
-    int32_t pad;
+    int32_t affine;           // 1: the deformation chain is affine and invertible (or empty)
     float sup_lo[3], sup_hi[3];  // dilated support box (FP32, world)
     // distance certificates (margin32): 1 / Lipschitz bound of the
     // deformation chain, and the absolute error allowance of a margin in
     // deformed coordinates (position error plus FP32 arithmetic)
     float inv_lip;
     float m_slack;
+    // ray certificates (dens_ray32, affine chains): capsule radius in
+    // deformed coordinates (m_slack plus the direction error over the span)
+    float ray_slack;
+    float pad2;
 };
 
 // One view (camera) of a batch, prepared on the host.
@@ -797,6 +801,444 @@ XRP_HD float dens_margin32(const SceneDev& S, float x, float y, float z, float& 
     else rho = item_dm<DEPTH>(S, S.root, x, y, z, m);
     m = fmaf(m, 0.9999f, -S.m_slack);
     m = m > 0.0f ? m * S.inv_lip : 0.0f;
+    return rho;
+}
+
+// ---------------------------------------------------------------------------
+// Ray certificates.  When the deformation chain is affine (linear, affine,
+// rigid or none) the samples ahead of a point lie on a straight line in
+// object coordinates, w + u t, with u the chain's linear part applied to the
+// ray direction (per unit of the ray parameter).  Instead of a ball around
+// the sample, the bound is a ray parameter t before which the line cannot
+// come within `eps` of a place where the density changes: the first
+// crossing of each primitive's boundary inflated (outside) or shrunk
+// (inside) by eps, of a tessellation cell face, of a candidate-list cell
+// face.  All points within eps of the segment [w, w + u t] (a capsule) then
+// have the density of the sample.  eps (SceneDev::ray_slack) covers the
+// position error of the FP32 sample, the direction error over the sampled
+// span and the FP32 arithmetic of the crossings, as m_slack does for balls.
+// Every bound is also at least the ball bound (distance - eps) / |u|.
+// ---------------------------------------------------------------------------
+struct RayDir {
+    float x, y, z;     // object-space direction per unit ray parameter
+    float ix, iy, iz;  // reciprocals of the components (0 for a zero component)
+    float a;           // |u|^2
+    float il;          // 1 / |u|
+    float eps;         // capsule radius (object units)
+};
+
+constexpr float kFar = 3.0e38f;
+constexpr float kU32 = 5.9604645e-8f;  // 2^-24
+
+// Reciprocal and reciprocal square root of the crossing arithmetic: the
+// hardware approximations on the device (a few ulp; the final bound is
+// scaled by 1 - 1e-5 and the capsule radius budgets relative errors of the
+// crossings), exact division on the host build.
+XRP_HD float frcp(float x) {
+#if defined(__CUDA_ARCH__)
+    return __fdividef(1.0f, x);
+#else
+    return 1.0f / x;
+#endif
+}
+
+XRP_HD float frsqrt(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
+
+// A direction component this small counts as zero (the slab is parallel).
+XRP_HD float rcp_dir(float d) { return fabsf(d) > 1e-30f ? frcp(d) : 0.0f; }
+
+// Object-space direction of a ray (linear parts of an affine chain).
+XRP_HD RayDir ray_dir32(const SceneDev& S, const float* d) {
+    float x = d[0], y = d[1], z = d[2];
+    for (int i = 0; i < S.ndefs; i++) {
+        const DefStep& s = S.defs[i];
+        const float* a = s.f;
+        if (s.type == D_LINEAR) {
+            float nx = fmaf(a[4], z, fmaf(a[5], y, fmaf(a[0], x, x)));
+            float ny = fmaf(a[3], z, fmaf(a[1], y, fmaf(a[5], x, y)));
+            float nz = fmaf(a[2], z, fmaf(a[3], y, fmaf(a[4], x, z)));
+            x = nx; y = ny; z = nz;
+        } else if (s.type == D_AFFINE) {
+            float nx = fmaf(a[2], z, fmaf(a[1], y, a[0] * x));
+            float ny = fmaf(a[5], z, fmaf(a[4], y, a[3] * x));
+            float nz = fmaf(a[8], z, fmaf(a[7], y, a[6] * x));
+            x = nx; y = ny; z = nz;
+        }
+    }
+    RayDir u;
+    u.x = x; u.y = y; u.z = z;
+    u.ix = rcp_dir(x); u.iy = rcp_dir(y); u.iz = rcp_dir(z);
+    u.a = fmaf(z, z, fmaf(y, y, x * x));
+    u.il = 1.0f / sqrtf(u.a);
+    u.eps = S.ray_slack;
+    return u;
+}
+
+// Slab q + dq t inside (lo, hi), idq = 1/dq (0: parallel): exit parameter
+// of the shrunk slab [lo + e, hi - e] for a point inside it.
+XRP_HD float slab_exit(float q, float idq, float lo, float hi, float e) {
+    if (idq > 0.0f) return (hi - e - q) * idq;
+    if (idq < 0.0f) return (lo + e - q) * idq;
+    return kFar;
+}
+
+// Slab q + dq t inside the inflated slab (lo - e, hi + e): narrows [tlo, thi].
+XRP_HD void slab_clip(float q, float idq, float lo, float hi, float e, float& tlo, float& thi) {
+    if (idq != 0.0f) {
+        float a = (lo - e - q) * idq, b = (hi + e - q) * idq;
+        tlo = fmaxf(tlo, fminf(a, b));
+        thi = fminf(thi, fmaxf(a, b));
+    } else if (!(q > lo - e && q < hi + e)) {
+        tlo = kFar;
+    }
+}
+
+// Line w + u t against a ball (3-D) or a disc (the projection of a
+// cylinder) of radius R about the origin: from the closest approach
+// tc = -b/a and the half chord sqrt(R^2 - h^2), h^2 = c2/a the squared
+// distance of the line from the origin (c2 = |w x u|^2, stable near
+// tangency).  `err` bounds the FP32 error of the half chord (large only
+// when the line is nearly tangent; a line within eps/2 of tangency to the
+// inflated ball stays clear of the true one).  Outside (R = r + eps):
+// returns the entry interval widened by the error, or false when the line
+// never enters.  Inside (R = r - eps): chord_exit is the shrunk exit.
+XRP_HD bool chord_interval(float a, float b, float c2, float wl1, float R, float eps, float& tlo,
+                           float& thi) {
+    const float ia = frcp(a);
+    const float h2 = c2 * ia;
+    const float tc = -b * ia;
+    const float Rt = R - 0.5f * eps;
+    if (!(h2 < Rt * Rt)) return false;
+    const float ch = sqrtf(fmaf(R, R, -h2));
+    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * wl1);
+    const float il = frsqrt(a);
+    tlo = tc - (ch + err) * il;
+    thi = tc + (ch + err) * il;
+    return true;
+}
+
+XRP_HD float chord_exit(float a, float b, float c2, float wl1, float R) {
+    const float ia = frcp(a);
+    const float h2 = c2 * ia;
+    const float tc = -b * ia;
+    const float ch = sqrtf(fmaxf(fmaf(R, R, -h2), 0.0f));
+    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * wl1);
+    return tc + (ch - err) * frsqrt(a);  // -inf when ch == 0: the caller's ball bound holds
+}
+
+// Every partial bound below is clamped with fmaxf(., 0) before it enters a
+// minimum, so that a NaN (never expected) can only shorten a jump.
+
+// Sphere of radius r, point w from the centre at signed distance g.
+XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const RayDir& u) {
+    const float eps = u.eps;
+    const float ag = fabsf(g) - eps;
+    if (!(ag > 0.0f)) return 0.0f;
+    const float tb = ag * u.il;
+    const float b = fmaf(wz, u.z, fmaf(wy, u.y, wx * u.x));
+    const float cx = fmaf(wy, u.z, -wz * u.y), cy = fmaf(wz, u.x, -wx * u.z), cz = fmaf(wx, u.y, -wy * u.x);
+    const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+    const float wl1 = fabsf(wx) + fabsf(wy) + fabsf(wz);
+    if (g > 0.0f) {
+        if (!(b < 0.0f)) return kFar;  // moving away: the distance only grows
+        float lo, hi;
+        if (!chord_interval(u.a, b, c2, wl1, r + eps, eps, lo, hi)) return kFar;
+        return fmaxf(tb, lo);
+    }
+    return fmaxf(tb, chord_exit(u.a, b, c2, wl1, r - eps));
+}
+
+// Finite cylinder: w from p0, axial fraction c, perpendicular part p, radial
+// and axial signed distances gr, ga (negative inside).
+XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, float gr, float ga,
+                     const RayDir& u) {
+    const float eps = u.eps;
+    const float g = fmaxf(gr, ga);
+    if (!(fabsf(g) > eps)) return 0.0f;
+    const float tb = (fabsf(g) - eps) * u.il;
+    const float cu = fmaf(u.z, f[5], fmaf(u.y, f[4], u.x * f[3])) * f[6];
+    const float qx = fmaf(-cu, f[3], u.x), qy = fmaf(-cu, f[4], u.y), qz = fmaf(-cu, f[5], u.z);
+    const float a = fmaf(qz, qz, fmaf(qy, qy, qx * qx));
+    const bool chord = a > 1e-12f * u.a;  // not parallel to the axis
+    float b = 0.0f, c2 = 0.0f;
+    if (chord) {
+        b = fmaf(pz, qz, fmaf(py, qy, px * qx));
+        const float cx = fmaf(py, qz, -pz * qy), cy = fmaf(pz, qx, -px * qz), cz = fmaf(px, qy, -py * qx);
+        c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+    }
+    const float wl1 = fabsf(px) + fabsf(py) + fabsf(pz);
+    const float r = f[8];
+    const float ec = fmaf(eps, f[9] * f[6], f[F_BAND2]);  // eps / |v| + band of c
+    float t;
+    if (g < 0.0f) {
+        float tr = chord ? fmaxf(chord_exit(a, b, c2, wl1, r - eps), 0.0f)
+                         : (a > 0.0f ? (-gr - eps) * frsqrt(a) : kFar);
+        t = fminf(fmaxf(slab_exit(c, rcp_dir(cu), 0.0f, 1.0f, ec), 0.0f), tr);
+    } else {
+        float lo = 0.0f, hi = kFar;
+        slab_clip(c, rcp_dir(cu), 0.0f, 1.0f, ec, lo, hi);
+        if (chord) {
+            float rlo, rhi;
+            if (chord_interval(a, b, c2, wl1, r + eps, eps, rlo, rhi)) {
+                lo = fmaxf(lo, rlo);
+                hi = fminf(hi, rhi);
+            } else {
+                lo = kFar;
+            }
+        } else if (gr > eps) {
+            lo = fmaxf(lo, a > 0.0f ? (gr - eps) * frsqrt(a) : kFar);
+        }
+        t = lo <= hi ? lo : kFar;
+    }
+    return fmaxf(fmaxf(t, 0.0f), tb);
+}
+
+// Axis-aligned box of half sides h (F_BAND b): point w from the centre,
+// mn = min(h - |w|).
+XRP_HD float box_ray(const float* h, float wx, float wy, float wz, float mn, float b, const RayDir& u) {
+    const float e = u.eps + b;
+    if (mn > e) {
+        float t = fminf(fminf(slab_exit(wx, u.ix, -h[0], h[0], e), slab_exit(wy, u.iy, -h[1], h[1], e)),
+                        slab_exit(wz, u.iz, -h[2], h[2], e));
+        return fmaxf(t, 0.0f);
+    }
+    if (mn < -e) {
+        float lo = 0.0f, hi = kFar;
+        slab_clip(wx, u.ix, -h[0], h[0], e, lo, hi);
+        slab_clip(wy, u.iy, -h[1], h[1], e, lo, hi);
+        slab_clip(wz, u.iz, -h[2], h[2], e, lo, hi);
+        return lo <= hi ? fmaxf(lo, 0.0f) : kFar;
+    }
+    return 0.0f;
+}
+
+// Leaf density (leaf_dm's decisions) and its ray bound t.
+XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, float& t) {
+    const float* f = n.f;
+    switch (n.type) {
+    case N_SPHERE: {
+        float dx = x - f[0], dy = y - f[1], dz = z - f[2];
+        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        t = sphere_ray(dx, dy, dz, sqrtf(d2) - f[4], f[4], u);
+        float q = d2 - f[3];
+        if (q < -f[F_BAND]) return f[F_RHO];
+        if (q > f[F_BAND]) return 0.0f;
+        return xnan();
+    }
+    case N_BOX: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float mn = fminf(f[3] - fabsf(wx), fminf(f[4] - fabsf(wy), f[5] - fabsf(wz)));
+        float b = f[F_BAND];
+        t = box_ray(f + 3, wx, wy, wz, mn, b, u);
+        if (mn > b) return f[F_RHO];
+        if (mn < -b) return 0.0f;
+        return xnan();
+    }
+    case N_CYL: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
+        float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
+        float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
+        t = cyl_ray(f, c, px, py, pz, sqrtf(p2) - f[8], fmaxf(-c, c - 1.0f) * f[9], u);
+        float bc = f[F_BAND2];
+        if (c < -bc || c > 1.0f + bc) return 0.0f;
+        float q = p2 - f[7];
+        float bd = f[F_BAND];
+        if (q > bd) return 0.0f;
+        if (q < -bd && c > bc && c < 1.0f - bc) return f[F_RHO];
+        return xnan();
+    }
+    case N_PPD: {
+        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        float b = f[F_BAND];
+        float mn = 3.0e38f, tin = kFar, lo = 0.0f, hi = kFar;
+        bool out = false;
+        for (int a = 0; a < 3; a++) {
+            const float* r = f + 3 + 3 * a;
+            float q = fmaf(r[2], wz, fmaf(r[1], wy, r[0] * wx));
+            float iqu = rcp_dir(fmaf(r[2], u.z, fmaf(r[1], u.y, r[0] * u.x)));
+            float e = fmaf(u.eps, f[12 + a], b);
+            float in = fminf(q, 1.0f - q);
+            mn = fminf(mn, in);
+            out = out || in < -e;
+            tin = fminf(tin, fmaxf(slab_exit(q, iqu, 0.0f, 1.0f, e), 0.0f));
+            if (!(in > e)) tin = 0.0f;
+            slab_clip(q, iqu, 0.0f, 1.0f, e, lo, hi);
+        }
+        t = out ? (lo <= hi ? fmaxf(lo, 0.0f) : kFar) : tin;
+        if (mn > b) return f[F_RHO];
+        if (mn < -b) return 0.0f;
+        return xnan();
+    }
+    case N_GYROID: {
+        float X = (x - f[0]) * f[3], Y = (y - f[1]) * f[3], Z = (z - f[2]) * f[3];
+        float sx, cx, sy, cy, sz, cz;
+        f_sincos(X, &sx, &cx);
+        f_sincos(Y, &sy, &cy);
+        f_sincos(Z, &sz, &cz);
+        float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
+        float q = f[4] - fabsf(g);
+        float m = fmaxf(fabsf(q) - f[F_BAND], 0.0f) / (2.4494898f * fabsf(f[3]));
+        t = fmaxf(m - u.eps, 0.0f) * u.il;
+        if (q > f[F_BAND]) return f[F_RHO];
+        if (q < -f[F_BAND]) return 0.0f;
+        return xnan();
+    }
+    default: t = 0.0f; return xnan();
+    }
+}
+
+// Box [lo, hi] (per axis, interleaved lo0 hi0 lo1 hi1 ...): exit of the box
+// shrunk by e for a point at least e inside, entry of the box inflated by e
+// for a point more than e outside, else 0.  `in` is the point's smallest
+// distance to a face (negative outside).
+XRP_HD float bounds_ray(const float* b, float x, float y, float z, float in, float e, const RayDir& u) {
+    if (in > e) {
+        float t = fminf(fminf(slab_exit(x, u.ix, b[0], b[1], e), slab_exit(y, u.iy, b[2], b[3], e)),
+                        slab_exit(z, u.iz, b[4], b[5], e));
+        return fmaxf(t, 0.0f);
+    }
+    if (in < -e) {
+        float lo = 0.0f, hi = kFar;
+        slab_clip(x, u.ix, b[0], b[1], e, lo, hi);
+        slab_clip(y, u.iy, b[2], b[3], e, lo, hi);
+        slab_clip(z, u.iz, b[4], b[5], e, lo, hi);
+        return lo <= hi ? fmaxf(lo, 0.0f) : kFar;
+    }
+    return 0.0f;
+}
+
+template <int D>
+XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float& t);
+
+// item_dm's decisions; t: the ray bound (tessellations: the outer bounds,
+// the cell faces of the fold and the unit-cell bounds cap the collection's).
+template <int D>
+XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const RayDir& u, float& t) {
+    const Node& n = S.nodes[id];
+    if (n.type <= N_GYROID) return leaf_dr(n, x, y, z, u, t);
+    if (n.type == N_TESS) {
+        if constexpr (D > 0) {
+            const float* f = n.f;
+            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
+                             fminf(z - f[4], f[5] - z));
+            const float to = bounds_ray(f, x, y, z, mo, u.eps + f[6], u);
+            if (mo < -f[6]) { t = to; return 0.0f; }  // outside: zero up to the bounds
+            if (!(mo > f[6])) { t = 0.0f; return xnan(); }
+            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
+            float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
+            float bq = f[23];
+            float frx = qx - nx, fry = qy - ny, frz = qz - nz;
+            float fr = fminf(fminf(fminf(frx, 1.0f - frx), fminf(fry, 1.0f - fry)), fminf(frz, 1.0f - frz));
+            if (!(fr > bq)) { t = 0.0f; return xnan(); }
+            // exit of this tessellation cell (q units; eps scaled by 1/cell size)
+            // (1/(u f17) = (1/u) f14: f14 is the cell size, f17 its reciprocal)
+            float tc = fminf(fminf(fmaxf(slab_exit(frx, u.ix * f[14], 0.0f, 1.0f, fmaf(u.eps, fabsf(f[17]), bq)), 0.0f),
+                                   fmaxf(slab_exit(fry, u.iy * f[15], 0.0f, 1.0f, fmaf(u.eps, fabsf(f[18]), bq)), 0.0f)),
+                             fmaxf(slab_exit(frz, u.iz * f[16], 0.0f, 1.0f, fmaf(u.eps, fabsf(f[19]), bq)), 0.0f));
+            const float tt = fminf(to, tc);
+            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
+            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
+                             fminf(fz - f[11], f[12] - fz));
+            const float tu = bounds_ray(f + 7, fx, fy, fz, mu, u.eps + f[13], u);
+            if (mu < -f[13]) { t = fminf(tt, tu); return 0.0f; }  // outside the unit-cell bounds
+            if (!(mu > f[13])) { t = 0.0f; return xnan(); }
+            float tk;
+            float r = coll_dr<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tk);
+            t = fminf(fminf(tt, tu), tk);
+            return r;
+        }
+    }
+    t = 0.0f;  // voxel grids and anything deeper: density by the plain path
+    if (n.type == N_VOXEL) return voxel32(S.vols[n.a], n.f[0], x, y, z, S.hier_zero_guard);
+    return xnan();
+}
+
+// coll_dm's decisions; t: the minimum over the candidates, capped (with
+// candidate lists) by the later of the exit from the point's list cell and
+// the clearance of the unlisted children.
+template <int D>
+XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float& t) {
+    const int32_t* kids = S.child + c.a;
+    int cnt = c.b;
+    const int32_t* list = nullptr;
+    t = kFar;
+    if (c.flags & C_ACCEL) {
+        int G = (c.flags >> 16) & 0xff;
+        float ux = (x - c.f[0]) * c.f[3], uy = (y - c.f[1]) * c.f[4], uz = (z - c.f[2]) * c.f[5];
+        int ix = (int)floorf(ux), iy = (int)floorf(uy), iz = (int)floorf(uz);
+        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
+        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
+        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
+        // inner faces only (the outer cells extend to infinity by the clamp)
+        float tc = kFar;
+        {
+            // grid units; 1/(u f3) = (1/u) f8 (f8: the cell size)
+            const float dx = u.ix * c.f[8], ex = u.eps * c.f[3];
+            if (dx > 0.0f && ix < G - 1) tc = fminf(tc, fmaxf(((float)(ix + 1) - ex - ux) * dx, 0.0f));
+            if (dx < 0.0f && ix > 0) tc = fminf(tc, fmaxf(((float)ix + ex - ux) * dx, 0.0f));
+            const float dy = u.iy * c.f[9], ey = u.eps * c.f[4];
+            if (dy > 0.0f && iy < G - 1) tc = fminf(tc, fmaxf(((float)(iy + 1) - ey - uy) * dy, 0.0f));
+            if (dy < 0.0f && iy > 0) tc = fminf(tc, fmaxf(((float)iy + ey - uy) * dy, 0.0f));
+            const float dz = u.iz * c.f[10], ez = u.eps * c.f[5];
+            if (dz > 0.0f && iz < G - 1) tc = fminf(tc, fmaxf(((float)(iz + 1) - ez - uz) * dz, 0.0f));
+            if (dz < 0.0f && iz > 0) tc = fminf(tc, fmaxf(((float)iz + ez - uz) * dz, 0.0f));
+        }
+        int cell_base = f2i(c.f[6]);
+        const int cell = cell_base + (iz * G + iy) * G + ix;
+        t = fmaxf(tc, fmaxf(S.clear[cell] - u.eps, 0.0f) * u.il);
+        const int32_t* off = S.cells + cell;
+        int s0 = off[0], s1 = off[1];
+        list = S.items + s0;
+        cnt = s1 - s0;
+    }
+    const bool greedy = (c.flags & C_GREEDY) != 0;
+    float sum = 0.0f, sabs = 0.0f;
+    bool unc = false, done = false;
+    for (int k = 0; k < cnt; k++) {
+        int slot = list ? list[k] : k;
+        float tk;
+        float r = item_dr<D>(S, kids[slot], x, y, z, u, tk);
+        t = fminf(t, tk);
+        if (done) continue;  // greedy value fixed; bounds of the rest still count
+        if (isunc(r)) {
+            unc = true;
+            done = true;
+            continue;
+        }
+        if (greedy && r > 0.0f) {
+            sum = r;
+            sabs = fabsf(r);
+            done = true;
+            continue;
+        }
+        sum += r;
+        sabs += fabsf(r);
+    }
+    if (unc) return xnan();
+    if (greedy && done) return sum;
+    if (!(c.flags & C_EXACT_SUM) && sabs > 0.0f && fabsf(sum) <= c.f[7] * sabs) return xnan();
+    if (c.flags & C_CLIP) sum = fminf(fmaxf(sum, 0.0f), 1.0f);
+    return sum;
+}
+
+// density32 at one point and the ray bound t (ray parameter units) of the
+// samples ahead that share its density; affine chains only.
+template <int DEPTH, bool DEFS>
+XRP_HD float dens_ray32(const SceneDev& S, float x, float y, float z, const RayDir& u, float& t) {
+    if constexpr (DEFS) deform32(S, x, y, z);
+    const Node& r = S.nodes[S.root];
+    float rho;
+    if (r.type <= N_GYROID) rho = leaf_dr(r, x, y, z, u, t);
+    else if (r.type == N_COLL) rho = coll_dr<DEPTH>(S, r, x, y, z, u, t);
+    else rho = item_dr<DEPTH>(S, S.root, x, y, z, u, t);
+    t = fmaxf(t, 0.0f) * 0.99999f;
     return rho;
 }
 
@@ -1491,15 +1933,19 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
 // Certificate tracing of one ray over lattice samples [k0, k1]: at sample k
 // the density and the certificate radius m (dens_margin32); the samples
 // k..k+j with j*ds <= m lie inside the ball around sample k, so they share
-// its density and are counted at once.  `unc(k)` returns the value of a
+// its density and are counted at once.  With RAY (affine chains) m is the
+// ray bound of dens_ray32 instead: the samples k..k+j with j*ds <= m lie on
+// the certified segment.  `unc(k)` returns the value of a
 // sample FP32 cannot decide (its FP64 density, or 0 when the caller
 // re-evaluates it later).  Returns the Kahan-compensated sum of densities,
 // the same terms as march_simple.
-template <int DEPTH, bool DEFS, class Unc>
+template <int DEPTH, bool DEFS, bool RAY, class Unc>
 XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
                        unsigned& evals) {
     KahanF acc;
     const float step = L.ds32 * 1.00001f;  // world distance between samples, rounded up
+    RayDir u;
+    if constexpr (RAY) u = ray_dir32(S, ray.d32);
     int k = k0;
     while (k <= k1) {
         const float tk = lattice_t(L, k);
@@ -1507,7 +1953,9 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
         const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
         const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
         float m;
-        const float rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+        float rho;
+        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, m);
+        else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         if (isunc(rho)) {
             acc.add(unc(k));
@@ -1529,19 +1977,24 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 // `unc(index, fine)` gives the value of an undecided coarse (fine = false,
 // index into s64) or fine (fine = true, index into f64) sample.  Returns
 // sum(w * rho) with w in {DS, DS/10}.
-template <int DEPTH, bool DEFS, class Unc>
+template <int DEPTH, bool DEFS, bool RAY, class Unc>
 XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
                             unsigned& evals) {
     KahanF acc;
     const float step = L.ds32 * 1.00001f;
+    RayDir u;
+    if constexpr (RAY) u = ray_dir32(S, ray.d32);
     bool prev_zero = true;  // coarse samples before k0 are outside the support
     int k = k0;
     while (k <= k1) {
         const float tk = lattice_t(L, k);
+        const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
+        const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
+        const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
         float m;
-        float rho = dens_margin32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tk, ray.pc[0]),
-                                               fmaf(ray.d32[1], tk, ray.pc[1]),
-                                               fmaf(ray.d32[2], tk, ray.pc[2]), m);
+        float rho;
+        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, m);
+        else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         int jmp = 0;
         if (isunc(rho)) {
@@ -1573,7 +2026,7 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
 }
 
 // One pixel by certificate tracing, FP64 for undecided samples in place.
-template <bool HIER, int DEPTH, bool DEFS>
+template <bool HIER, int DEPTH, bool DEFS, bool RAY>
 XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P, const ViewDev& V,
                          int i, int j, unsigned& evals) {
     Ray r;
@@ -1588,14 +2041,14 @@ XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams
     float acc = 0.0f;
     if (sample_range(L, t0, t1, L.K, k0, k1)) {
         if constexpr (HIER) {
-            acc = trace_sum_hier<DEPTH, DEFS>(
+            acc = trace_sum_hier<DEPTH, DEFS, RAY>(
                 S, L, r, k0, k1,
                 [&](int q, bool fine) {
                     return (float)sample64_pixel(S, V, P.xs, i, j, fine ? L.f64[q] : L.s64[q]);
                 },
                 evals);
         } else {
-            acc = trace_sum<DEPTH, DEFS>(
+            acc = trace_sum<DEPTH, DEFS, RAY>(
                 S, L, r, k0, k1,
                 [&](int k) { return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[k]); }, evals);
         }

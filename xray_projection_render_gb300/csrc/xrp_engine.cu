@@ -985,7 +985,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     std::vector<HostPrepared> hps(n);
     std::vector<std::vector<ViewDev>> vws(n);
     int depth = 0;
-    bool defs = false;
+    bool defs = false, affine = true;
     for (int q = 0; q < n; q++) {
         const xrp_batch_item& it = items[order[q]];
         double fov_max;
@@ -1002,6 +1002,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         }
         depth = std::max(depth, hps[q].fs.depth);
         defs = defs || !hps[q].fs.defs.empty();
+        affine = affine && hps[q].fs.affine;
     }
     const HostLattice& hl = hps[0].hl;
     // one upload: per item its scene tables, views and pixel table, then the
@@ -1076,7 +1077,8 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
     const bool hier = oo.integration == XRP_INTEGRATE_HIERARCHICAL;
-    const bool trace = (oo.flags & XRP_FLAG_TRACE) != 0;
+    // ray certificates when every scene's chain is affine (and not refused)
+    const int trace = !(oo.flags & XRP_FLAG_TRACE) ? 0 : (affine && !(oo.flags & XRP_FLAG_BALL)) ? 2 : 1;
     const int kdepth = depth == 0 ? 0 : kMaxDepth;
     if ((e = batch_blocks_per_sm(kdepth, defs, hier, trace, &occ)) != cudaSuccess)
         return cuda_fail(7, "batch occupancy", e);
@@ -1553,7 +1555,7 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     memset(&pl.Q, 0, sizeof(pl.Q));
     pl.Q.mc = segment;
     pl.Q.refine = (o->flags & XRP_FLAG_NO_REFINE) ? 0 : 1;
-    pl.Q.trace = (o->flags & XRP_FLAG_TRACE) ? 1 : 0;
+    pl.Q.trace = !(o->flags & XRP_FLAG_TRACE) ? 0 : (o->flags & XRP_FLAG_BALL) ? 2 : 1;
     pl.Q.min_piece = 8;
     if (prop) {
         pl.Q.mlp = prop->params;

@@ -1,126 +1,23 @@
-// xrp_kern_batch.cu -- the batch kernel: many scenes of uneven size in one
-// persistent launch (xrp_batch_* in xrp_engine.cu).
-#include "xrp_launch.h"
+// xrp_kern_batch.cu -- the batch kernel with the plain integrator, and the
+// dispatch over certificate modes (xrp_batch_* in xrp_engine.cu).
+#include "xrp_batch.cuh"
 
 namespace xrp {
 
-// Batches of scenes (general path): every warp of a persistent grid takes
-// 32-pixel tiles (tw x th) from a global counter, so scenes, resolutions
-// and view counts of uneven size share one launch and balance across SMs
-// without block barriers (rays differ in length; a block-wide tile would
-// hold finished warps at a barrier).  Items are ordered by decreasing work
-// and their tiles numbered consecutively; a tile's item is found by binary
-// search on the items' first tile.  The tile's scene header, item
-// parameters and view are staged in the warp's shared memory.
-static_assert(sizeof(SceneDev) % 4 == 0 && sizeof(RenderParams) % 4 == 0 && sizeof(ViewDev) % 4 == 0,
-              "staged structures are copied as 32-bit words");
-
-struct BatchStage {
-    SceneDev S;
-    RenderParams P;
-    ViewDev V;
-};
-
-template <bool HIER, int DEPTH, bool DEFS, bool TRACE>
-__global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 3 : XRP_SCENE_MIN_BLOCKS)
-    k_batch(const SceneDev* __restrict__ scenes, const BatchItemDev* __restrict__ items, int nitems,
-            const ViewDev* __restrict__ views, const __grid_constant__ Lattice L, long long ntiles, int tw,
-            int th, unsigned long long* __restrict__ counter, long long stride, long long limit,
-            float* __restrict__ out) {
-    __shared__ __align__(16) BatchStage stage[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    BatchStage& sg = stage[warp];
-    for (;;) {
-        long long t = -1;
-        int item = 0;
-        if (lane == 0) {
-            unsigned long long k = atomicAdd(counter, 1ull);
-            t = (long long)k < limit ? (long long)k * stride : ntiles;
-            if (t >= ntiles) t = -1;
-            if (t >= 0) {
-                int lo = 0, hi = nitems - 1;
-                while (lo < hi) {  // last item with tile0 <= t
-                    int mid = (lo + hi + 1) >> 1;
-                    if (items[mid].tile0 <= t) lo = mid;
-                    else hi = mid - 1;
-                }
-                item = lo;
-            }
-        }
-        t = __shfl_sync(0xffffffffu, t, 0);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (t < 0) break;
-        const BatchItemDev& B = items[item];
-        const int res = B.P.res;
-        const long long local = t - B.tile0;
-        const int tpv = B.tiles_x * B.tiles_y;
-        const int v = (int)(local / tpv);
-        {
-            const unsigned* src_s = reinterpret_cast<const unsigned*>(scenes + B.scene);
-            const unsigned* src_p = reinterpret_cast<const unsigned*>(&B.P);
-            const unsigned* src_v = reinterpret_cast<const unsigned*>(views + B.view0 + v);
-            unsigned* ds_ = reinterpret_cast<unsigned*>(&sg.S);
-            unsigned* dp_ = reinterpret_cast<unsigned*>(&sg.P);
-            unsigned* dv_ = reinterpret_cast<unsigned*>(&sg.V);
-            constexpr int ns = sizeof(SceneDev) / 4, np = sizeof(RenderParams) / 4, nv = sizeof(ViewDev) / 4;
-            for (int q = lane; q < ns + np + nv; q += 32) {
-                if (q < ns) ds_[q] = src_s[q];
-                else if (q < ns + np) dp_[q - ns] = src_p[q - ns];
-                else dv_[q - ns - np] = src_v[q - ns - np];
-            }
-        }
-        __syncwarp();
-        const int tt = (int)(local - (long long)v * tpv);
-        const int ty = tt / B.tiles_x, tx = tt - ty * B.tiles_x;
-        const int i = ty * th + lane / tw;
-        const int j = tx * tw + lane % tw;
-        if (i < res && j < res) {
-            float val;
-            if constexpr (TRACE) {
-                unsigned ev = 0;
-                val = trace_pixel<HIER, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, ev);
-            } else {
-                RayStats st{0, 0};
-                val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);
-            }
-            out[B.out0 + ((long long)v * res + i) * res + j] = val;
-        }
-        __syncwarp();  // before the next tile overwrites the staged data
-    }
-}
-
-template <bool HIER, int DEPTH, bool DEFS, bool TRACE>
-static cudaError_t launch_batch_t(const BatchLaunch& b, cudaStream_t st) {
-    k_batch<HIER, DEPTH, DEFS, TRACE><<<b.blocks, 256, 0, st>>>(b.scenes, b.items, b.nitems, b.views, b.L,
-                                                                b.ntiles, b.tw, b.th, b.counter, b.stride,
-                                                                b.limit, b.out);
-    return cudaGetLastError();
-}
-
-template <int DEPTH, bool DEFS>
-static cudaError_t launch_batch_d(const BatchLaunch& b, cudaStream_t st) {
-    if (b.trace) return b.hier ? launch_batch_t<true, DEPTH, DEFS, true>(b, st)
-                               : launch_batch_t<false, DEPTH, DEFS, true>(b, st);
-    if (b.hier) return launch_batch_t<true, DEPTH, DEFS, false>(b, st);
-    return launch_batch_t<false, DEPTH, DEFS, false>(b, st);
-}
+cudaError_t launch_batch_plain(const BatchLaunch& b, cudaStream_t st) { return launch_batch_mode<0>(b, st); }
+const void* batch_fn_plain(int depth, bool defs, bool hier) { return batch_fn_mode<0>(depth, defs, hier); }
 
 cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st) {
     if (b.blocks <= 0 || b.ntiles <= 0) return cudaSuccess;
-    if (b.depth == 0) return b.defs ? launch_batch_d<0, true>(b, st) : launch_batch_d<0, false>(b, st);
-    return b.defs ? launch_batch_d<3, true>(b, st) : launch_batch_d<3, false>(b, st);
+    if (b.trace == 2) return launch_batch_ray(b, st);
+    if (b.trace == 1) return launch_batch_ball(b, st);
+    return launch_batch_plain(b, st);
 }
 
-template <int DEPTH, bool DEFS>
-static const void* batch_fn(bool hier, bool trace) {
-    if (trace) return hier ? (const void*)k_batch<true, DEPTH, DEFS, true> : (const void*)k_batch<false, DEPTH, DEFS, true>;
-    if (hier) return (const void*)k_batch<true, DEPTH, DEFS, false>;
-    return (const void*)k_batch<false, DEPTH, DEFS, false>;
-}
-
-cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, bool trace, int* out) {
-    const void* f = depth == 0 ? (defs ? batch_fn<0, true>(hier, trace) : batch_fn<0, false>(hier, trace))
-                               : (defs ? batch_fn<3, true>(hier, trace) : batch_fn<3, false>(hier, trace));
+cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int trace, int* out) {
+    const int d = depth == 0 ? 0 : 3;
+    const void* f = trace == 2 ? batch_fn_ray(d, defs, hier)
+                               : trace == 1 ? batch_fn_ball(d, defs, hier) : batch_fn_plain(d, defs, hier);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, f, 256, 0);
 }
 

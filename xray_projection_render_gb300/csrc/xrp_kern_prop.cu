@@ -7,32 +7,9 @@
 
 namespace xrp {
 
-template <int DEPTH, bool DEFS>
-static cudaError_t trace_t(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
-                           cudaStream_t st) {
-    const int tpr = (pr.P.res + 15) / 16;
-    long blocks = (long)nviews * tpr * tpr;
-    if (blocks <= 0) return cudaSuccess;
-    if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
-    if (pr.L.hierarchical)
-        k_trace<DEPTH, DEFS, true><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, nviews, Q, dout);
-    else
-        k_trace<DEPTH, DEFS, false><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0, nviews, Q, dout);
-    return cudaGetLastError();
-}
-
 static cudaError_t march(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                          cudaStream_t st) {
-    if (Q.trace) {
-        if (pr.defs) {
-            if (pr.depth == 0) return trace_t<0, true>(pr, view0, nviews, Q, dout, st);
-            if (pr.depth == 1) return trace_t<1, true>(pr, view0, nviews, Q, dout, st);
-            return trace_t<3, true>(pr, view0, nviews, Q, dout, st);
-        }
-        if (pr.depth == 0) return trace_t<0, false>(pr, view0, nviews, Q, dout, st);
-        if (pr.depth == 1) return trace_t<1, false>(pr, view0, nviews, Q, dout, st);
-        return trace_t<3, false>(pr, view0, nviews, Q, dout, st);
-    }
+    if (Q.trace) return launch_trace(pr, view0, nviews, Q, dout, st);
     if (Q.mlp) return launch_prop_net(pr, view0, nviews, Q, dout, st);
     if (Q.refine) { XRP_PROP_DISPATCH(kPropRefine, dout) }
     XRP_PROP_DISPATCH(kPropDense, dout)

@@ -90,7 +90,7 @@ struct BatchLaunch {
     int blocks;            // persistent grid size
     int depth;             // 0: no tessellation in the batch, else up to kMaxDepth
     bool defs, hier;
-    bool trace;            // certificate tracing (simple integrator)
+    int trace;             // certificate tracing: 0 off, 1 ball certificates, 2 ray certificates
     unsigned long long* counter;
     long long stride, limit;
     float* out;
@@ -98,13 +98,18 @@ struct BatchLaunch {
 
 // xrp_kern_batch.cu: the batch kernel and its occupancy.
 cudaError_t launch_batch(const BatchLaunch& b, cudaStream_t st);
-cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, bool trace, int* out);
+cudaError_t batch_blocks_per_sm(int depth, bool defs, bool hier, int trace, int* out);
 
 // xrp_kern_export.cu: volume export of a scene and device-side image finishing.
 cudaError_t launch_voxelize_scene(const SceneDev& S, int depth, bool defs, int res, double dm, float* out,
                                   unsigned* vmax_bits, unsigned char* u8, cudaStream_t st);
 cudaError_t launch_finish(const float* img, int nviews, int res, int transparency, unsigned short* gray,
                           unsigned short* alpha, float* minmax, cudaStream_t st);
+
+// xrp_kern_trace.cu: certificate tracing (k_trace); Q.trace 1: ray
+// certificates where the scene's chain is affine, else ball; 2: ball only.
+cudaError_t launch_trace(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                         cudaStream_t st);
 
 // xrp_kern_prop.cu: the proposal march (rendering).
 cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,

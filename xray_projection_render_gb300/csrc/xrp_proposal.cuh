@@ -428,16 +428,18 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
     }
 }
 
-#if defined(XRP_PROP_RENDER_KERNELS)
 // Certificate tracing: one thread per ray (16x16 pixel tiles, warps of 8x4
 // pixels like k_render, so neighbouring rays stay coherent).  At sample k
 // the density and the certificate radius m are evaluated; samples k .. k+j
 // with j*ds <= m lie inside the ball around sample k, so they all have its
 // density and are counted at once, and the march jumps to k+j+1.  Far from
 // any boundary the jumps are long; approaching one they shrink
-// geometrically; next to it the march steps sample by sample.  Samples FP32
-// cannot decide go to the FP64 list like the other march modes.
-template <int DEPTH, bool DEFS, bool HIER>
+// geometrically; next to it the march steps sample by sample.  RAY (affine
+// deformation chains): the certificate is the ray bound of dens_ray32, the
+// distance along the ray to the next possible density change, so a ray
+// jumps straight to the next boundary instead of approaching it.  Samples
+// FP32 cannot decide go to the FP64 list like the other march modes.
+template <int DEPTH, bool DEFS, bool HIER, bool RAY>
 __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
@@ -470,7 +472,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
                 // a coarse sample's value decides refinement: FP64 in place;
                 // fine samples only add, so they go to the list (high bit)
                 const ViewDev& V = views[view0 + v];
-                sum = trace_sum_hier<DEPTH, DEFS>(
+                sum = trace_sum_hier<DEPTH, DEFS, RAY>(
                     S, L, ray, k0, k1,
                     [&](int q, bool fine) {
                         if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
                     },
                     evals);
             } else {
-                sum = trace_sum<DEPTH, DEFS>(
+                sum = trace_sum<DEPTH, DEFS, RAY>(
                     S, L, ray, k0, k1,
                     [&](int k) {
                         unsigned slot = atomicAdd(Q.fb_count, 1u);
@@ -499,6 +501,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
     }
 }
 
+#if defined(XRP_PROP_RENDER_KERNELS)
 // FP64 re-evaluation of the samples the march left undecided: adds
 // w * density (reference arithmetic at the reference's position) to the
 // ray's optical depth.  Rays are numbered within the launch (view0 first).

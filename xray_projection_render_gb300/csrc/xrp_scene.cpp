@@ -510,7 +510,55 @@ struct Flattener {
         Box3 box;              // where FP32 may report non-zero or uncertain
         bool can_be_positive = false;
         Box3 pos_box;          // where the exact output may be positive
+        // spheres and cylinders: `box` is also contained in the capsule of
+        // radius reff around the segment p0-p1 (p0 == p1 for a sphere); a
+        // tighter test for the per-cell candidate lists than the box
+        bool capsule = false;
+        double p0[3] = {0, 0, 0}, p1[3] = {0, 0, 0};
+        double reff = 0.0;
     };
+
+    // Lower bound on the distance from box [lo, hi] (bounds may be
+    // infinite) to the capsule of `in` (0 when they may touch).  The
+    // distance from the box to the point p0 + t (p1 - p0) is convex in t:
+    // golden-section search, then minus the Lipschitz constant |p1 - p0|
+    // times the final bracket.
+    static double capsule_gap(const Info& in, const double lo[3], const double hi[3]) {
+        double v[3], L2 = 0;
+        for (int a = 0; a < 3; a++) {
+            v[a] = in.p1[a] - in.p0[a];
+            L2 += v[a] * v[a];
+        }
+        auto dist = [&](double t) {
+            double d2 = 0;
+            for (int a = 0; a < 3; a++) {
+                double p = in.p0[a] + v[a] * t;
+                double g = std::max(0.0, std::max(lo[a] - p, p - hi[a]));
+                d2 += g * g;
+            }
+            return std::sqrt(d2);
+        };
+        double a = 0.0, b = 1.0, best;
+        if (L2 > 0) {
+            const double q = 0.6180339887498949;
+            double x1 = b - q * (b - a), x2 = a + q * (b - a);
+            double f1 = dist(x1), f2 = dist(x2);
+            for (int it = 0; it < 40; it++) {
+                if (f1 < f2) {
+                    b = x2; x2 = x1; f2 = f1;
+                    x1 = b - q * (b - a); f1 = dist(x1);
+                } else {
+                    a = x1; x1 = x2; f1 = f2;
+                    x2 = a + q * (b - a); f2 = dist(x2);
+                }
+            }
+            best = std::min(f1, f2) - std::sqrt(L2) * (b - a) * 1.01;
+        } else {
+            best = dist(0.0);
+        }
+        best = best * (1.0 - 1e-9) - 1e-12 - in.reff;
+        return std::isfinite(best) ? std::max(best, 0.0) : 0.0;
+    }
 
     int emit(const Node& n, const Node64& n64) {
         fs.nodes.push_back(n);
@@ -544,7 +592,10 @@ struct Flattener {
             for (int a = 0; a < 3; a++) {
                 info.box.lo[a] = d[a] - reff;
                 info.box.hi[a] = d[a] + reff;
+                info.p0[a] = info.p1[a] = d[a];
             }
+            info.capsule = true;
+            info.reff = reff;
             break;
         }
         case N_BOX: {
@@ -599,7 +650,11 @@ struct Flattener {
             for (int a = 0; a < 3; a++) {
                 info.box.lo[a] = std::min(d[a], d[3 + a]) - reff;
                 info.box.hi[a] = std::max(d[a], d[3 + a]) + reff;
+                info.p0[a] = d[a];
+                info.p1[a] = d[3 + a];
             }
+            info.capsule = true;
+            info.reff = reff;
             break;
         }
         case N_PPD: {
@@ -622,6 +677,10 @@ struct Flattener {
             }
             for (int a = 0; a < 3; a++) n.f[a] = (float)d[a];
             for (int i = 0; i < 9; i++) n.f[3 + i] = (float)M[i];
+            // row norms (ray certificates: world distance -> q units)
+            for (int r2 = 0; r2 < 3; r2++)
+                n.f[12 + r2] = (float)(std::sqrt(M[r2 * 3] * M[r2 * 3] + M[r2 * 3 + 1] * M[r2 * 3 + 1] +
+                                                 M[r2 * 3 + 2] * M[r2 * 3 + 2]) * (1.0 + 1e-6));
             n.f[F_BAND] = (float)(kSafety * band);
             rho = d[12];
             if (!ok) {
@@ -826,6 +885,7 @@ struct Flattener {
                 h3[a] = w / G;
                 c.f[a] = (float)all.lo[a];
                 c.f[3 + a] = (float)(1.0 / h3[a]);
+                c.f[8 + a] = (float)h3[a];  // cell size (ray certificates)
             }
             double margin = 4 * E + 16 * kU * (P + all.maxabs() + ext) * (G + 1) + 1e-12;
             int cell_base = (int)fs.cells.size();
@@ -852,16 +912,21 @@ struct Flattener {
                         for (size_t k = 0; k < kids.size(); k++) {
                             const Box3& b = infos[k].box;
                             if (b.empty()) continue;
-                            bool hit = true;
-                            for (int a = 0; a < 3; a++) hit = hit && b.lo[a] <= hi[a] && b.hi[a] >= lo[a];
-                            if (hit) {
+                            double d2 = 0;
+                            for (int a = 0; a < 3; a++) {
+                                double gap = std::max(b.lo[a] - hi[a], lo[a] - b.hi[a]);
+                                if (gap > 0) d2 += gap * gap;
+                            }
+                            // spheres and cylinders: the distance to the capsule
+                            // (a box hit may still miss the capsule, e.g. a
+                            // diagonal strut and a corner cell)
+                            if (d2 == 0 && infos[k].capsule) {
+                                double g = capsule_gap(infos[k], lo, hi);
+                                d2 = g * g;
+                            }
+                            if (d2 == 0) {
                                 fs.items.push_back((int32_t)k);
                             } else {
-                                double d2 = 0;
-                                for (int a = 0; a < 3; a++) {
-                                    double gap = std::max(b.lo[a] - hi[a], lo[a] - b.hi[a]);
-                                    if (gap > 0) d2 += gap * gap;
-                                }
                                 clear2 = std::min(clear2, d2);
                             }
                         }
@@ -1059,6 +1124,41 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
     // a certificate radius is computed in FP32 from deformed coordinates of
     // magnitude P carrying the per-axis error E
     fs.margin_slack = 4.0 * (std::sqrt(3.0) * E + 64 * kU * (P + 1.0));
+    // ray certificates: an affine, invertible chain maps the ray to a line.
+    // The object-space direction is formed in FP32 from the FP32 direction
+    // (relative error ~(ndefs + 2) kU of lip per step); over the sampled span
+    // 2T that displaces the line by at most the term below, and the FP32
+    // crossing arithmetic adds a relative error of the same order.
+    {
+        double J[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        bool affine = true;
+        for (auto& d : hs.defs) {
+            const double* a = d.d;
+            double A[9];
+            if (d.type == D_LINEAR) {
+                double L[9] = {1 + a[0], a[5], a[4], a[5], 1 + a[1], a[3], a[4], a[3], 1 + a[2]};
+                std::memcpy(A, L, sizeof(A));
+            } else if (d.type == D_AFFINE) {
+                std::memcpy(A, a, sizeof(A));
+            } else if (d.type == D_RIGID) {
+                continue;
+            } else {
+                affine = false;
+                break;
+            }
+            double N[9];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++)
+                    N[3 * r + c] = A[3 * r] * J[c] + A[3 * r + 1] * J[3 + c] + A[3 * r + 2] * J[6 + c];
+            std::memcpy(J, N, sizeof(J));
+        }
+        double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+        // smallest singular value >= |det| / lip^2: keep 1/|u| finite and modest
+        fs.affine = affine && std::isfinite(det) && std::fabs(det) > 1e-6 * lip * lip;
+        double span = 2.0 * T + 1.0;
+        fs.ray_slack = fs.margin_slack + 4.0 * (8.0 * (double)(hs.defs.size() + 2) + 32.0) * kU * lip * span;
+    }
     Flattener F{hs, fs, hierarchical, {}};
     Flattener::Info info;
     fs.root = F.node(hs.root, E, P, 0, info);
@@ -1326,6 +1426,8 @@ HostPrepared prepare_host(const HostScene& hs, int res, int integration, double 
     }
     S.inv_lip = (float)(1.0 / hp.fs.def_lip) * (1.0f - 1e-6f);
     S.m_slack = (float)hp.fs.margin_slack;
+    S.affine = hp.fs.affine ? 1 : 0;
+    S.ray_slack = (float)hp.fs.ray_slack;
     memset(&hp.P, 0, sizeof(hp.P));
     hp.P.res = res;
     hp.P.flat_field = (float)flat_field;

@@ -83,6 +83,8 @@ struct FlatScene {
     int depth = 0;                // deepest tessellation nesting (0: none)
     double def_lip = 1.0;         // Lipschitz bound of the deformation chain
     double margin_slack = 0.0;    // error allowance of certificate radii (deformed units)
+    bool affine = true;           // deformation chain affine and invertible (ray certificates)
+    double ray_slack = 0.0;       // capsule radius of ray certificates (deformed units)
 };
 
 FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical);

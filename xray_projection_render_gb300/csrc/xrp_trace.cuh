@@ -1,0 +1,38 @@
+// xrp_trace.cuh -- launch helpers of certificate tracing (k_trace in
+// xrp_proposal.cuh), instantiated per certificate kind in
+// xrp_kern_trace.cu (balls) and xrp_kern_trace_ray.cu (ray bounds).
+#pragma once
+#include "xrp_launch.h"
+
+namespace xrp {
+
+template <int DEPTH, bool DEFS, bool RAY>
+cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                    cudaStream_t st) {
+    const int tpr = (pr.P.res + 15) / 16;
+    long blocks = (long)nviews * tpr * tpr;
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
+    if (pr.L.hierarchical)
+        k_trace<DEPTH, DEFS, true, RAY><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
+                                                                         nviews, Q, dout);
+    else
+        k_trace<DEPTH, DEFS, false, RAY><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
+                                                                          nviews, Q, dout);
+    return cudaGetLastError();
+}
+
+template <bool RAY>
+cudaError_t launch_trace_mode(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                              cudaStream_t st) {
+    if (pr.defs) {
+        if (pr.depth == 0) return trace_r<0, true, RAY>(pr, view0, nviews, Q, dout, st);
+        if (pr.depth == 1) return trace_r<1, true, RAY>(pr, view0, nviews, Q, dout, st);
+        return trace_r<3, true, RAY>(pr, view0, nviews, Q, dout, st);
+    }
+    if (pr.depth == 0) return trace_r<0, false, RAY>(pr, view0, nviews, Q, dout, st);
+    if (pr.depth == 1) return trace_r<1, false, RAY>(pr, view0, nviews, Q, dout, st);
+    return trace_r<3, false, RAY>(pr, view0, nviews, Q, dout, st);
+}
+
+}  // namespace xrp

@@ -188,7 +188,9 @@ def finish_images(images, transparency=False, stream=None):
 class Batch:
     """Many scenes rendered in one persistent, autotuned launch captured in a
     CUDA graph (xrp_batch_create).  ``items``: (scene, angles, resolution)
-    triples; every item shares ds, R, fov and the other options."""
+    triples; every item shares ds, R, fov and the other options.  ``trace``:
+    True for certificate tracing (ray bounds when every scene's chain is
+    affine), "ball" for ball certificates only."""
 
     def __init__(self, items, *, ds, R=4.0, fov=40.0, flat_field=0.0, density_multiplier=1.0,
                  integration="simple", autotune=True, trace=False):
@@ -204,6 +206,8 @@ class Batch:
         o = _opts(items[0][2], ds, R, flat_field, density_multiplier, integration, False)
         if trace:
             o.flags |= _lib.XRP_FLAG_TRACE
+            if trace == "ball":
+                o.flags |= _lib.XRP_FLAG_BALL
         h = ctypes.c_void_p()
         check(L.xrp_batch_create(arr, len(items), ctypes.byref(o), 1 if autotune else 0,
                                  ctypes.byref(h)), "xrp_batch_create")
@@ -309,7 +313,9 @@ def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resoluti
     """Render with the proposal march (xrp_render_proposal).  ``proposal``
     None: no network (every candidate refined, or integrated densely with
     ``refine=False``; ``trace=True``: per-ray certificate tracing, either
-    ``integration``; the segment march needs "simple").  Host path
+    ``integration``, with ray bounds where the deformation chain is affine
+    (``trace="ball"``: ball certificates only); the segment march needs
+    "simple").  Host path
     returns a float32 array [views, res, res]
     (with ``stats``: (images, dict)); a contiguous float32 CUDA tensor as
     ``out`` selects the device path."""
@@ -320,6 +326,8 @@ def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resoluti
         o.flags |= _lib.XRP_FLAG_NO_REFINE
     if trace:
         o.flags |= _lib.XRP_FLAG_TRACE
+        if trace == "ball":
+            o.flags |= _lib.XRP_FLAG_BALL
     ph = proposal.handle if proposal is not None else None
     if out is not None and _is_torch_cuda(out):
         import torch
