@@ -146,7 +146,7 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
             if (dirs && S.affine) {
                 float d[3] = {(float)dirs[3 * q], (float)dirs[3 * q + 1], (float)dirs[3 * q + 2]};
                 RayDir u = ray_dir32(S, d);
-                rho3_out[q] = dens_ray32<kMaxDepth, true>(S, x, y, z, u, t_out[q]);
+                rho3_out[q] = dens_ray32<kMaxDepth, true>(S, x, y, z, u, kFar, t_out[q]);
             }
         }
         if (affine_out) *affine_out = S.affine;

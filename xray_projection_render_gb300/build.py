@@ -36,7 +36,7 @@ def _nvcc():
 
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
-            if f.endswith((".cu", ".cpp", ".h"))] + [os.path.join(INCLUDE, "xrp.h")]
+            if f.endswith((".cu", ".cuh", ".cpp", ".h"))] + [os.path.join(INCLUDE, "xrp.h")]
 
 
 def _stale(target):

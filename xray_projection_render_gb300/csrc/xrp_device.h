@@ -850,6 +850,18 @@ XRP_HD float frsqrt(float x) {
 #endif
 }
 
+// Square root of the crossing arithmetic (relative error within 2^-23 on
+// the device; the bounds that use it budget for it).
+XRP_HD float fsqrt(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return sqrtf(x);
+#endif
+}
+
 // A direction component this small counts as zero (the slab is parallel).
 XRP_HD float rcp_dir(float d) { return fabsf(d) > 1e-30f ? frcp(d) : 0.0f; }
 
@@ -915,8 +927,8 @@ XRP_HD bool chord_interval(float a, float b, float c2, float wl1, float R, float
     const float tc = -b * ia;
     const float Rt = R - 0.5f * eps;
     if (!(h2 < Rt * Rt)) return false;
-    const float ch = sqrtf(fmaf(R, R, -h2));
-    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * wl1);
+    const float ch = fsqrt(fmaf(R, R, -h2));
+    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
     const float il = frsqrt(a);
     tlo = tc - (ch + err) * il;
     thi = tc + (ch + err) * il;
@@ -927,8 +939,8 @@ XRP_HD float chord_exit(float a, float b, float c2, float wl1, float R) {
     const float ia = frcp(a);
     const float h2 = c2 * ia;
     const float tc = -b * ia;
-    const float ch = sqrtf(fmaxf(fmaf(R, R, -h2), 0.0f));
-    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * wl1);
+    const float ch = fsqrt(fmaxf(fmaf(R, R, -h2), 0.0f));
+    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
     return tc + (ch - err) * frsqrt(a);  // -inf when ch == 0: the caller's ball bound holds
 }
 
@@ -936,11 +948,12 @@ XRP_HD float chord_exit(float a, float b, float c2, float wl1, float R) {
 // minimum, so that a NaN (never expected) can only shorten a jump.
 
 // Sphere of radius r, point w from the centre at signed distance g.
-XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const RayDir& u) {
+XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const RayDir& u, float tcap) {
     const float eps = u.eps;
     const float ag = fabsf(g) - eps;
     if (!(ag > 0.0f)) return 0.0f;
     const float tb = ag * u.il;
+    if (tb >= tcap) return tb;  // cannot lower the caller's minimum
     const float b = fmaf(wz, u.z, fmaf(wy, u.y, wx * u.x));
     const float cx = fmaf(wy, u.z, -wz * u.y), cy = fmaf(wz, u.x, -wx * u.z), cz = fmaf(wx, u.y, -wy * u.x);
     const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
@@ -956,44 +969,65 @@ XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const Ra
 
 // Finite cylinder: w from p0, axial fraction c, perpendicular part p, radial
 // and axial signed distances gr, ga (negative inside).
+// Inside (g < -eps) the bound is the exit of the cylinder shrunk by eps,
+// outside (g > eps) the entry of the cylinder inflated by eps: the axial
+// slab and the radial chord are intervals of t either way, so both cases run
+// the same straight-line code (lanes of a warp inside and outside struts do
+// not diverge).
 XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, float gr, float ga,
-                     const RayDir& u) {
+                     const RayDir& u, float tcap) {
     const float eps = u.eps;
     const float g = fmaxf(gr, ga);
     if (!(fabsf(g) > eps)) return 0.0f;
     const float tb = (fabsf(g) - eps) * u.il;
+    if (tb >= tcap) return tb;  // cannot lower the caller's minimum
+    const bool in = g < 0.0f;
+    const float sg = in ? -1.0f : 1.0f;
+    // axial: c + cu t inside (-es, 1 + es), es = +-(eps / |v| + band of c)
     const float cu = fmaf(u.z, f[5], fmaf(u.y, f[4], u.x * f[3])) * f[6];
+    const float icu = rcp_dir(cu);
+    const float es = sg * fmaf(eps, f[9] * f[6], f[F_BAND2]);
+    float alo = -kFar, ahi = kFar;
+    if (icu != 0.0f) {
+        const float a1 = (-es - c) * icu, a2 = (1.0f + es - c) * icu;
+        alo = fminf(a1, a2);
+        ahi = fmaxf(a1, a2);
+    } else if (!in && !(c > -es && c < 1.0f + es)) {
+        alo = kFar;
+    }
+    // radial: the line's projection against the disc of radius r +- eps
     const float qx = fmaf(-cu, f[3], u.x), qy = fmaf(-cu, f[4], u.y), qz = fmaf(-cu, f[5], u.z);
     const float a = fmaf(qz, qz, fmaf(qy, qy, qx * qx));
-    const bool chord = a > 1e-12f * u.a;  // not parallel to the axis
-    float b = 0.0f, c2 = 0.0f;
-    if (chord) {
-        b = fmaf(pz, qz, fmaf(py, qy, px * qx));
+    float rlo = -kFar, rhi = kFar;
+    if (a > 1e-12f * u.a) {
+        const float b = fmaf(pz, qz, fmaf(py, qy, px * qx));
         const float cx = fmaf(py, qz, -pz * qy), cy = fmaf(pz, qx, -px * qz), cz = fmaf(px, qy, -py * qx);
-        c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+        const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+        const float wl1 = fabsf(px) + fabsf(py) + fabsf(pz);
+        const float R = fmaf(sg, eps, f[8]);
+        const float ia = frcp(a);
+        const float h2 = c2 * ia;
+        const float tc = -b * ia;
+        const float ch = fsqrt(fmaxf(fmaf(R, R, -h2), 0.0f));
+        const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
+        const float half = fmaf(sg, err, ch) * frsqrt(a);  // widened outside, shrunk inside
+        rlo = tc - half;
+        rhi = tc + half;
+        // outside, a line within eps/2 of tangency never reaches the true disc
+        const float Rt = R - 0.5f * eps;
+        if (!in && !(h2 < Rt * Rt)) rlo = kFar;
+    } else if (a > 0.0f) {  // nearly parallel to the axis: the radius changes at rate |u_perp|
+        const float tr = (fabsf(gr) - eps) * frsqrt(a);
+        if (in) rhi = tr;
+        else if (gr > eps) rlo = tr;
+    } else if (!in && gr > eps) {
+        rlo = kFar;
     }
-    const float wl1 = fabsf(px) + fabsf(py) + fabsf(pz);
-    const float r = f[8];
-    const float ec = fmaf(eps, f[9] * f[6], f[F_BAND2]);  // eps / |v| + band of c
     float t;
-    if (g < 0.0f) {
-        float tr = chord ? fmaxf(chord_exit(a, b, c2, wl1, r - eps), 0.0f)
-                         : (a > 0.0f ? (-gr - eps) * frsqrt(a) : kFar);
-        t = fminf(fmaxf(slab_exit(c, rcp_dir(cu), 0.0f, 1.0f, ec), 0.0f), tr);
+    if (in) {
+        t = fminf(ahi, rhi);
     } else {
-        float lo = 0.0f, hi = kFar;
-        slab_clip(c, rcp_dir(cu), 0.0f, 1.0f, ec, lo, hi);
-        if (chord) {
-            float rlo, rhi;
-            if (chord_interval(a, b, c2, wl1, r + eps, eps, rlo, rhi)) {
-                lo = fmaxf(lo, rlo);
-                hi = fminf(hi, rhi);
-            } else {
-                lo = kFar;
-            }
-        } else if (gr > eps) {
-            lo = fmaxf(lo, a > 0.0f ? (gr - eps) * frsqrt(a) : kFar);
-        }
+        const float lo = fmaxf(fmaxf(alo, rlo), 0.0f), hi = fminf(ahi, rhi);
         t = lo <= hi ? lo : kFar;
     }
     return fmaxf(fmaxf(t, 0.0f), tb);
@@ -1018,14 +1052,16 @@ XRP_HD float box_ray(const float* h, float wx, float wy, float wz, float mn, flo
     return 0.0f;
 }
 
-// Leaf density (leaf_dm's decisions) and its ray bound t.
-XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, float& t) {
+// Leaf density (leaf_dm's decisions) and its ray bound t.  `tcap`: the
+// caller's current minimum; a bound at or above it may be returned without
+// its exact value (it cannot lower the minimum).
+XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, float tcap, float& t) {
     const float* f = n.f;
     switch (n.type) {
     case N_SPHERE: {
         float dx = x - f[0], dy = y - f[1], dz = z - f[2];
         float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        t = sphere_ray(dx, dy, dz, sqrtf(d2) - f[4], f[4], u);
+        t = sphere_ray(dx, dy, dz, fsqrt(d2) - f[4], f[4], u, tcap);
         float q = d2 - f[3];
         if (q < -f[F_BAND]) return f[F_RHO];
         if (q > f[F_BAND]) return 0.0f;
@@ -1045,7 +1081,7 @@ XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, 
         float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
         float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
         float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
-        t = cyl_ray(f, c, px, py, pz, sqrtf(p2) - f[8], fmaxf(-c, c - 1.0f) * f[9], u);
+        t = cyl_ray(f, c, px, py, pz, fsqrt(p2) - f[8], fmaxf(-c, c - 1.0f) * f[9], u, tcap);
         float bc = f[F_BAND2];
         if (c < -bc || c > 1.0f + bc) return 0.0f;
         float q = p2 - f[7];
@@ -1115,14 +1151,16 @@ XRP_HD float bounds_ray(const float* b, float x, float y, float z, float in, flo
 }
 
 template <int D>
-XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float& t);
+XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float tcap,
+                     float& t);
 
 // item_dm's decisions; t: the ray bound (tessellations: the outer bounds,
 // the cell faces of the fold and the unit-cell bounds cap the collection's).
 template <int D>
-XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const RayDir& u, float& t) {
+XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const RayDir& u, float tcap,
+                     float& t) {
     const Node& n = S.nodes[id];
-    if (n.type <= N_GYROID) return leaf_dr(n, x, y, z, u, t);
+    if (n.type <= N_GYROID) return leaf_dr(n, x, y, z, u, tcap, t);
     if (n.type == N_TESS) {
         if constexpr (D > 0) {
             const float* f = n.f;
@@ -1150,7 +1188,8 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
             if (mu < -f[13]) { t = fminf(tt, tu); return 0.0f; }  // outside the unit-cell bounds
             if (!(mu > f[13])) { t = 0.0f; return xnan(); }
             float tk;
-            float r = coll_dr<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tk);
+            const float tm = fminf(fminf(tt, tu), tcap);
+            float r = coll_dr<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tm, tk);
             t = fminf(fminf(tt, tu), tk);
             return r;
         }
@@ -1164,7 +1203,8 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
 // candidate lists) by the later of the exit from the point's list cell and
 // the clearance of the unlisted children.
 template <int D>
-XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float& t) {
+XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float tcap,
+                     float& t) {
     const int32_t* kids = S.child + c.a;
     int cnt = c.b;
     const int32_t* list = nullptr;
@@ -1204,7 +1244,7 @@ XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z
     for (int k = 0; k < cnt; k++) {
         int slot = list ? list[k] : k;
         float tk;
-        float r = item_dr<D>(S, kids[slot], x, y, z, u, tk);
+        float r = item_dr<D>(S, kids[slot], x, y, z, u, fminf(t, tcap), tk);
         t = fminf(t, tk);
         if (done) continue;  // greedy value fixed; bounds of the rest still count
         if (isunc(r)) {
@@ -1229,15 +1269,16 @@ XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z
 }
 
 // density32 at one point and the ray bound t (ray parameter units) of the
-// samples ahead that share its density; affine chains only.
+// samples ahead that share its density; affine chains only.  Bounds at or
+// above `tcap` (the end of the caller's range) need not be exact.
 template <int DEPTH, bool DEFS>
-XRP_HD float dens_ray32(const SceneDev& S, float x, float y, float z, const RayDir& u, float& t) {
+XRP_HD float dens_ray32(const SceneDev& S, float x, float y, float z, const RayDir& u, float tcap, float& t) {
     if constexpr (DEFS) deform32(S, x, y, z);
     const Node& r = S.nodes[S.root];
     float rho;
-    if (r.type <= N_GYROID) rho = leaf_dr(r, x, y, z, u, t);
-    else if (r.type == N_COLL) rho = coll_dr<DEPTH>(S, r, x, y, z, u, t);
-    else rho = item_dr<DEPTH>(S, S.root, x, y, z, u, t);
+    if (r.type <= N_GYROID) rho = leaf_dr(r, x, y, z, u, tcap, t);
+    else if (r.type == N_COLL) rho = coll_dr<DEPTH>(S, r, x, y, z, u, tcap, t);
+    else rho = item_dr<DEPTH>(S, S.root, x, y, z, u, tcap, t);
     t = fmaxf(t, 0.0f) * 0.99999f;
     return rho;
 }
@@ -1944,6 +1985,7 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
                        unsigned& evals) {
     KahanF acc;
     const float step = L.ds32 * 1.00001f;  // world distance between samples, rounded up
+    const float istep = (1.0f / step) * 0.999999f;  // rounded down
     RayDir u;
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     int k = k0;
@@ -1954,7 +1996,7 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
         const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
         float m;
         float rho;
-        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, m);
+        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         if (isunc(rho)) {
@@ -1962,7 +2004,7 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
             k++;
             continue;
         }
-        const int jmp = (int)fminf(floorf(m / step), (float)(k1 - k));
+        const int jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
         acc.add(rho * (float)(jmp + 1));
         k += jmp + 1;
     }
@@ -1982,6 +2024,7 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
                             unsigned& evals) {
     KahanF acc;
     const float step = L.ds32 * 1.00001f;
+    const float istep = (1.0f / step) * 0.999999f;  // rounded down
     RayDir u;
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     bool prev_zero = true;  // coarse samples before k0 are outside the support
@@ -1993,14 +2036,14 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
         const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
         float m;
         float rho;
-        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, m);
+        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         int jmp = 0;
         if (isunc(rho)) {
             rho = unc(k, false);
         } else {
-            jmp = (int)fminf(floorf(m / step), (float)(k1 - k));
+            jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
         }
         const bool zero = (rho == 0.0f);
         if (zero != prev_zero) {

@@ -1576,8 +1576,12 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     // list of samples for FP64 re-evaluation (per launch of at most
     // pl.max_rays rays; reused): four entries per ray (the deformed lattice
     // leaves about one undecided sample per ray; an overflow costs a plain
-    // re-render of the whole call)
-    const unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, pl.max_rays * 4);
+    // re-render of the whole call).  The hierarchical integrator refines
+    // every boundary crossing into ten fine samples next to the boundary,
+    // where undecided samples gather (several per ray on the lattice): the
+    // same list for a quarter of the rays, sixteen entries per ray.
+    if (o->integration == XRP_INTEGRATE_HIERARCHICAL) pl.max_rays = 1LL << 21;
+    const unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, (1LL << 23) * 4);
     PoolBuf fb, fbc;
     if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
         (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)
