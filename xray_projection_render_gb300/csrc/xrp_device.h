@@ -911,38 +911,16 @@ XRP_HD void slab_clip(float q, float idq, float lo, float hi, float e, float& tl
     }
 }
 
-// Line w + u t against a ball (3-D) or a disc (the projection of a
-// cylinder) of radius R about the origin: from the closest approach
-// tc = -b/a and the half chord sqrt(R^2 - h^2), h^2 = c2/a the squared
-// distance of the line from the origin (c2 = |w x u|^2, stable near
-// tangency).  `err` bounds the FP32 error of the half chord (large only
-// when the line is nearly tangent; a line within eps/2 of tangency to the
-// inflated ball stays clear of the true one).  Outside (R = r + eps):
-// returns the entry interval widened by the error, or false when the line
-// never enters.  Inside (R = r - eps): chord_exit is the shrunk exit.
-XRP_HD bool chord_interval(float a, float b, float c2, float wl1, float R, float eps, float& tlo,
-                           float& thi) {
-    const float ia = frcp(a);
-    const float h2 = c2 * ia;
-    const float tc = -b * ia;
-    const float Rt = R - 0.5f * eps;
-    if (!(h2 < Rt * Rt)) return false;
-    const float ch = fsqrt(fmaf(R, R, -h2));
-    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
-    const float il = frsqrt(a);
-    tlo = tc - (ch + err) * il;
-    thi = tc + (ch + err) * il;
-    return true;
-}
-
-XRP_HD float chord_exit(float a, float b, float c2, float wl1, float R) {
-    const float ia = frcp(a);
-    const float h2 = c2 * ia;
-    const float tc = -b * ia;
-    const float ch = fsqrt(fmaxf(fmaf(R, R, -h2), 0.0f));
-    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
-    return tc + (ch - err) * frsqrt(a);  // -inf when ch == 0: the caller's ball bound holds
-}
+// Spheres and cylinders: the line w + u t against a ball (3-D) or a disc
+// (the projection of a cylinder across its axis) of radius R about the
+// origin, from the closest approach tc = -b/a and the half chord
+// sqrt(R^2 - h^2), h^2 = c2/a the squared distance of the line from the
+// origin (c2 = |w x u|^2, stable near tangency).  `err` bounds the FP32
+// error of the half chord (large only when the line is nearly tangent, where
+// the ball bound takes over); a line within eps/2 of tangency to the
+// inflated ball stays clear of the true one.  Outside, R = r + eps and the
+// entry interval is widened by err; inside, R = r - eps and the exit is
+// shrunk by it.
 
 // Every partial bound below is clamped with fmaxf(., 0) before it enters a
 // minimum, so that a NaN (never expected) can only shorten a jump.
@@ -954,17 +932,27 @@ XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const Ra
     if (!(ag > 0.0f)) return 0.0f;
     const float tb = ag * u.il;
     if (tb >= tcap) return tb;  // cannot lower the caller's minimum
+    // inside: exit of the ball shrunk by eps; outside: entry of the ball
+    // inflated by eps (one straight-line computation for both)
+    const bool in = g < 0.0f;
+    const float sg = in ? -1.0f : 1.0f;
     const float b = fmaf(wz, u.z, fmaf(wy, u.y, wx * u.x));
     const float cx = fmaf(wy, u.z, -wz * u.y), cy = fmaf(wz, u.x, -wx * u.z), cz = fmaf(wx, u.y, -wy * u.x);
     const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
     const float wl1 = fabsf(wx) + fabsf(wy) + fabsf(wz);
-    if (g > 0.0f) {
-        if (!(b < 0.0f)) return kFar;  // moving away: the distance only grows
-        float lo, hi;
-        if (!chord_interval(u.a, b, c2, wl1, r + eps, eps, lo, hi)) return kFar;
-        return fmaxf(tb, lo);
-    }
-    return fmaxf(tb, chord_exit(u.a, b, c2, wl1, r - eps));
+    const float R = fmaf(sg, eps, r);
+    const float ia = u.il * u.il;
+    const float h2 = c2 * ia;
+    const float tc = -b * ia;
+    const float ch = fsqrt(fmaxf(fmaf(R, R, -h2), 0.0f));
+    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
+    const float half = fmaf(sg, err, ch) * u.il;  // widened outside, shrunk inside
+    float t = in ? tc + half : tc - half;
+    // outside: moving away (the distance only grows), or within eps/2 of
+    // tangency (never reaches the true ball)
+    const float Rt = R - 0.5f * eps;
+    if (!in && (!(b < 0.0f) || !(h2 < Rt * Rt))) t = kFar;
+    return fmaxf(t, tb);
 }
 
 // Finite cylinder: w from p0, axial fraction c, perpendicular part p, radial
@@ -1037,19 +1025,16 @@ XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, floa
 // mn = min(h - |w|).
 XRP_HD float box_ray(const float* h, float wx, float wy, float wz, float mn, float b, const RayDir& u) {
     const float e = u.eps + b;
-    if (mn > e) {
-        float t = fminf(fminf(slab_exit(wx, u.ix, -h[0], h[0], e), slab_exit(wy, u.iy, -h[1], h[1], e)),
-                        slab_exit(wz, u.iz, -h[2], h[2], e));
-        return fmaxf(t, 0.0f);
-    }
-    if (mn < -e) {
-        float lo = 0.0f, hi = kFar;
-        slab_clip(wx, u.ix, -h[0], h[0], e, lo, hi);
-        slab_clip(wy, u.iy, -h[1], h[1], e, lo, hi);
-        slab_clip(wz, u.iz, -h[2], h[2], e, lo, hi);
-        return lo <= hi ? fmaxf(lo, 0.0f) : kFar;
-    }
-    return 0.0f;
+    if (!(fabsf(mn) > e)) return 0.0f;
+    // inside: exit of the box shrunk by e; outside: entry of the box
+    // inflated by e
+    const bool in = mn > 0.0f;
+    const float es = in ? -e : e;
+    float lo = 0.0f, hi = kFar;
+    slab_clip(wx, u.ix, -h[0], h[0], es, lo, hi);
+    slab_clip(wy, u.iy, -h[1], h[1], es, lo, hi);
+    slab_clip(wz, u.iz, -h[2], h[2], es, lo, hi);
+    return in ? fmaxf(hi, 0.0f) : (lo <= hi ? lo : kFar);
 }
 
 // Leaf density (leaf_dm's decisions) and its ray bound t.  `tcap`: the
@@ -1093,21 +1078,29 @@ XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, 
     case N_PPD: {
         float wx = x - f[0], wy = y - f[1], wz = z - f[2];
         float b = f[F_BAND];
-        float mn = 3.0e38f, tin = kFar, lo = 0.0f, hi = kFar;
+        float q[3], iqu[3], e[3];
+        float mn = 3.0e38f, mrel = 3.0e38f;
         bool out = false;
         for (int a = 0; a < 3; a++) {
             const float* r = f + 3 + 3 * a;
-            float q = fmaf(r[2], wz, fmaf(r[1], wy, r[0] * wx));
-            float iqu = rcp_dir(fmaf(r[2], u.z, fmaf(r[1], u.y, r[0] * u.x)));
-            float e = fmaf(u.eps, f[12 + a], b);
-            float in = fminf(q, 1.0f - q);
+            q[a] = fmaf(r[2], wz, fmaf(r[1], wy, r[0] * wx));
+            iqu[a] = rcp_dir(fmaf(r[2], u.z, fmaf(r[1], u.y, r[0] * u.x)));
+            e[a] = fmaf(u.eps, f[12 + a], b);
+            float in = fminf(q[a], 1.0f - q[a]);
             mn = fminf(mn, in);
-            out = out || in < -e;
-            tin = fminf(tin, fmaxf(slab_exit(q, iqu, 0.0f, 1.0f, e), 0.0f));
-            if (!(in > e)) tin = 0.0f;
-            slab_clip(q, iqu, 0.0f, 1.0f, e, lo, hi);
+            mrel = fminf(mrel, in - e[a]);
+            out = out || in < -e[a];
         }
-        t = out ? (lo <= hi ? fmaxf(lo, 0.0f) : kFar) : tin;
+        // inside (every slab at least e inside): exit of the shrunk slabs;
+        // outside (some slab more than e outside): entry of the inflated
+        // ones; else 0
+        if (out || mrel > 0.0f) {
+            float lo = 0.0f, hi = kFar;
+            for (int a = 0; a < 3; a++) slab_clip(q[a], iqu[a], 0.0f, 1.0f, out ? e[a] : -e[a], lo, hi);
+            t = out ? (lo <= hi ? lo : kFar) : fmaxf(hi, 0.0f);
+        } else {
+            t = 0.0f;
+        }
         if (mn > b) return f[F_RHO];
         if (mn < -b) return 0.0f;
         return xnan();
@@ -1135,19 +1128,14 @@ XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, 
 // for a point more than e outside, else 0.  `in` is the point's smallest
 // distance to a face (negative outside).
 XRP_HD float bounds_ray(const float* b, float x, float y, float z, float in, float e, const RayDir& u) {
-    if (in > e) {
-        float t = fminf(fminf(slab_exit(x, u.ix, b[0], b[1], e), slab_exit(y, u.iy, b[2], b[3], e)),
-                        slab_exit(z, u.iz, b[4], b[5], e));
-        return fmaxf(t, 0.0f);
-    }
-    if (in < -e) {
-        float lo = 0.0f, hi = kFar;
-        slab_clip(x, u.ix, b[0], b[1], e, lo, hi);
-        slab_clip(y, u.iy, b[2], b[3], e, lo, hi);
-        slab_clip(z, u.iz, b[4], b[5], e, lo, hi);
-        return lo <= hi ? fmaxf(lo, 0.0f) : kFar;
-    }
-    return 0.0f;
+    if (!(fabsf(in) > e)) return 0.0f;
+    const bool inside = in > 0.0f;
+    const float es = inside ? -e : e;
+    float lo = 0.0f, hi = kFar;
+    slab_clip(x, u.ix, b[0], b[1], es, lo, hi);
+    slab_clip(y, u.iy, b[2], b[3], es, lo, hi);
+    slab_clip(z, u.iz, b[4], b[5], es, lo, hi);
+    return inside ? fmaxf(hi, 0.0f) : (lo <= hi ? lo : kFar);
 }
 
 template <int D>
@@ -1626,6 +1614,40 @@ XRP_HD void setup_ray64(const ViewDev& V, const double* xs, int i, int j, Ray64&
     r.o[2] = V.eye[2];
 }
 
+// The ray of pixel (i, j) for the FP32 march: the direction to ~1e-13
+// relative rather than in the reference's operation order.  An FP32
+// reciprocal square root refined by one Newton step in FP64 replaces the
+// FP64 square root and division (long instruction sequences on a GPU whose
+// FP64 rate is a small fraction of FP32).  The positions it gives differ
+// from the reference's by under 1e-12, inside the absolute term of the
+// FP32 position error bound; the FP64 re-evaluation of undecided samples
+// keeps setup_ray64.
+XRP_HD void setup_ray64_fast(const ViewDev& V, const double* xs, int i, int j, Ray64& r) {
+    const double v0 = xs[i], v1 = xs[j], v2 = -V.f;
+    const double* m = V.m;
+    const double t0 = fma(m[8], v2, fma(m[4], v1, fma(m[0], v0, m[12])));
+    const double t1 = fma(m[9], v2, fma(m[5], v1, fma(m[1], v0, m[13])));
+    const double t2 = fma(m[10], v2, fma(m[6], v1, fma(m[2], v0, m[14])));
+    double iw = V.inv_w;
+    if (V.general_w) iw = 1.0 / fma(m[11], v2, fma(m[7], v1, fma(m[3], v0, m[15])));
+    const double dx = fma(t0, iw, -V.eye[0]);
+    const double dy = fma(t1, iw, -V.eye[1]);
+    const double dz = fma(t2, iw, -V.eye[2]);
+    const double dd = fma(dz, dz, fma(dy, dy, dx * dx));
+#if defined(__CUDA_ARCH__)
+    double y = (double)rsqrtf((float)dd);
+#else
+    double y = (double)(1.0f / sqrtf((float)dd));
+#endif
+    y = y * fma(-0.5 * dd * y, y, 1.5);  // Newton: relative error ~1.5 e0^2
+    r.d[0] = dx * y;
+    r.d[1] = dy * y;
+    r.d[2] = dz * y;
+    r.o[0] = V.eye[0];
+    r.o[1] = V.eye[1];
+    r.o[2] = V.eye[2];
+}
+
 XRP_HD void setup_ray32(const Ray64& r64, double s_c, Ray& r) {
     for (int a = 0; a < 3; a++) {
         r.pc[a] = (float)fma(r64.d[a], s_c, r64.o[a]);
@@ -2075,7 +2097,7 @@ XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams
     Ray r;
     {
         Ray64 r64;
-        setup_ray64(V, P.xs, i, j, r64);
+        setup_ray64_fast(V, P.xs, i, j, r64);
         setup_ray32(r64, L.s_c, r);
     }
     float t0, t1;
@@ -2114,7 +2136,7 @@ XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParam
         VolRay vr;
         {
             Ray64 r64;
-            setup_ray64(V, P.xs, i, j, r64);
+            setup_ray64_fast(V, P.xs, i, j, r64);
             setup_ray32(r64, L.s_c, r);
             setup_volray(vol, r64, L.s_c, vr);
         }
@@ -2126,7 +2148,7 @@ XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParam
     } else {
         {
             Ray64 r64;
-            setup_ray64(V, P.xs, i, j, r64);
+            setup_ray64_fast(V, P.xs, i, j, r64);
             setup_ray32(r64, L.s_c, r);
         }
         SceneSampler<DEPTH, DEFS> smp{S, r, px};

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256, 4)
         VoxSampler<TEX> smp{Q, V, P.xs, {0, 0, 0}, {0, 0, 0}, i, j};
         {
             Ray64 r64;
-            setup_ray64(*V, P.xs, i, j, r64);
+            setup_ray64_fast(*V, P.xs, i, j, r64);
             setup_ray32(r64, L.s_c, r);
             for (int a = 0; a < 3; a++) {
                 double sc = (double)Q.scale[a];

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
         int my_k0 = 0, my_k1 = -1;
         if (rvalid) {
             Ray64 r64;
-            setup_ray64(views[v], P.xs, i, j, r64);
+            setup_ray64_fast(views[v], P.xs, i, j, r64);
             setup_ray32(r64, L.s_c, myray);
             float t0, t1;
             clip_ray(S.sup_lo, S.sup_hi, myray, t0, t1);
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
         Ray ray;
         {
             Ray64 r64;
-            setup_ray64(views[view0 + v], P.xs, i, j, r64);
+            setup_ray64_fast(views[view0 + v], P.xs, i, j, r64);
             setup_ray32(r64, L.s_c, ray);
         }
         float t0, t1;
