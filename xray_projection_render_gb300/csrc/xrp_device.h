@@ -19,6 +19,7 @@
 #pragma once
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define XRP_HD __host__ __device__ __forceinline__
@@ -106,7 +107,9 @@ enum CollFlags : int32_t {
 // Leaf parameter slots (Node.f).  RHO and BAND slots are shared by leaves.
 enum : int { F_RHO = 27, F_BAND = 26, F_BAND2 = 25 };
 
-struct Node {
+// 16-byte aligned so that a leaf's parameters load as 128-bit vectors
+// (f[0] sits at byte 16).
+struct alignas(16) Node {
     int32_t type;
     int32_t a;      // COLL: first slot in the child list; TESS: unit-cell collection node; VOXEL: volume id
     int32_t b;      // COLL: number of children
@@ -209,41 +212,62 @@ struct RenderParams {
     const double* xs;     // pixel coordinate table i/(res/2)-1, length res
 };
 
+// Four consecutive node parameters f[k..k+3], k a multiple of 4: one
+// 128-bit load on the device.
+struct alignas(16) F4 {
+    float x, y, z, w;
+};
+
+XRP_HD F4 ld4(const float* p) {
+#if defined(__CUDA_ARCH__)
+    return *reinterpret_cast<const F4*>(p);
+#else
+    F4 r;
+    memcpy(&r, p, sizeof(r));
+    return r;
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // FP32 guarded evaluation
 // ---------------------------------------------------------------------------
 // Returns the density (pre-multiplier) or NaN when a predicate is too close
 // to its decision boundary for FP32 to decide.
 
+// (f[24..27] holds F_BAND2, F_BAND, F_RHO: one vector load with the first.)
 XRP_HD float sphere32(const float* f, float x, float y, float z) {
-    float dx = x - f[0], dy = y - f[1], dz = z - f[2];
-    float m = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - f[3];
-    if (m < -f[F_BAND]) return f[F_RHO];
-    if (m > f[F_BAND]) return 0.0f;
+    const F4 a = ld4(f), t = ld4(f + 24);
+    float dx = x - a.x, dy = y - a.y, dz = z - a.z;
+    float m = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - a.w;
+    if (m < -t.z) return t.w;
+    if (m > t.z) return 0.0f;
     return xnan();
 }
 
 XRP_HD float box32(const float* f, float x, float y, float z) {
-    float mx = f[3] - fabsf(x - f[0]);
-    float my = f[4] - fabsf(y - f[1]);
-    float mz = f[5] - fabsf(z - f[2]);
-    float b = f[F_BAND];
+    const F4 a = ld4(f), c = ld4(f + 4), t = ld4(f + 24);
+    float mx = a.w - fabsf(x - a.x);
+    float my = c.x - fabsf(y - a.y);
+    float mz = c.y - fabsf(z - a.z);
+    float b = t.z;
     float mn = fminf(mx, fminf(my, mz));
-    if (mn > b) return f[F_RHO];
+    if (mn > b) return t.w;
     if (mn < -b) return 0.0f;
     return xnan();
 }
 
 XRP_HD float cyl32(const float* f, float x, float y, float z) {
-    float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-    float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
-    float bc = f[F_BAND2];
+    // a: p0, v.x; c: v.y, v.z, 1/|v|^2, r^2
+    const F4 a = ld4(f), c4 = ld4(f + 4), t = ld4(f + 24);
+    float wx = x - a.x, wy = y - a.y, wz = z - a.z;
+    float c = fmaf(wz, c4.y, fmaf(wy, c4.x, wx * a.w)) * c4.z;
+    float bc = t.y;
     if (c < -bc || c > 1.0f + bc) return 0.0f;
-    float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
-    float m = fmaf(pz, pz, fmaf(py, py, px * px)) - f[7];
-    float bd = f[F_BAND];
+    float px = fmaf(-c, a.w, wx), py = fmaf(-c, c4.x, wy), pz = fmaf(-c, c4.y, wz);
+    float m = fmaf(pz, pz, fmaf(py, py, px * px)) - c4.w;
+    float bd = t.z;
     if (m > bd) return 0.0f;
-    if (m < -bd && c > bc && c < 1.0f - bc) return f[F_RHO];
+    if (m < -bd && c > bc && c < 1.0f - bc) return t.w;
     return xnan();
 }
 
@@ -962,8 +986,9 @@ XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const Ra
 // slab and the radial chord are intervals of t either way, so both cases run
 // the same straight-line code (lanes of a warp inside and outside struts do
 // not diverge).
-XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, float gr, float ga,
-                     const RayDir& u, float tcap) {
+// v: the axis p1 - p0, ivv = 1/|v|^2, vl = |v|, bc: the band of c.
+XRP_HD float cyl_ray(float vx, float vy, float vz, float ivv, float r, float vl, float bc, float c,
+                     float px, float py, float pz, float gr, float ga, const RayDir& u, float tcap) {
     const float eps = u.eps;
     const float g = fmaxf(gr, ga);
     if (!(fabsf(g) > eps)) return 0.0f;
@@ -972,9 +997,9 @@ XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, floa
     const bool in = g < 0.0f;
     const float sg = in ? -1.0f : 1.0f;
     // axial: c + cu t inside (-es, 1 + es), es = +-(eps / |v| + band of c)
-    const float cu = fmaf(u.z, f[5], fmaf(u.y, f[4], u.x * f[3])) * f[6];
+    const float cu = fmaf(u.z, vz, fmaf(u.y, vy, u.x * vx)) * ivv;
     const float icu = rcp_dir(cu);
-    const float es = sg * fmaf(eps, f[9] * f[6], f[F_BAND2]);
+    const float es = sg * fmaf(eps, vl * ivv, bc);
     float alo = -kFar, ahi = kFar;
     if (icu != 0.0f) {
         const float a1 = (-es - c) * icu, a2 = (1.0f + es - c) * icu;
@@ -984,7 +1009,7 @@ XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, floa
         alo = kFar;
     }
     // radial: the line's projection against the disc of radius r +- eps
-    const float qx = fmaf(-cu, f[3], u.x), qy = fmaf(-cu, f[4], u.y), qz = fmaf(-cu, f[5], u.z);
+    const float qx = fmaf(-cu, vx, u.x), qy = fmaf(-cu, vy, u.y), qz = fmaf(-cu, vz, u.z);
     const float a = fmaf(qz, qz, fmaf(qy, qy, qx * qx));
     float rlo = -kFar, rhi = kFar;
     if (a > 1e-12f * u.a) {
@@ -992,7 +1017,7 @@ XRP_HD float cyl_ray(const float* f, float c, float px, float py, float pz, floa
         const float cx = fmaf(py, qz, -pz * qy), cy = fmaf(pz, qx, -px * qz), cz = fmaf(px, qy, -py * qx);
         const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
         const float wl1 = fabsf(px) + fabsf(py) + fabsf(pz);
-        const float R = fmaf(sg, eps, f[8]);
+        const float R = fmaf(sg, eps, r);
         const float ia = frcp(a);
         const float h2 = c2 * ia;
         const float tc = -b * ia;
@@ -1044,35 +1069,41 @@ XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, 
     const float* f = n.f;
     switch (n.type) {
     case N_SPHERE: {
-        float dx = x - f[0], dy = y - f[1], dz = z - f[2];
+        const F4 a = ld4(f), c4 = ld4(f + 4), tb = ld4(f + 24);  // centre, r^2; r; bands, rho
+        float dx = x - a.x, dy = y - a.y, dz = z - a.z;
         float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        t = sphere_ray(dx, dy, dz, fsqrt(d2) - f[4], f[4], u, tcap);
-        float q = d2 - f[3];
-        if (q < -f[F_BAND]) return f[F_RHO];
-        if (q > f[F_BAND]) return 0.0f;
+        t = sphere_ray(dx, dy, dz, fsqrt(d2) - c4.x, c4.x, u, tcap);
+        float q = d2 - a.w;
+        if (q < -tb.z) return tb.w;
+        if (q > tb.z) return 0.0f;
         return xnan();
     }
     case N_BOX: {
-        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-        float mn = fminf(f[3] - fabsf(wx), fminf(f[4] - fabsf(wy), f[5] - fabsf(wz)));
-        float b = f[F_BAND];
-        t = box_ray(f + 3, wx, wy, wz, mn, b, u);
-        if (mn > b) return f[F_RHO];
+        const F4 a = ld4(f), c4 = ld4(f + 4), tb = ld4(f + 24);  // centre, half sides; bands, rho
+        const float h[3] = {a.w, c4.x, c4.y};
+        float wx = x - a.x, wy = y - a.y, wz = z - a.z;
+        float mn = fminf(h[0] - fabsf(wx), fminf(h[1] - fabsf(wy), h[2] - fabsf(wz)));
+        float b = tb.z;
+        t = box_ray(h, wx, wy, wz, mn, b, u);
+        if (mn > b) return tb.w;
         if (mn < -b) return 0.0f;
         return xnan();
     }
     case N_CYL: {
-        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-        float c = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * f[6];
-        float px = fmaf(-c, f[3], wx), py = fmaf(-c, f[4], wy), pz = fmaf(-c, f[5], wz);
+        // a: p0, v.x; c4: v.y, v.z, 1/|v|^2, r^2; e: r, |v|; tb: bands, rho
+        const F4 a = ld4(f), c4 = ld4(f + 4), e = ld4(f + 8), tb = ld4(f + 24);
+        float wx = x - a.x, wy = y - a.y, wz = z - a.z;
+        float c = fmaf(wz, c4.y, fmaf(wy, c4.x, wx * a.w)) * c4.z;
+        float px = fmaf(-c, a.w, wx), py = fmaf(-c, c4.x, wy), pz = fmaf(-c, c4.y, wz);
         float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
-        t = cyl_ray(f, c, px, py, pz, fsqrt(p2) - f[8], fmaxf(-c, c - 1.0f) * f[9], u, tcap);
-        float bc = f[F_BAND2];
+        float bc = tb.y;
+        t = cyl_ray(a.w, c4.x, c4.y, c4.z, e.x, e.y, bc, c, px, py, pz, fsqrt(p2) - e.x,
+                    fmaxf(-c, c - 1.0f) * e.y, u, tcap);
         if (c < -bc || c > 1.0f + bc) return 0.0f;
-        float q = p2 - f[7];
-        float bd = f[F_BAND];
+        float q = p2 - c4.w;
+        float bd = tb.z;
         if (q > bd) return 0.0f;
-        if (q < -bd && c > bc && c < 1.0f - bc) return f[F_RHO];
+        if (q < -bd && c > bc && c < 1.0f - bc) return tb.w;
         return xnan();
     }
     case N_PPD: {
