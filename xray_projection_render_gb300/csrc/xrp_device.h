@@ -365,25 +365,29 @@ XRP_HD float item32(const SceneDev& S, int id, float x, float y, float z) {
     if (n.type == N_VOXEL) return voxel32(S.vols[n.a], n.f[0], x, y, z, S.hier_zero_guard);
     if (n.type == N_TESS) {
         if constexpr (D > 0) {
-            const float* f = n.f;
+            // f[0..5] outer bounds, f[6] their band, f[7..12] unit-cell
+            // bounds, f[13] their band, f[14..16] cell size, f[17..19] its
+            // reciprocal, f[20..22] unit-cell origin, f[23] fold band
+            const F4 f0 = ld4(n.f), f4 = ld4(n.f + 4), f8 = ld4(n.f + 8), f12 = ld4(n.f + 12);
+            const F4 f16 = ld4(n.f + 16), f20 = ld4(n.f + 20);
             // outer inclusive bounds (objects.go:570)
-            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
-                             fminf(z - f[4], f[5] - z));
-            if (mo < -f[6]) return 0.0f;
-            if (!(mo > f[6])) return xnan();
+            float mo = fminf(fminf(fminf(x - f0.x, f0.y - x), fminf(y - f0.z, f0.w - y)),
+                             fminf(z - f4.x, f4.y - z));
+            if (mo < -f4.z) return 0.0f;
+            if (!(mo > f4.z)) return xnan();
             // fold into the unit cell (objects.go:574-579)
-            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
+            float qx = (x - f20.x) * f16.y, qy = (y - f20.y) * f16.z, qz = (z - f20.z) * f16.w;
             float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
-            float bq = f[23];
+            float bq = f20.w;
             float fr = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)), fminf(qy - ny, 1.0f - (qy - ny))),
                              fminf(qz - nz, 1.0f - (qz - nz)));
             if (!(fr > bq)) return xnan();
-            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
+            float fx = fmaf(-f12.z, nx, x), fy = fmaf(-f12.w, ny, y), fz = fmaf(-f16.x, nz, z);
             // unit-cell inclusive bounds (objects.go:460)
-            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
-                             fminf(fz - f[11], f[12] - fz));
-            if (mu < -f[13]) return 0.0f;
-            if (!(mu > f[13])) return xnan();
+            float mu = fminf(fminf(fminf(fx - f4.w, f8.x - fx), fminf(fy - f8.y, f8.z - fy)),
+                             fminf(fz - f8.w, f12.x - fz));
+            if (mu < -f12.y) return 0.0f;
+            if (!(mu > f12.y)) return xnan();
             return coll32<D - 1>(S, S.nodes[n.a], fx, fy, fz);
         } else {
             return xnan();
@@ -400,13 +404,14 @@ XRP_HD float coll32(const SceneDev& S, const Node& c, float x, float y, float z)
     const int32_t* list = nullptr;
     if (c.flags & C_ACCEL) {
         int G = (c.flags >> 16) & 0xff;
-        int ix = (int)floorf((x - c.f[0]) * c.f[3]);
-        int iy = (int)floorf((y - c.f[1]) * c.f[4]);
-        int iz = (int)floorf((z - c.f[2]) * c.f[5]);
+        const F4 g0 = ld4(c.f), g4 = ld4(c.f + 4);  // grid origin, 1/cell size, cell base
+        int ix = (int)floorf((x - g0.x) * g0.w);
+        int iy = (int)floorf((y - g0.y) * g4.x);
+        int iz = (int)floorf((z - g0.z) * g4.y);
         ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
         iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
         iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
-        int cell_base = f2i(c.f[6]);
+        int cell_base = f2i(g4.z);
         const int32_t* off = S.cells + cell_base + (iz * G + iy) * G + ix;
         int s0 = off[0], s1 = off[1];
         list = S.items + s0;
@@ -1182,30 +1187,35 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
     if (n.type <= N_GYROID) return leaf_dr(n, x, y, z, u, tcap, t);
     if (n.type == N_TESS) {
         if constexpr (D > 0) {
-            const float* f = n.f;
-            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
-                             fminf(z - f[4], f[5] - z));
-            const float to = bounds_ray(f, x, y, z, mo, u.eps + f[6], u);
-            if (mo < -f[6]) { t = to; return 0.0f; }  // outside: zero up to the bounds
-            if (!(mo > f[6])) { t = 0.0f; return xnan(); }
-            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
+            // node layout as in item32
+            const F4 f0 = ld4(n.f), f4 = ld4(n.f + 4), f8 = ld4(n.f + 8), f12 = ld4(n.f + 12);
+            const F4 f16 = ld4(n.f + 16), f20 = ld4(n.f + 20);
+            const float ob[6] = {f0.x, f0.y, f0.z, f0.w, f4.x, f4.y};
+            const float ub[6] = {f4.w, f8.x, f8.y, f8.z, f8.w, f12.x};
+            float mo = fminf(fminf(fminf(x - ob[0], ob[1] - x), fminf(y - ob[2], ob[3] - y)),
+                             fminf(z - ob[4], ob[5] - z));
+            const float to = bounds_ray(ob, x, y, z, mo, u.eps + f4.z, u);
+            if (mo < -f4.z) { t = to; return 0.0f; }  // outside: zero up to the bounds
+            if (!(mo > f4.z)) { t = 0.0f; return xnan(); }
+            float qx = (x - f20.x) * f16.y, qy = (y - f20.y) * f16.z, qz = (z - f20.z) * f16.w;
             float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
-            float bq = f[23];
+            float bq = f20.w;
             float frx = qx - nx, fry = qy - ny, frz = qz - nz;
             float fr = fminf(fminf(fminf(frx, 1.0f - frx), fminf(fry, 1.0f - fry)), fminf(frz, 1.0f - frz));
             if (!(fr > bq)) { t = 0.0f; return xnan(); }
-            // exit of this tessellation cell (q units; eps scaled by 1/cell size)
-            // (1/(u f17) = (1/u) f14: f14 is the cell size, f17 its reciprocal)
-            float tc = fminf(fminf(fmaxf(slab_exit(frx, u.ix * f[14], 0.0f, 1.0f, fmaf(u.eps, fabsf(f[17]), bq)), 0.0f),
-                                   fmaxf(slab_exit(fry, u.iy * f[15], 0.0f, 1.0f, fmaf(u.eps, fabsf(f[18]), bq)), 0.0f)),
-                             fmaxf(slab_exit(frz, u.iz * f[16], 0.0f, 1.0f, fmaf(u.eps, fabsf(f[19]), bq)), 0.0f));
+            // exit of this tessellation cell (q units; eps scaled by 1/cell
+            // size; 1/(u f17) = (1/u) f14: f14 is the cell size, f17 its
+            // reciprocal)
+            float tc = fminf(fminf(fmaxf(slab_exit(frx, u.ix * f12.z, 0.0f, 1.0f, fmaf(u.eps, fabsf(f16.y), bq)), 0.0f),
+                                   fmaxf(slab_exit(fry, u.iy * f12.w, 0.0f, 1.0f, fmaf(u.eps, fabsf(f16.z), bq)), 0.0f)),
+                             fmaxf(slab_exit(frz, u.iz * f16.x, 0.0f, 1.0f, fmaf(u.eps, fabsf(f16.w), bq)), 0.0f));
             const float tt = fminf(to, tc);
-            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
-            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
-                             fminf(fz - f[11], f[12] - fz));
-            const float tu = bounds_ray(f + 7, fx, fy, fz, mu, u.eps + f[13], u);
-            if (mu < -f[13]) { t = fminf(tt, tu); return 0.0f; }  // outside the unit-cell bounds
-            if (!(mu > f[13])) { t = 0.0f; return xnan(); }
+            float fx = fmaf(-f12.z, nx, x), fy = fmaf(-f12.w, ny, y), fz = fmaf(-f16.x, nz, z);
+            float mu = fminf(fminf(fminf(fx - ub[0], ub[1] - fx), fminf(fy - ub[2], ub[3] - fy)),
+                             fminf(fz - ub[4], ub[5] - fz));
+            const float tu = bounds_ray(ub, fx, fy, fz, mu, u.eps + f12.y, u);
+            if (mu < -f12.y) { t = fminf(tt, tu); return 0.0f; }  // outside the unit-cell bounds
+            if (!(mu > f12.y)) { t = 0.0f; return xnan(); }
             float tk;
             const float tm = fminf(fminf(tt, tu), tcap);
             float r = coll_dr<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tm, tk);
@@ -1230,7 +1240,10 @@ XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z
     t = kFar;
     if (c.flags & C_ACCEL) {
         int G = (c.flags >> 16) & 0xff;
-        float ux = (x - c.f[0]) * c.f[3], uy = (y - c.f[1]) * c.f[4], uz = (z - c.f[2]) * c.f[5];
+        // f[0..2] grid origin, f[3..5] 1/cell size, f[6] cell base, f[8..10] cell size
+        const F4 g0 = ld4(c.f), g4 = ld4(c.f + 4), g8 = ld4(c.f + 8);
+        const float cf[11] = {g0.x, g0.y, g0.z, g0.w, g4.x, g4.y, g4.z, g4.w, g8.x, g8.y, g8.z};
+        float ux = (x - cf[0]) * cf[3], uy = (y - cf[1]) * cf[4], uz = (z - cf[2]) * cf[5];
         int ix = (int)floorf(ux), iy = (int)floorf(uy), iz = (int)floorf(uz);
         ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
         iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
@@ -1239,17 +1252,17 @@ XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z
         float tc = kFar;
         {
             // grid units; 1/(u f3) = (1/u) f8 (f8: the cell size)
-            const float dx = u.ix * c.f[8], ex = u.eps * c.f[3];
+            const float dx = u.ix * cf[8], ex = u.eps * cf[3];
             if (dx > 0.0f && ix < G - 1) tc = fminf(tc, fmaxf(((float)(ix + 1) - ex - ux) * dx, 0.0f));
             if (dx < 0.0f && ix > 0) tc = fminf(tc, fmaxf(((float)ix + ex - ux) * dx, 0.0f));
-            const float dy = u.iy * c.f[9], ey = u.eps * c.f[4];
+            const float dy = u.iy * cf[9], ey = u.eps * cf[4];
             if (dy > 0.0f && iy < G - 1) tc = fminf(tc, fmaxf(((float)(iy + 1) - ey - uy) * dy, 0.0f));
             if (dy < 0.0f && iy > 0) tc = fminf(tc, fmaxf(((float)iy + ey - uy) * dy, 0.0f));
-            const float dz = u.iz * c.f[10], ez = u.eps * c.f[5];
+            const float dz = u.iz * cf[10], ez = u.eps * cf[5];
             if (dz > 0.0f && iz < G - 1) tc = fminf(tc, fmaxf(((float)(iz + 1) - ez - uz) * dz, 0.0f));
             if (dz < 0.0f && iz > 0) tc = fminf(tc, fmaxf(((float)iz + ez - uz) * dz, 0.0f));
         }
-        int cell_base = f2i(c.f[6]);
+        int cell_base = f2i(cf[6]);
         const int cell = cell_base + (iz * G + iy) * G + ix;
         t = fmaxf(tc, fmaxf(S.clear[cell] - u.eps, 0.0f) * u.il);
         const int32_t* off = S.cells + cell;
