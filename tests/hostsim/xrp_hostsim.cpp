@@ -57,6 +57,7 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
         RenderParams P = hp.P;
         P.nviews = ncams;
         P.xs = hp.xs.data();
+        P.xsf = hp.xsf.data();
         bool vf = hp.volume_fast && !force_general;
         long total = rays ? nrays : (long)ncams * res * res;
         std::vector<unsigned long long> s0(nthreads, 0), s1(nthreads, 0);
@@ -158,4 +159,40 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
         }
         return 2;
     }
+}
+
+// FP32 march rays of the listed pixels by the two setups (double-float FP32
+// and FP64): out[q] = pc[3], d32[3] of each, for the equality test of the
+// double-float arithmetic.
+extern "C" __attribute__((visibility("default"))) int hs_ray_setup(const double* cams, int ncams, int res,
+                                                                   double R, const int* rays, long n,
+                                                                   float* out_df, float* out_64) {
+    std::vector<ViewDev> views(ncams);
+    for (int c = 0; c < ncams; c++) {
+        const double* p = cams + 20 * c;
+        view_from_camera(p, p + 3, p[19], views[c]);
+    }
+    HostLattice hl = build_lattice(R, 0.01, false);
+    std::vector<double> xs = pixel_table(res);
+    std::vector<float> xsf(2 * xs.size());
+    for (size_t q = 0; q < xs.size(); q++) {
+        xsf[2 * q] = (float)xs[q];
+        xsf[2 * q + 1] = (float)(xs[q] - (double)xsf[2 * q]);
+    }
+    for (long q = 0; q < n; q++) {
+        const ViewDev& V = views[rays[3 * q]];
+        int i = rays[3 * q + 1], j = rays[3 * q + 2];
+        Ray a, b;
+        setup_ray32_df(V, xsf.data(), i, j, hl.hdr.s_c2, a);
+        Ray64 r64;
+        setup_ray64_fast(V, xs.data(), i, j, r64);
+        setup_ray32(r64, hl.hdr.s_c, b);
+        for (int k = 0; k < 3; k++) {
+            out_df[6 * q + k] = a.pc[k];
+            out_df[6 * q + 3 + k] = a.d32[k];
+            out_64[6 * q + k] = b.pc[k];
+            out_64[6 * q + 3 + k] = b.d32[k];
+        }
+    }
+    return 0;
 }

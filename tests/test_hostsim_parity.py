@@ -156,3 +156,33 @@ def test_certificate_tracing(name, integration):
                        [(10.0, 80.0), (200.0, 120.0)], 64, 0.01)
     st = check(w, integration, nrays=1500, trace=True)
     assert st[0] > 0
+
+
+@pytest.mark.parametrize("res", [64, 96, 512, 1024])
+def test_double_float_ray_setup_matches_fp64(res):
+    """The FP32-only ray setup of the march (double-float camera, pixel table
+    and s_c) gives the FP32 origin and direction of the FP64 setup: the same
+    floats but for rare rounding ties."""
+    import ctypes
+    rng = np.random.default_rng(res)
+    angles = [(float(a), float(p)) for a, p in zip(rng.uniform(0, 360, 24), rng.uniform(5, 175, 24))]
+    w = W.Workload("r", {"type": "sphere", "center": [0, 0, 0], "radius": 0.5, "rho": 1.0}, None,
+                   angles, res, 0.01)
+    cams = np.ascontiguousarray(cams_of(w))
+    n = 20000
+    rays = np.stack([rng.integers(0, len(angles), n), rng.integers(0, res, n), rng.integers(0, res, n)],
+                    1).astype(np.int32)
+    a = np.zeros((n, 6), np.float32)
+    b = np.zeros((n, 6), np.float32)
+    L = hostsim.lib()
+    L.hs_ray_setup.restype = ctypes.c_int
+    L.hs_ray_setup.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p, ctypes.c_void_p]
+    assert L.hs_ray_setup(cams.ctypes.data, len(angles), res, w.R, rays.ctypes.data, n,
+                          a.ctypes.data, b.ctypes.data) == 0
+    same = a == b
+    assert same.mean() > 0.999
+    # one unit apart at most, or (origins near 0, where o + d s_c cancels)
+    # within 1e-12, the absolute term of the position error bound
+    ulp = np.spacing(np.abs(b).astype(np.float32))
+    assert np.all(np.abs(a - b) <= np.maximum(ulp, 1e-12))

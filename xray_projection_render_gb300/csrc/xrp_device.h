@@ -175,6 +175,10 @@ struct ViewDev {
     double f;           // focal length 1/tan(fov/2)
     int32_t general_w;  // 1: divide by the per-pixel w
     int32_t pad[3];
+    // the same camera for the FP32 march, as (hi, lo) float pairs (general_w
+    // == 0): direction before normalisation c0 * x_i + c1 * x_j + k, and the
+    // eye
+    float c0[6], c1[6], k[6], eye2[6];
 };
 
 // Sample lattice of one integrator run (same for every ray of a batch).
@@ -194,6 +198,7 @@ struct Lattice {
     float t_first;        // float(s_0 - s_c)
     float inv_ds;         // 1/ds (FP32, for clipping)
     float ds_hi, ds_lo;   // ds split so that t_k = t_first + k*(ds_hi + ds_lo)
+    float s_c2[2];        // s_c as a (hi, lo) float pair
 };
 
 // FP32 offset of lattice sample k from s_c: t_first + k*ds with ds carried
@@ -210,6 +215,7 @@ struct RenderParams {
     float flat_field;
     float density_multiplier;
     const double* xs;     // pixel coordinate table i/(res/2)-1, length res
+    const float* xsf;     // the same as (hi, lo) float pairs, length 2 res
 };
 
 // Four consecutive node parameters f[k..k+3], k a multiple of 4: one
@@ -1699,6 +1705,83 @@ XRP_HD void setup_ray32(const Ray64& r64, double s_c, Ray& r) {
     }
 }
 
+// Double-float arithmetic (a value is hi + lo, |lo| <= ulp(hi)/2): products
+// by FMA (exact error of a*b), sums by the two-sum.  About 44 significant
+// bits, from FP32 instructions only; the rounded-to-nearest forms keep the
+// device compiler from contracting the error terms.
+struct DF {
+    float hi, lo;
+};
+
+#if defined(__CUDA_ARCH__)
+XRP_HD float df_rn_add(float a, float b) { return __fadd_rn(a, b); }
+XRP_HD float df_rn_sub(float a, float b) { return __fsub_rn(a, b); }
+XRP_HD float df_rn_mul(float a, float b) { return __fmul_rn(a, b); }
+#else
+XRP_HD float df_rn_add(float a, float b) { return a + b; }
+XRP_HD float df_rn_sub(float a, float b) { return a - b; }
+XRP_HD float df_rn_mul(float a, float b) { return a * b; }
+#endif
+
+XRP_HD DF df_norm(float s, float e) {  // |s| >= |e|
+    const float r = df_rn_add(s, e);
+    return {r, df_rn_sub(e, df_rn_sub(r, s))};
+}
+
+XRP_HD DF df_add(DF a, DF b) {
+    const float s = df_rn_add(a.hi, b.hi);
+    const float v = df_rn_sub(s, a.hi);
+    float e = df_rn_add(df_rn_sub(a.hi, df_rn_sub(s, v)), df_rn_sub(b.hi, v));
+    e = df_rn_add(e, df_rn_add(a.lo, b.lo));
+    return df_norm(s, e);
+}
+
+XRP_HD DF df_mul(DF a, DF b) {
+    const float p = df_rn_mul(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    return df_norm(p, e);
+}
+
+// The ray of pixel (i, j) for the FP32 march without FP64 instructions
+// (general_w == 0): the direction c0 x_i + c1 x_j + k (camera folded on the
+// host), normalised by a reciprocal square root refined by one Newton step,
+// all in double-float; then float(d) and float(o + d s_c).  Agrees with
+// setup_ray64_fast + setup_ray32 up to ~1e-13 relative before the final
+// rounding to FP32.
+XRP_HD void setup_ray32_df(const ViewDev& V, const float* xsf, int i, int j, const float* s_c2, Ray& r) {
+    const DF xi = {xsf[2 * i], xsf[2 * i + 1]}, xj = {xsf[2 * j], xsf[2 * j + 1]};
+    DF d[3];
+    for (int a = 0; a < 3; a++)
+        d[a] = df_add(df_add(df_mul({V.c0[2 * a], V.c0[2 * a + 1]}, xi), df_mul({V.c1[2 * a], V.c1[2 * a + 1]}, xj)),
+                      {V.k[2 * a], V.k[2 * a + 1]});
+    const DF dd = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
+    // y0 ~ 1/sqrt(dd) to ~2^-22; y1 = y0 + y0 (1 - dd y0^2) / 2
+    const float y0 = 1.0f / sqrtf(dd.hi);
+    const DF y2 = df_norm(df_rn_mul(y0, y0), fmaf(y0, y0, -df_rn_mul(y0, y0)));
+    const DF q = df_mul(dd, y2);  // ~1
+    const float rres = df_rn_add(df_rn_sub(1.0f, q.hi), -q.lo);
+    const DF y = df_norm(y0, df_rn_mul(df_rn_mul(0.5f, y0), rres));
+    const DF sc = {s_c2[0], s_c2[1]};
+    for (int a = 0; a < 3; a++) {
+        const DF dn = df_mul(d[a], y);
+        r.d32[a] = dn.hi;
+        r.pc[a] = df_add({V.eye2[2 * a], V.eye2[2 * a + 1]}, df_mul(dn, sc)).hi;
+    }
+}
+
+// The FP32 march's ray of pixel (i, j): FP32 instructions only for cameras
+// without a per-pixel w, else the FP64 setup.
+XRP_HD void setup_ray_march(const ViewDev& V, const RenderParams& P, const Lattice& L, int i, int j, Ray& r) {
+    if (!V.general_w) {
+        setup_ray32_df(V, P.xsf, i, j, L.s_c2, r);
+        return;
+    }
+    Ray64 r64;
+    setup_ray64_fast(V, P.xs, i, j, r64);
+    setup_ray32(r64, L.s_c, r);
+}
+
 // FP64 density of sample s of pixel (i, j), positions formed exactly as the
 // reference does (main.go:148-150).  The ray is recomputed here so that the
 // FP32 march keeps no FP64 state live.
@@ -2139,11 +2222,7 @@ template <bool HIER, int DEPTH, bool DEFS, bool RAY>
 XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P, const ViewDev& V,
                          int i, int j, unsigned& evals) {
     Ray r;
-    {
-        Ray64 r64;
-        setup_ray64_fast(V, P.xs, i, j, r64);
-        setup_ray32(r64, L.s_c, r);
-    }
+    setup_ray_march(V, P, L, i, j, r);
     float t0, t1;
     clip_ray(S.sup_lo, S.sup_hi, r, t0, t1);
     int k0, k1;
@@ -2190,11 +2269,7 @@ XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParam
         acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
                    : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st, 4.0f * vol.band_w + 2e-4f);
     } else {
-        {
-            Ray64 r64;
-            setup_ray64_fast(V, P.xs, i, j, r64);
-            setup_ray32(r64, L.s_c, r);
-        }
+        setup_ray_march(V, P, L, i, j, r);
         SceneSampler<DEPTH, DEFS> smp{S, r, px};
         acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
                    : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);

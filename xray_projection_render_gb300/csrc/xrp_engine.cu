@@ -447,7 +447,7 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
     size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
     size_t o_clear = T.add(fs.clear);
-    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs);
+    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs), o_xsf = T.add(hp.xsf);
     size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
     size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
     cudaError_t e = tab.alloc(E, T.host.size(), st);
@@ -475,6 +475,7 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     out.P = hp.P;
     out.P.nviews = (int)views.size();
     out.P.xs = (const double*)(base + o_xs);
+    out.P.xsf = (const float*)(base + o_xsf);
     out.views = (const ViewDev*)(base + o_views);
     out.volume_fast = hp.volume_fast;
     out.depth = fs.depth;
@@ -1008,14 +1009,15 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     // one upload: per item its scene tables, views and pixel table, then the
     // lattice, the SceneDev array and the item array (patched with addresses)
     Tables T;
-    struct Off { size_t nodes, n64, child, cells, items, defs, vols, xs, clear; };
+    struct Off { size_t nodes, n64, child, cells, items, defs, vols, xs, clear, xsf; };
     std::vector<Off> off(n);
     std::vector<ViewDev> allv;  // every item's views, in work order
     std::vector<int> view0(n);
     for (int q = 0; q < n; q++) {
         const FlatScene& fs = hps[q].fs;
         off[q] = {T.add(fs.nodes), T.add(fs.nodes64), T.add(fs.child), T.add(fs.cells), T.add(fs.items),
-                  T.add(fs.defs), T.add(hps[q].vols), T.add(hps[q].xs), T.add(fs.clear)};
+                  T.add(fs.defs), T.add(hps[q].vols), T.add(hps[q].xs), T.add(fs.clear),
+                  T.add(hps[q].xsf)};
         view0[q] = (int)allv.size();
         allv.insert(allv.end(), vws[q].begin(), vws[q].end());
     }
@@ -1050,6 +1052,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         I.P = hps[q].P;
         I.P.nviews = it.num_views;
         I.P.xs = (const double*)(base + off[q].xs);
+        I.P.xsf = (const float*)(base + off[q].xsf);
         I.out0 = out_total;
         out0[q] = out_total;
         out_total += (long long)it.num_views * it.resolution * it.resolution;
@@ -1776,7 +1779,7 @@ extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, 
     size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
     size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
     size_t o_clear = T.add(fs.clear);
-    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs);
+    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs), o_xsf = T.add(hp.xsf);
     size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
     size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
     if (T.host.size() > kNoAllocScratchBytes)
@@ -1805,6 +1808,7 @@ extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, 
     pr.P = hp.P;
     pr.P.nviews = ncams;
     pr.P.xs = (const double*)(base + o_xs);
+    pr.P.xsf = (const float*)(base + o_xsf);
     pr.views = (const ViewDev*)(base + o_views);
     pr.volume_fast = hp.volume_fast;  // per-tap loads: a texture would need an array allocation
     pr.tex = 0;

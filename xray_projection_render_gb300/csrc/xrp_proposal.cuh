@@ -206,9 +206,7 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
         Ray myray;
         int my_k0 = 0, my_k1 = -1;
         if (rvalid) {
-            Ray64 r64;
-            setup_ray64_fast(views[v], P.xs, i, j, r64);
-            setup_ray32(r64, L.s_c, myray);
+            setup_ray_march(views[v], P, L, i, j, myray);
             float t0, t1;
             clip_ray(S.sup_lo, S.sup_hi, myray, t0, t1);
             if (!sample_range(L, t0, t1, L.K, my_k0, my_k1)) {
@@ -458,11 +456,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
     if (v < nviews && i < res && j < res) {
         const long r = ((long)v * res + i) * res + j;
         Ray ray;
-        {
-            Ray64 r64;
-            setup_ray64_fast(views[view0 + v], P.xs, i, j, r64);
-            setup_ray32(r64, L.s_c, ray);
-        }
+        setup_ray_march(views[view0 + v], P, L, i, j, ray);
         float t0, t1;
         clip_ray(S.sup_lo, S.sup_hi, ray, t0, t1);
         int k0, k1;

@@ -1113,7 +1113,7 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
     double Pspan = std::fabs(g.R) + T + Pc;
     // rounding of p_c, of the direction (times |t|), of the offset t (three
     // roundings, lattice_t) and of the final fma
-    double E0 = kSafety * kU * (Pc + 4 * T + Pspan) + 1e-12;
+    double E0 = kSafety * kU * (Pc + 4 * T + Pspan) + 1e-11;  // + FP32 ray setup (~1e-12)
     double E = E0, P = Pspan, lip = 1.0;
     for (auto& d : hs.defs) {
         E = def_error(d, E, P);
@@ -1333,6 +1333,21 @@ void view_from_camera(const double eye[3], const double m[16], double fov_deg, V
     } else {
         v.general_w = 1;
     }
+    // double-float camera of the FP32 march (setup_ray32_df): the unnormalised
+    // direction (M (x_i, x_j, -f, 1)) w - eye = c0 x_i + c1 x_j + k
+    if (!v.general_w) {
+        auto split = [](double x, float* out) {
+            out[0] = (float)x;
+            out[1] = (float)(x - (double)out[0]);
+        };
+        const double w = v.inv_w;
+        for (int a = 0; a < 3; a++) {
+            split(m[a] * w, v.c0 + 2 * a);
+            split(m[4 + a] * w, v.c1 + 2 * a);
+            split(std::fma(m[8 + a], -v.f, m[12 + a]) * w - eye[a], v.k + 2 * a);
+            split(eye[a], v.eye2 + 2 * a);
+        }
+    }
 }
 
 HostLattice build_lattice(double R, double ds, bool hierarchical) {
@@ -1375,6 +1390,8 @@ HostLattice build_lattice(double R, double ds, bool hierarchical) {
     L.hdr.K = (int32_t)L.s64.size();
     L.hdr.hierarchical = hierarchical ? 1 : 0;
     L.hdr.s_c = s_c;
+    L.hdr.s_c2[0] = (float)s_c;
+    L.hdr.s_c2[1] = (float)(s_c - (double)L.hdr.s_c2[0]);
     L.hdr.smin = smin;
     L.hdr.t_first = L.t32.empty() ? 0.0f : L.t32[0];
     L.hdr.inv_ds = (float)(1.0 / ds);
@@ -1402,6 +1419,11 @@ HostPrepared prepare_host(const HostScene& hs, int res, int integration, double 
         hp.hl.ft32.push_back(0.0f);
     }
     hp.xs = pixel_table(res);
+    hp.xsf.resize(2 * hp.xs.size());
+    for (size_t q = 0; q < hp.xs.size(); q++) {
+        hp.xsf[2 * q] = (float)hp.xs[q];
+        hp.xsf[2 * q + 1] = (float)(hp.xs[q] - (double)hp.xsf[2 * q]);
+    }
     hp.vols.resize(hs.vols.size());
     for (size_t k = 0; k < hs.vols.size(); k++) {
         const HVolume& hv = hs.vols[k];

@@ -113,6 +113,7 @@ struct HostPrepared {
     FlatScene fs;
     HostLattice hl;
     std::vector<double> xs;
+    std::vector<float> xsf;  // xs as (hi, lo) float pairs
     std::vector<Volume> vols;
     SceneDev S;       // pointers null
     RenderParams P;   // xs null
