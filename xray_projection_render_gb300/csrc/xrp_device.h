@@ -102,6 +102,7 @@ enum CollFlags : int32_t {
     C_EXACT_SUM = 2,  // every partial sum of child densities is exact in FP32
     C_ACCEL = 4,      // per-cell candidate lists are present
     C_CLIP = 8,       // clip the sum to [0, 1] (every ObjectCollection)
+    C_UNIFORM = 16,   // greedy, every child a leaf of the same FP32 density > 0
 };
 
 // Leaf parameter slots (Node.f).  RHO and BAND slots are shared by leaves.
@@ -1180,7 +1181,7 @@ XRP_HD float bounds_ray(const float* b, float x, float y, float z, float in, flo
     return inside ? fmaxf(hi, 0.0f) : (lo <= hi ? lo : kFar);
 }
 
-template <int D>
+template <int D, bool UNI = false>
 XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float tcap,
                      float& t);
 
@@ -1224,7 +1225,8 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
             if (!(mu > f12.y)) { t = 0.0f; return xnan(); }
             float tk;
             const float tm = fminf(fminf(tt, tu), tcap);
-            float r = coll_dr<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tm, tk);
+            // unit cells are where uniform greedy collections occur (lattices)
+            float r = coll_dr<D - 1, true>(S, S.nodes[n.a], fx, fy, fz, u, tm, tk);
             t = fminf(fminf(tt, tu), tk);
             return r;
         }
@@ -1234,10 +1236,36 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
     return xnan();
 }
 
+// Uniform greedy collections (every child a leaf of the same density > 0):
+// the decisions of coll_dm; inside a child (for certain) the density is
+// that child's whatever the others do, so its exit alone bounds the ray (no
+// list-cell cap, no other candidate).  `t` holds the list-cell cap on entry.
+XRP_HD float coll_dr_uniform(const SceneDev& S, const int32_t* kids, const int32_t* list, int cnt, float x,
+                             float y, float z, const RayDir& u, float tcap, float& t) {
+    for (int k = 0; k < cnt; k++) {
+        const int slot = list ? list[k] : k;
+        float tk;
+        const float r = leaf_dr(S.nodes[kids[slot]], x, y, z, u, tcap, tk);
+        if (isunc(r)) {  // an undecided child before any certain one
+            t = 0.0f;
+            return r;
+        }
+        if (r > 0.0f) {
+            t = tk;
+            return r;
+        }
+        t = fminf(t, tk);
+    }
+    return 0.0f;  // outside every candidate (greedy sum of zeros, clipped)
+}
+
 // coll_dm's decisions; t: the minimum over the candidates, capped (with
 // candidate lists) by the later of the exit from the point's list cell and
 // the clearance of the unlisted children.
-template <int D>
+// UNI: the collection may be uniform (unit cells of tessellations); the
+// uniform path is compiled only there, which keeps it out of the kernels of
+// scenes without tessellations.
+template <int D, bool UNI>
 XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float tcap,
                      float& t) {
     const int32_t* kids = S.child + c.a;
@@ -1277,6 +1305,9 @@ XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z
         cnt = s1 - s0;
     }
     const bool greedy = (c.flags & C_GREEDY) != 0;
+    if constexpr (UNI) {
+        if (c.flags & C_UNIFORM) return coll_dr_uniform(S, kids, list, cnt, x, y, z, u, tcap, t);
+    }
     float sum = 0.0f, sabs = 0.0f;
     bool unc = false, done = false;
     for (int k = 0; k < cnt; k++) {

@@ -937,6 +937,15 @@ struct Flattener {
             flags |= C_ACCEL | (G << 16);
         }
         flags |= homo << 8;
+        if (h.greedy && !kids.empty()) {
+            bool uni = true;
+            const float r0 = fs.nodes[kids[0]].f[F_RHO];
+            for (int k : kids) {
+                const Node& kn = fs.nodes[k];
+                uni = uni && kn.type <= N_GYROID && kn.f[F_RHO] == r0;
+            }
+            if (uni && r0 > 0.0f) flags |= C_UNIFORM;
+        }
         fs.nodes[me].flags = flags;
         // outputs of the collection
         info.dyadic = (flags & C_EXACT_SUM) != 0;
