@@ -196,3 +196,31 @@ def test_non_affine_chain_has_no_ray_certificates():
     _, _, affine = hostsim.ray_bound(w.obj, np.zeros((1, 3)), np.array([[1.0, 0, 0]]),
                                      deformation=w.deformation)
     assert not affine
+
+
+def test_ray_far_camera_and_offset_scene():
+    # a distant, narrow camera (R 60, fov 8) and a scene offset from the
+    # origin: larger position errors, larger capsule radius
+    obj = {"type": "object_collection", "objects": [
+        {"type": "sphere", "center": [3.1, -2.2, 1.05], "radius": 0.4, "rho": 0.7},
+        {"type": "cylinder", "p0": [2.5, -2.5, 0.8], "p1": [3.5, -1.6, 1.3], "radius": 0.1},
+        {"type": "box", "center": [3.0, -2.0, 1.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5}]}
+    rng = np.random.default_rng(11)
+    n = 600
+    P = np.array([3.0, -2.0, 1.0]) + rng.uniform(-0.7, 0.7, (n, 3))
+    D = rng.normal(size=(n, 3))
+    D /= np.linalg.norm(D, axis=1, keepdims=True)
+    d = {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]}
+    rho, t, affine = hostsim.ray_bound(obj, P, D, deformation=d, R=60.0, fov=8.0)
+    assert affine
+    sc = O.Scene(obj, d)
+    checked = 0
+    for k in range(n):
+        if not (t[k] > 0) or np.isnan(rho[k]):
+            continue
+        r0 = sc.density(*P[k])
+        assert np.float32(r0) == rho[k]
+        for tau in np.concatenate([[0.999 * min(float(t[k]), 4.0)], rng.uniform(0, min(float(t[k]), 4.0), 5)]):
+            assert sc.density(*(P[k] + D[k] * tau)) == r0
+        checked += 1
+    assert checked > n // 2

@@ -186,3 +186,19 @@ def test_double_float_ray_setup_matches_fp64(res):
     # within 1e-12, the absolute term of the position error bound
     ulp = np.spacing(np.abs(b).astype(np.float32))
     assert np.all(np.abs(a - b) <= np.maximum(ulp, 1e-12))
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_tracing_far_narrow_camera(integration):
+    """Ray and ball certificates with a distant, narrow camera (R 20, fov 12):
+    larger position error bounds and capsule radius."""
+    coll = {"type": "object_collection", "objects": [
+        {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+        {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+        {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+         "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9}]}
+    for deform in (None, {"type": "affine", "matrix": [[1.1, 0.0, 0.1], [0.0, 0.9, 0.0], [0.05, 0.0, 1.0]]},
+                   {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02], "sigmas": [0.3, 0.3, 0.5],
+                    "centers": [0.0, 0.1, 0.0]}):
+        w = W.Workload("far", coll, deform, [(10.0, 80.0), (200.0, 120.0)], 64, 0.004, R=20.0, fov=12.0)
+        check(w, integration, nrays=1200, trace=True)
