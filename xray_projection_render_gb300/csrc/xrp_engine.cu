@@ -19,6 +19,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/xrp.h"
@@ -931,10 +932,14 @@ static void batch_free(xrp_batch* b) {
     if (!b) return;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->cap) cudaStreamDestroy(b->cap);
+    // cudaFree waits for the device, so no replay can still use the images
     if (b->tables) cudaFree(b->tables);
-    if (b->out) cudaFree(b->out);
     if (b->counter) cudaFree(b->counter);
+    if (b->out) {  // back to the engine pool
+        if (b->cap) cudaFreeAsync(b->out, b->cap);
+        else cudaFree(b->out);
+    }
+    if (b->cap) cudaStreamDestroy(b->cap);
     delete b;
 }
 
@@ -987,16 +992,34 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     std::vector<std::vector<ViewDev>> vws(n);
     int depth = 0;
     bool defs = false, affine = true;
+    // flattening is independent per item: host threads share the items
+    std::vector<std::string> errs(n);
+    {
+        std::atomic<int> next{0};
+        auto work = [&]() {
+            for (int q; (q = next.fetch_add(1)) < n;) {
+                const xrp_batch_item& it = items[order[q]];
+                double fov_max;
+                vws[q] = views_from(it.views, it.num_views, &fov_max);
+                try {
+                    hps[q] = prepare_host(it.scene->hs, it.resolution, oo.integration, oo.ds, oo.R,
+                                          oo.flat_field, oo.density_multiplier, fov_max);
+                } catch (const std::exception& ex) {
+                    errs[q] = ex.what();
+                    if (errs[q].empty()) errs[q] = "flattening failed";
+                }
+            }
+        };
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int nth = (int)std::min<unsigned>(std::min<unsigned>(hw, 16u), (unsigned)n);
+        std::vector<std::thread> pool;
+        for (int k = 1; k < nth; k++) pool.emplace_back(work);
+        work();
+        for (auto& th : pool) th.join();
+    }
     for (int q = 0; q < n; q++) {
         const xrp_batch_item& it = items[order[q]];
-        double fov_max;
-        vws[q] = views_from(it.views, it.num_views, &fov_max);
-        try {
-            hps[q] = prepare_host(it.scene->hs, it.resolution, oo.integration, oo.ds, oo.R, oo.flat_field,
-                                  oo.density_multiplier, fov_max);
-        } catch (const std::exception& ex) {
-            return fail(2, "item %d: %s", order[q], ex.what());
-        }
+        if (!errs[q].empty()) return fail(2, "item %d: %s", order[q], errs[q].c_str());
         for (size_t v = 0; v < hps[q].vols.size(); v++) {
             hps[q].vols[v].data = it.scene->vdev[v];
             hps[q].vols[v].data64 = it.scene->v64[v];
@@ -1071,12 +1094,17 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         B->offset[order[q]] = out0[q];
         B->size[order[q]] = (long long)items[order[q]].num_views * items[order[q]].resolution * items[order[q]].resolution;
     }
-    if ((e = cudaMalloc(&B->out, (size_t)std::max<long long>(out_total, 1) * sizeof(float))) != cudaSuccess)
+    if ((e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(3, "batch stream", e);
+    // the images come from the engine's pool: memory released by an earlier
+    // batch is reused already mapped (copies out of freshly mapped device
+    // memory ran at 20-60 GB/s against ~190 GB/s once warm)
+    if ((e = cudaMallocFromPoolAsync((void**)&B->out, (size_t)std::max<long long>(out_total, 1) * sizeof(float),
+                                     E->pool, B->cap)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(B->cap)) != cudaSuccess)
         return cuda_fail(3, "batch output", e);
     if ((e = cudaMalloc(&B->counter, sizeof(unsigned long long))) != cudaSuccess)
         return cuda_fail(3, "batch counter", e);
-    if ((e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking)) != cudaSuccess)
-        return cuda_fail(3, "batch stream", e);
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
     const bool hier = oo.integration == XRP_INTEGRATE_HIERARCHICAL;
