@@ -165,7 +165,7 @@ struct SceneDev {
     // ray certificates (dens_ray32, affine chains): capsule radius in
     // deformed coordinates (m_slack plus the direction error over the span)
     float ray_slack;
-    float pad2;
+    int32_t nnodes;  // node count when the tracing kernels stage the table in shared memory, else 0
 };
 
 // One view (camera) of a batch, prepared on the host.

@@ -466,6 +466,8 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     S.clear = (const float*)(base + o_clear);
     S.defs = (const DefStep*)(base + o_defs);
     S.vols = (const Volume*)(base + o_vols);
+    // tracing kernels stage node tables of up to 32 KB in shared memory
+    S.nnodes = fs.nodes.size() * sizeof(Node) <= 32768 ? (int32_t)fs.nodes.size() : 0;
     out.L = hl.hdr;
     Lattice& L = out.L;
     L.s64 = (const double*)(base + o_s64);

@@ -453,6 +453,18 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
     const int i = (ti << 4) + ((warp >> 1) << 2) + (lane >> 3);
     const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
     unsigned evals = 0;
+    // the scene's node table in shared memory (S.nnodes > 0: it fits); the
+    // FP64 re-evaluation keeps the global table
+    extern __shared__ __align__(16) unsigned char trace_smem[];
+    SceneDev Sl = S;
+    if (S.nnodes > 0) {
+        const int4* src = reinterpret_cast<const int4*>(S.nodes);
+        int4* dst = reinterpret_cast<int4*>(trace_smem);
+        for (int q = threadIdx.x; q < S.nnodes * (int)(sizeof(Node) / sizeof(int4)); q += blockDim.x)
+            dst[q] = src[q];
+        __syncthreads();
+        Sl.nodes = reinterpret_cast<const Node*>(trace_smem);
+    }
     if (v < nviews && i < res && j < res) {
         const long r = ((long)v * res + i) * res + j;
         Ray ray;
@@ -467,7 +479,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
                 // fine samples only add, so they go to the list (high bit)
                 const ViewDev& V = views[view0 + v];
                 sum = trace_sum_hier<DEPTH, DEFS, RAY>(
-                    S, L, ray, k0, k1,
+                    Sl, L, ray, k0, k1,
                     [&](int q, bool fine) {
                         if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
                         unsigned slot = atomicAdd(Q.fb_count, 1u);
@@ -477,7 +489,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 3)
                     evals);
             } else {
                 sum = trace_sum<DEPTH, DEFS, RAY>(
-                    S, L, ray, k0, k1,
+                    Sl, L, ray, k0, k1,
                     [&](int k) {
                         unsigned slot = atomicAdd(Q.fb_count, 1u);
                         if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);

@@ -13,12 +13,13 @@ cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams&
     long blocks = (long)nviews * tpr * tpr;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
+    const size_t smem = (size_t)pr.S.nnodes * sizeof(Node);
     if (pr.L.hierarchical)
-        k_trace<DEPTH, DEFS, true, RAY><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
-                                                                         nviews, Q, dout);
+        k_trace<DEPTH, DEFS, true, RAY><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
+                                                                            nviews, Q, dout);
     else
-        k_trace<DEPTH, DEFS, false, RAY><<<(unsigned)blocks, 256, 0, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
-                                                                          nviews, Q, dout);
+        k_trace<DEPTH, DEFS, false, RAY><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
+                                                                             nviews, Q, dout);
     return cudaGetLastError();
 }
 
