@@ -26,11 +26,12 @@ struct BatchStage {
 
 // TRACE: 0 plain integrator, 1 certificate tracing with ball certificates,
 // 2 with ray certificates (every scene of the batch has an affine chain).
-// Resident blocks per SM (register budget) measured on GB300: ray tracing
-// 4 (64 registers: 4809 Mrays/s on the 64-scene batch, against 4591 with 3
-// and 4116 with 2; spills cost less than the lost warps), ball tracing 3.
+// Resident blocks per SM (register budget) measured on GB300 for tracing:
+// 4 (64 registers). Ray bounds on the 64-scene batch: 4116 Mrays/s with 2
+// blocks, 4591 with 3, 4809 with 4, 4841 with 5; ball certificates: 1678
+// with 3, 1911 with 4 (spills cost less than the lost warps).
 template <bool HIER, int DEPTH, bool DEFS, int TRACE>
-__global__ void __launch_bounds__(256, DEPTH >= 3 ? XRP_SCENE_MIN_BLOCKS : (TRACE == 2 ? 4 : (TRACE ? 3 : XRP_SCENE_MIN_BLOCKS)))
+__global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 4 : XRP_SCENE_MIN_BLOCKS)
     k_batch(const SceneDev* __restrict__ scenes, const BatchItemDev* __restrict__ items, int nitems,
             const ViewDev* __restrict__ views, const __grid_constant__ Lattice L, long long ntiles, int tw,
             int th, unsigned long long* __restrict__ counter, long long stride, long long limit,

@@ -437,10 +437,11 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // distance along the ray to the next possible density change, so a ray
 // jumps straight to the next boundary instead of approaching it.  Samples
 // FP32 cannot decide go to the FP64 list like the other march modes.
-// Resident blocks per SM for depth < 3, measured: ray bounds 4 (64
-// registers; lattice 415 against 382 Mrays/s with 3), balls 3.
+// Resident blocks per SM for depth < 3, measured: 4 (64 registers; lattice
+// with ray bounds 415 against 382 Mrays/s with 3 and 410 with 5, gyroid with
+// balls 1462 against 1406 with 3).
 template <int DEPTH, bool DEFS, bool HIER, bool RAY>
-__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (RAY ? 4 : 3))
+__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 4)
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
