@@ -292,3 +292,22 @@ def test_ray_tracing_matches_plain_at_scale(X, name):
         traced, st = X.render_proposal(s, None, angles, trace=True, stats=True, **kw)
     assert st["fp64_list_overflow"] == 0
     assert np.max(np.abs(traced - plain) / plain) <= 2 * REL_TOL
+
+
+def test_tracing_large_scene_reads_nodes_from_global_memory(X):
+    """A scene whose node table exceeds the 32 KB staged in shared memory
+    (300 primitives): the tracing kernel reads the global table."""
+    rng = np.random.default_rng(21)
+    objs = []
+    for _ in range(300):
+        c = rng.uniform(-0.8, 0.8, 3).tolist()
+        objs.append({"type": "sphere", "center": c, "radius": float(rng.uniform(0.02, 0.08)),
+                     "rho": 1.0 if rng.uniform() < 0.7 else -1.0})
+    w = W.Workload("many_spheres", {"type": "object_collection", "objects": objs}, None,
+                   [(10.0, 80.0), (200.0, 120.0)], 48, 0.005)
+    ref = _oracle(w)
+    with X.Scene(w.obj, w.deformation) as s:
+        for mode in (True, "ball"):
+            img = X.render_proposal(s, None, w.angles, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                                    trace=mode)
+            assert np.max(np.abs(img - ref) / ref) <= REL_TOL
