@@ -202,3 +202,44 @@ def test_tracing_far_narrow_camera(integration):
                     "centers": [0.0, 0.1, 0.0]}):
         w = W.Workload("far", coll, deform, [(10.0, 80.0), (200.0, 120.0)], 64, 0.004, R=20.0, fov=12.0)
         check(w, integration, nrays=1200, trace=True)
+
+
+def _nested_lattice(depth):
+    """Tessellations nested `depth` deep; the innermost unit cell holds eight
+    struts of density 1 (a uniform greedy collection with candidate lists),
+    the middle one mixes densities (not uniform)."""
+    a = 0.2
+    struts = [{"type": "cylinder", "p0": [0.0, u, v], "p1": [a, u, v], "radius": 0.02, "rho": 1.0}
+              for u in (0.0, a) for v in (0.0, a)]
+    struts += [{"type": "cylinder", "p0": [u, 0.0, v], "p1": [u, a, v], "radius": 0.02, "rho": 1.0}
+               for u in (0.0, a) for v in (0.0, a)]
+    obj = {"type": "tessellated_obj_coll",
+           "uc": {"objects": {"type": "object_collection", "objects": struts},
+                  "xmin": 0, "xmax": a, "ymin": 0, "ymax": a, "zmin": 0, "zmax": a},
+           "xmin": 0, "xmax": 0.4, "ymin": 0, "ymax": 0.4, "zmin": 0, "zmax": 0.4}
+    if depth == 1:
+        obj.update(xmin=-1, xmax=1, ymin=-1, ymax=1, zmin=-1, zmax=1)
+    for level in range(1, depth):
+        objs = [obj, {"type": "sphere", "center": [0.45, 0.45, 0.45], "radius": 0.04, "rho": 0.5}]
+        size = 0.5 * (2 ** (level - 1)) if level < depth - 1 else 0.5
+        hi = 1.0 if level == depth - 1 else 2 * size
+        lo = -1.0 if level == depth - 1 else 0.0
+        obj = {"type": "tessellated_obj_coll",
+               "uc": {"objects": {"type": "object_collection", "objects": objs},
+                      "xmin": 0, "xmax": 0.5, "ymin": 0, "ymax": 0.5, "zmin": 0, "zmax": 0.5},
+               "xmin": lo, "xmax": hi, "ymin": lo, "ymax": hi, "zmin": lo, "zmax": hi}
+    return obj
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+@pytest.mark.parametrize("depth", [1, 2, 3])
+def test_tracing_nested_tessellations(depth, integration):
+    """Ray certificates through nested tessellations (folds at every level,
+    uniform and mixed unit cells) under a linear strain, and ball
+    certificates under a gaussian deformation."""
+    obj = _nested_lattice(depth)
+    for deform in ({"type": "linear", "strains": [0.01, 0.0, 0.05, 0.0, 0.02, 0.0]},
+                   {"type": "gaussian", "amplitudes": [0.05, -0.03, 0.02], "sigmas": [0.4, 0.4, 0.5],
+                    "centers": [0.0, 0.1, 0.0]}):
+        w = W.Workload("nested", obj, deform, [(30.0, 75.0), (200.0, 110.0)], 64, 0.004)
+        check(w, integration, nrays=1500, trace=True)
