@@ -89,7 +89,8 @@ def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integrat
            flat_field=0.0, density_multiplier=1.0, rays=None, nthreads=None, force_general=False,
            trace=False):
     """cams: array (n, 20) = eye(3), column-major camera(16), fov.  ``trace``:
-    certificate tracing (simple integrator; stats[0] counts evaluations)."""
+    certificate tracing (stats[0] counts evaluations); "curve": curved-ray
+    certificates for non-affine chains."""
     cams = np.ascontiguousarray(cams, dtype=np.float64).reshape(-1, 20)
     n = cams.shape[0]
     vol = None
@@ -112,7 +113,28 @@ def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integrat
                          nthreads or os.cpu_count() or 1,
                          rays.ctypes.data if rays is not None else None,
                          rays.shape[0] if rays is not None else 0, 1 if force_general else 0,
-                         1 if trace else 0, err, 512)
+                         2 if trace == "curve" else (1 if trace else 0), err, 512)
     if rc != 0:
         raise ValueError(err.value.decode())
     return out, stats
+
+
+def curve_bound(obj, points, dirs, *, deformation=None, R=4.0, fov=40.0, ds=0.01):
+    """Curved-ray certificates at points [n,3] along world directions [n,3]:
+    (density, bound t).  Every sample at ray parameter s in [0, t] must have
+    the density of the point."""
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    d = np.ascontiguousarray(dirs, dtype=np.float64).reshape(-1, 3)
+    n = pts.shape[0]
+    rho, t = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    err = ctypes.create_string_buffer(512)
+    L = lib()
+    L.hs_curve.restype = ctypes.c_int
+    L.hs_curve.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p,
+                           ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+    rc = L.hs_curve(json.dumps(obj).encode(), json.dumps(deformation).encode() if deformation else None,
+                    pts.ctypes.data, d.ctypes.data, n, R, fov, ds, rho.ctypes.data, t.ctypes.data, err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return rho, t

@@ -81,6 +81,9 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
                     if (S.affine)
                         val = hier ? trace_pixel<true, kMaxDepth, true, true>(S, L, P, views[v], i, j, ev)
                                    : trace_pixel<false, kMaxDepth, true, true>(S, L, P, views[v], i, j, ev);
+                    else if (trace == 2)  // curved-ray certificates
+                        val = hier ? trace_pixel<true, kMaxDepth, true, false, true>(S, L, P, views[v], i, j, ev)
+                                   : trace_pixel<false, kMaxDepth, true, false, true>(S, L, P, views[v], i, j, ev);
                     else
                         val = hier ? trace_pixel<true, kMaxDepth, true, false>(S, L, P, views[v], i, j, ev)
                                    : trace_pixel<false, kMaxDepth, true, false>(S, L, P, views[v], i, j, ev);
@@ -195,4 +198,37 @@ extern "C" __attribute__((visibility("default"))) int hs_ray_setup(const double*
         }
     }
     return 0;
+}
+
+// Curved-ray certificates at FP64 points along FP64 world directions (CPU
+// build): the density and the curve bound t, for the soundness tests.
+extern "C" __attribute__((visibility("default"))) int hs_curve(const char* obj_json, const char* def_json,
+                                                               const double* pts, const double* dirs, long n,
+                                                               double R, double fov, double ds, float* rho_out,
+                                                               float* t_out, char* err, int errlen) {
+    try {
+        HostScene hs = load_scene(obj_json, def_json, {});
+        HostPrepared hp = prepare_host(hs, 8, 0, ds, R, 0.0, 1.0, fov);
+        SceneDev S = hp.S;
+        S.nodes = hp.fs.nodes.data();
+        S.nodes64 = hp.fs.nodes64.data();
+        S.child = hp.fs.child.data();
+        S.cells = hp.fs.cells.data();
+        S.items = hp.fs.items.data();
+        S.clear = hp.fs.clear.data();
+        S.defs = hp.fs.defs.data();
+        S.vols = hp.vols.data();
+        for (long q = 0; q < n; q++) {
+            float d[3] = {(float)dirs[3 * q], (float)dirs[3 * q + 1], (float)dirs[3 * q + 2]};
+            rho_out[q] = dens_curve32<kMaxDepth, true>(S, (float)pts[3 * q], (float)pts[3 * q + 1],
+                                                       (float)pts[3 * q + 2], d, t_out[q]);
+        }
+        return 0;
+    } catch (const std::exception& ex) {
+        if (err && errlen > 0) {
+            strncpy(err, ex.what(), errlen - 1);
+            err[errlen - 1] = 0;
+        }
+        return 2;
+    }
 }

@@ -224,3 +224,67 @@ def test_ray_far_camera_and_offset_scene():
             assert sc.density(*(P[k] + D[k] * tau)) == r0
         checked += 1
     assert checked > n // 2
+
+
+# ---------------------------------------------------------------------------
+# Curved-ray certificates (smooth non-affine chains, CPU build): along a
+# world direction D the density must stay that of the point for every ray
+# parameter in [0, t], the deformed path being curved.
+# ---------------------------------------------------------------------------
+
+def check_curve(obj, deformation, n=800, per=8, seed=0, span=4.0):
+    rng = np.random.default_rng(seed)
+    P = rng.uniform(-1.1, 1.1, (n, 3))
+    D = rng.normal(size=(n, 3))
+    D /= np.linalg.norm(D, axis=1, keepdims=True)
+    rho, t = hostsim.curve_bound(obj, P, D, deformation=deformation)
+    rho_pt, _ = hostsim.margin(obj, P, deformation=deformation)
+    assert np.array_equal(np.isnan(rho), np.isnan(rho_pt))
+    ok = ~np.isnan(rho)
+    assert np.array_equal(rho[ok], rho_pt[ok])
+    sc = O.Scene(obj, deformation)
+    certified = 0
+    for k in range(n):
+        if not (t[k] > 0) or np.isnan(rho[k]):
+            continue
+        r0 = sc.density(*P[k])
+        assert np.float32(r0) == rho[k]
+        tk = min(float(t[k]), span)
+        for tau in np.concatenate([[tk, 0.999 * tk, 0.5 * tk], rng.uniform(0, tk, per - 3)]):
+            assert sc.density(*(P[k] + D[k] * tau)) == r0, (k, P[k], D[k], float(t[k]), tau)
+        certified += 1
+    return certified, n
+
+
+GAUSS = {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02], "sigmas": [0.3, 0.3, 0.5],
+         "centers": [0.0, 0.1, 0.0]}
+SIGMOID = {"type": "sigmoid", "amplitude": 0.2, "center": 0.0, "lengthscale": 0.2, "direction": "y"}
+
+
+def test_curve_gyroid_sigmoid():
+    w = W.gyroid_sigmoid()
+    c, n = check_curve(w.obj, w.deformation)
+    assert c > n // 2
+
+
+def test_curve_every_primitive_and_collection():
+    prims = [
+        {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+        {"type": "box", "center": [0.0, 0.2, 0.0], "sides": [0.5, 0.3, 0.9], "rho": 0.5},
+        {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+        {"type": "parallelepiped", "origin": [0.0, 0.0, 0.0], "v0": [0.4, 0.1, 0.0],
+         "v1": [0.0, 0.5, 0.1], "v2": [0.1, 0.0, 0.3], "rho": 0.9},
+        {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0},
+    ]
+    chain = {"type": "composed", "deformations": [
+        GAUSS, {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]}, SIGMOID]}
+    for d in (GAUSS, SIGMOID, chain):
+        for p in prims:
+            check_curve(p, d, n=250, per=6)
+        check_curve({"type": "object_collection", "objects": prims}, d, n=300, per=6)
+
+
+def test_curve_tessellated_lattice_under_gaussian():
+    w = W.deformed_lattice()
+    c, n = check_curve(w.obj, GAUSS, n=600)
+    assert c > n // 3

@@ -232,6 +232,31 @@ def _nested_lattice(depth):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+@pytest.mark.parametrize("name", ["gyroid", "coll_defs", "lattice_gauss"])
+def test_curved_ray_tracing(name, integration):
+    """Curved-ray certificates (CPU build) for non-affine chains: the traced
+    renders match the oracle, with fewer evaluations than ball certificates
+    on the gyroid."""
+    gauss = {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02], "sigmas": [0.3, 0.3, 0.5],
+             "centers": [0.0, 0.1, 0.0]}
+    if name == "gyroid":
+        w = W.reduced(W.gyroid_sigmoid(), 128, 4)
+    elif name == "lattice_gauss":
+        base = W.reduced(W.deformed_lattice(), 96, 3)
+        w = W.Workload("lattice_gauss", base.obj, gauss, base.angles, base.res, base.ds)
+    else:
+        coll = {"type": "object_collection", "objects": [
+            {"type": "sphere", "center": [0.1, -0.2, 0.05], "radius": 0.4, "rho": 0.7},
+            {"type": "cylinder", "p0": [-0.5, -0.5, -0.2], "p1": [0.5, 0.4, 0.3], "radius": 0.1},
+            {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2, "rho": 1.0}]}
+        w = W.Workload("c", coll, gauss, [(10.0, 80.0), (200.0, 120.0)], 64, 0.01)
+    st_curve = check(w, integration, nrays=1500, trace="curve")
+    if name == "gyroid" and integration == "simple":
+        st_ball = check(w, integration, nrays=1500, trace=True)
+        assert 2 * st_curve[0] < st_ball[0]
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 @pytest.mark.parametrize("depth", [1, 2, 3])
 def test_tracing_nested_tessellations(depth, integration):
     """Ray certificates through nested tessellations (folds at every level,
@@ -243,3 +268,5 @@ def test_tracing_nested_tessellations(depth, integration):
                     "centers": [0.0, 0.1, 0.0]}):
         w = W.Workload("nested", obj, deform, [(30.0, 75.0), (200.0, 110.0)], 64, 0.004)
         check(w, integration, nrays=1500, trace=True)
+        if deform["type"] == "gaussian":
+            check(w, integration, nrays=1500, trace="curve")

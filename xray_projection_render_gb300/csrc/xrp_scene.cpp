@@ -1168,6 +1168,36 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
         double span = 2.0 * T + 1.0;
         fs.ray_slack = fs.margin_slack + 4.0 * (8.0 * (double)(hs.defs.size() + 2) + 32.0) * kU * lip * span;
     }
+    // curved-ray certificates: the deformed point q(s) of a unit-speed ray
+    // moves at most lip per unit s; its acceleration, step by step (chain
+    // rule: q'' = J p'' + H[p', p']), with V the speed bound into the step
+    {
+        double acc = 0.0, V = 1.0;
+        for (auto& d : hs.defs) {
+            const double* a = d.d;
+            const double l = def_lip(d);
+            switch (d.type) {
+            case D_SIGMOID: {  // q_k = p_k + A sigma((p_k - c)/L): |sigma'| <= 1/4, |sigma''| <= 0.0962
+                const double A = std::fabs(a[0]), L = std::fabs(a[2]);
+                acc = acc * (1.0 + A / (4.0 * L)) + A * 0.0963 * V * V / (L * L);
+                break;
+            }
+            case D_GAUSSIAN: {  // Hessian of a e^{-s r^2}: norm <= 4 s |a| e^{-1/2}, s = 1/(2 sigma^2)
+                double h2 = 0.0;
+                for (int i = 0; i < 3; i++) {
+                    const double s2 = 1.0 / (2.0 * a[3 + i] * a[3 + i]);
+                    const double h = 4.0 * s2 * std::fabs(a[i]) * std::exp(-0.5);
+                    h2 += h * h;
+                }
+                acc = acc * l + std::sqrt(h2) * V * V;
+                break;
+            }
+            default: acc = acc * l; break;  // affine steps bend nothing
+            }
+            V *= l;
+        }
+        fs.curve_acc = acc * 1.01 + 1e-12;
+    }
     Flattener F{hs, fs, hierarchical, {}};
     Flattener::Info info;
     fs.root = F.node(hs.root, E, P, 0, info);
@@ -1459,6 +1489,8 @@ HostPrepared prepare_host(const HostScene& hs, int res, int integration, double 
     S.m_slack = (float)hp.fs.margin_slack;
     S.affine = hp.fs.affine ? 1 : 0;
     S.ray_slack = (float)hp.fs.ray_slack;
+    S.curve_vmax = (float)hp.fs.def_lip * (1.0f + 1e-6f);
+    S.curve_acc = (float)hp.fs.curve_acc * (1.0f + 1e-6f);
     memset(&hp.P, 0, sizeof(hp.P));
     hp.P.res = res;
     hp.P.flat_field = (float)flat_field;

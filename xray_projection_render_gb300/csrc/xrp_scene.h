@@ -85,6 +85,7 @@ struct FlatScene {
     double margin_slack = 0.0;    // error allowance of certificate radii (deformed units)
     bool affine = true;           // deformation chain affine and invertible (ray certificates)
     double ray_slack = 0.0;       // capsule radius of ray certificates (deformed units)
+    double curve_acc = 0.0;       // bound on |d^2 q/ds^2| of the deformed point along a unit ray
 };
 
 FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical);
