@@ -1448,6 +1448,20 @@ XRP_HD float curve_time(float m, const CurveDir& c) { return fmaxf(m - c.eps, 0.
 // eps from every face: the first parameter at which the curve can reach a
 // face, face by face (gap to the face, speed toward it, acceleration bound),
 // at least the ball bound.
+// Box b and a point outside it: entering needs every coordinate inside its
+// slab (grown by eps), so the latest per-axis arrival bounds the entry.
+XRP_HD float box_curve_entry(const float* b, float x, float y, float z, const CurveDir& c) {
+    const float M = c.acc + 1e-20f;
+    const float p[3] = {x, y, z}, v[3] = {c.vx, c.vy, c.vz};
+    float t = 0.0f;
+    for (int a = 0; a < 3; a++) {
+        const float below = b[2 * a] - c.eps - p[a], above = p[a] - b[2 * a + 1] - c.eps;
+        if (below > 0.0f) t = fmaxf(t, gap_time(below, v[a] + 1e-6f * c.vmax, M));
+        if (above > 0.0f) t = fmaxf(t, gap_time(above, -v[a] + 1e-6f * c.vmax, M));
+    }
+    return t;
+}
+
 XRP_HD float box_curve_time(const float* b, float x, float y, float z, const CurveDir& c) {
     const float M = c.acc + 1e-20f;
     const float gaps[6] = {x - b[0] - c.eps, b[1] - x - c.eps, y - b[2] - c.eps,
@@ -1509,7 +1523,11 @@ XRP_HD float item_dc(const SceneDev& S, int id, float x, float y, float z, const
             const float* f = n.f;
             float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
                              fminf(z - f[4], f[5] - z));
-            if (mo < -f[6]) { t = curve_time(-mo, u); return 0.0f; }
+            const float ob[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
+            if (mo < -f[6]) {  // outside: zero until the curve can enter the bounds
+                t = fmaxf(curve_time(-mo, u), box_curve_entry(ob, x, y, z, u));
+                return 0.0f;
+            }
             if (!(mo > f[6])) { t = 0.0f; return xnan(); }
             float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
             float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
@@ -1529,7 +1547,6 @@ XRP_HD float item_dc(const SceneDev& S, int id, float x, float y, float z, const
             float r = coll_dc<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tk);
             // the outer bounds, the fold's cell and the unit-cell bounds, face
             // by face along the curve (their distances alone bound it too)
-            const float ob[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
             const float ub[6] = {f[7], f[8], f[9], f[10], f[11], f[12]};
             float cb[6];
             for (int a = 0; a < 3; a++) {
