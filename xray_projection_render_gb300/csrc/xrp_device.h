@@ -1475,13 +1475,135 @@ XRP_HD float box_curve_time(const float* b, float x, float y, float z, const Cur
     return t;
 }
 
-// Leaf density (leaf_dm's decisions) and its curve bound t.
+// Slab lo < a < hi of a coordinate a(s) with a' = w at the sample and
+// |a''| <= M: inside (at least e from both faces) the first exit, outside
+// the first arrival at the slab (grown by e); 0 within e of a face.
+XRP_HD float slab_curve(float a, float w, float lo, float hi, float e, float M, bool inside) {
+    if (inside) {
+        const float g0 = a - lo - e, g1 = hi - a - e;
+        if (!(g0 > 0.0f && g1 > 0.0f)) return 0.0f;
+        return fminf(gap_time(g0, -w, M), gap_time(g1, w, M));
+    }
+    if (a < lo - e) return gap_time(lo - e - a, w, M);
+    if (a > hi + e) return gap_time(a - hi - e, -w, M);
+    return 0.0f;
+}
+
+// Squared radius f = |w|^2 (3-D, or across a cylinder's axis) against r^2:
+// f' = 2 w.v, |f''| <= 2 vmax^2 + 2 |w| acc with |w| <= r inside.  Inside
+// (|w| < r - e): the first time f can reach (r - e)^2.  Outside the radius
+// d = |w| has |d''| <= vmax^2 / r + acc while d >= r: the first time d can
+// come down to r + e.
+XRP_HD float radius_curve(float w2, float wv, float r, float e, float vmax, float acc, bool inside) {
+    if (inside) {
+        const float ri = r - e;
+        const float gap = ri * ri - w2;
+        if (!(ri > 0.0f && gap > 0.0f)) return 0.0f;
+        return gap_time(gap, 2.0f * wv + 1e-6f * vmax * ri, fmaf(2.0f * r, acc, 2.0f * vmax * vmax) * 1.01f);
+    }
+    const float d = sqrtf(w2);
+    const float gap = d - r - e;
+    if (!(gap > 0.0f && r > 0.0f)) return 0.0f;
+    return gap_time(gap, -wv / d + 1e-6f * vmax, fmaf(vmax, vmax / r, acc) * 1.01f + 1e-20f);
+}
+
+// Leaf density (leaf_dm's decisions) and its curve bound t: the ball bound,
+// or better the second-order bound of the leaf's defining conditions
+// (entry: the latest arrival over the violated conditions; exit: the
+// earliest over all).
 XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t) {
     float m;
     const float rho = leaf_dm(n, x, y, z, m);
     t = curve_time(m, c);
-    if (n.type != N_GYROID || isunc(rho)) return rho;
+    if (isunc(rho)) return rho;
     const float* f = n.f;
+    const float e = c.eps;
+    const float M = c.acc * 1.01f + 1e-20f;
+    switch (n.type) {
+    case N_SPHERE: {
+        const float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        const float w2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
+        const float wv = fmaf(wz, c.vz, fmaf(wy, c.vy, wx * c.vx));
+        const float r = f[4], b = sqrtf(f[F_BAND]);  // band of d^2 - r^2 as a distance (upper bound)
+        t = fmaxf(t, radius_curve(w2, wv, r, e + b, c.vmax, c.acc, w2 < r * r));
+        return rho;
+    }
+    case N_BOX: {
+        const float bb[6] = {f[0] - f[3], f[0] + f[3], f[1] - f[4], f[1] + f[4], f[2] - f[5], f[2] + f[5]};
+        const float mn = fminf(f[3] - fabsf(x - f[0]), fminf(f[4] - fabsf(y - f[1]), f[5] - fabsf(z - f[2])));
+        const float eb = e + f[F_BAND];
+        float tt;
+        if (mn > eb) {
+            tt = kFar;
+            const float p[3] = {x, y, z}, v[3] = {c.vx, c.vy, c.vz};
+            for (int a = 0; a < 3; a++) tt = fminf(tt, slab_curve(p[a], v[a], bb[2 * a], bb[2 * a + 1], eb, M, true));
+        } else if (mn < -eb) {
+            tt = 0.0f;
+            const float p[3] = {x, y, z}, v[3] = {c.vx, c.vy, c.vz};
+            for (int a = 0; a < 3; a++) tt = fmaxf(tt, slab_curve(p[a], v[a], bb[2 * a], bb[2 * a + 1], eb, M, false));
+        } else {
+            tt = 0.0f;
+        }
+        t = fmaxf(t, tt);
+        return rho;
+    }
+    case N_CYL: {
+        // axis v (f[3..5]), 1/|v|^2 f[6], r f[8], |v| f[9]: axial coordinate
+        // a = (q - p0).v/|v| in [0, |v|], radial part across the axis
+        const float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        const float il = f[9] * f[6];  // 1/|v|
+        const float a = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * il;
+        const float va = fmaf(c.vz, f[5], fmaf(c.vy, f[4], c.vx * f[3])) * il;
+        const float cc = a * il;
+        const float px = fmaf(-cc, f[3], wx), py = fmaf(-cc, f[4], wy), pz = fmaf(-cc, f[5], wz);
+        const float ca = va * il;
+        const float qx = fmaf(-ca, f[3], c.vx), qy = fmaf(-ca, f[4], c.vy), qz = fmaf(-ca, f[5], c.vz);
+        const float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
+        const float pv = fmaf(pz, qz, fmaf(py, qy, px * qx));
+        const float r = f[8], br = sqrtf(f[F_BAND]);
+        const float ea = e + f[F_BAND2] * f[9];  // band of c as an axial distance
+        const bool in_r = p2 < r * r, in_a = a > 0.0f && a < f[9];
+        float tt;
+        if (rho != 0.0f || (in_r && in_a)) {  // inside both: the earlier exit
+            tt = fminf(radius_curve(p2, pv, r, e + br, c.vmax, c.acc, true),
+                       slab_curve(a, va, 0.0f, f[9], ea, M, true));
+        } else {  // entering needs both: the later arrival of the violated ones
+            tt = 0.0f;
+            if (!in_r) tt = fmaxf(tt, radius_curve(p2, pv, r, e + br, c.vmax, c.acc, false));
+            if (!in_a) tt = fmaxf(tt, slab_curve(a, va, 0.0f, f[9], ea, M, false));
+        }
+        t = fmaxf(t, tt);
+        return rho;
+    }
+    case N_PPD: {
+        const float wx = x - f[0], wy = y - f[1], wz = z - f[2];
+        const float b = f[F_BAND];
+        float q[3], qv[3], ea[3], Ma[3];
+        float mrel = 3.0e38f;
+        bool out = false;
+        for (int k = 0; k < 3; k++) {
+            const float* rr = f + 3 + 3 * k;
+            q[k] = fmaf(rr[2], wz, fmaf(rr[1], wy, rr[0] * wx));
+            qv[k] = fmaf(rr[2], c.vz, fmaf(rr[1], c.vy, rr[0] * c.vx));
+            ea[k] = fmaf(e, f[12 + k], b);
+            Ma[k] = M * f[12 + k];
+            const float in = fminf(q[k], 1.0f - q[k]);
+            mrel = fminf(mrel, in - ea[k]);
+            out = out || in < -ea[k];
+        }
+        float tt = 0.0f;
+        if (out) {
+            for (int k = 0; k < 3; k++) tt = fmaxf(tt, slab_curve(q[k], qv[k], 0.0f, 1.0f, ea[k], Ma[k], false));
+        } else if (mrel > 0.0f) {
+            tt = kFar;
+            for (int k = 0; k < 3; k++) tt = fminf(tt, slab_curve(q[k], qv[k], 0.0f, 1.0f, ea[k], Ma[k], true));
+        }
+        t = fmaxf(t, tt);
+        return rho;
+    }
+    default: break;
+    }
+    if (n.type != N_GYROID) return rho;
     const float is = f[3], ais = fabsf(is);
     float X = (x - f[0]) * is, Y = (y - f[1]) * is, Z = (z - f[2]) * is;
     float sx, cx, sy, cy, sz, cz;
@@ -1494,17 +1616,17 @@ XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c
     // error of g1 (trigonometry, velocity, position) and of g (position slack)
     const float dg1 = fmaf(1e-5f, fabsf(g1), ais * c.vmax * fmaf(16.0f * ais, c.eps, 1e-5f));
     const float eg = 2.4494898f * ais * c.eps;
-    const float M = fmaf(4.0f * is * is, c.vmax * c.vmax, 2.4494898f * ais * c.acc) * 1.01f + 1e-20f;
+    const float Mg = fmaf(4.0f * is * is, c.vmax * c.vmax, 2.4494898f * ais * c.acc) * 1.01f + 1e-20f;
     const float th = f[4], band = f[F_BAND];
     float t2 = 0.0f;
     if (th - fabsf(g) > band) {  // inside |g| < th: both edges of the band
         const float T = th - band - eg;
         if (T - fabsf(g) > 0.0f)
-            t2 = fminf(gap_time(T - g, g1 + dg1, M), gap_time(T + g, -g1 + dg1, M));
+            t2 = fminf(gap_time(T - g, g1 + dg1, Mg), gap_time(T + g, -g1 + dg1, Mg));
     } else {  // outside: the nearer edge
         const float T = th + band + eg;
-        if (g > T) t2 = gap_time(g - T, -g1 + dg1, M);
-        else if (g < -T) t2 = gap_time(-T - g, g1 + dg1, M);
+        if (g > T) t2 = gap_time(g - T, -g1 + dg1, Mg);
+        else if (g < -T) t2 = gap_time(-T - g, g1 + dg1, Mg);
     }
     t = fmaxf(t, t2);
     return rho;
@@ -1591,8 +1713,26 @@ XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z
         if (iy < G - 1) m = fminf(m, ((float)(iy + 1) - uy) / c.f[4]);
         if (iz > 0) m = fminf(m, (uz - (float)iz) / c.f[5]);
         if (iz < G - 1) m = fminf(m, ((float)(iz + 1) - uz) / c.f[5]);
+        // the cell's inner faces along the curve (world distance = grid distance * cell size)
+        float tf = kFar;
+        {
+            const float M = u.acc * 1.01f + 1e-20f;
+            const float gu[3] = {ux, uy, uz}, vv[3] = {u.vx, u.vy, u.vz};
+            const int ii[3] = {ix, iy, iz};
+            for (int a = 0; a < 3; a++) {
+                const float h = c.f[8 + a];
+                if (ii[a] > 0) {
+                    const float gap = (gu[a] - (float)ii[a]) * h - u.eps;
+                    tf = gap > 0.0f ? fminf(tf, gap_time(gap, -vv[a] + 1e-6f * u.vmax, M)) : 0.0f;
+                }
+                if (ii[a] < G - 1) {
+                    const float gap = ((float)(ii[a] + 1) - gu[a]) * h - u.eps;
+                    tf = gap > 0.0f ? fminf(tf, gap_time(gap, vv[a] + 1e-6f * u.vmax, M)) : 0.0f;
+                }
+            }
+        }
         const int cell = f2i(c.f[6]) + (iz * G + iy) * G + ix;
-        t = curve_time(fmaxf(fmaxf(m, 0.0f), S.clear[cell]), u);
+        t = fmaxf(fmaxf(curve_time(fmaxf(fmaxf(m, 0.0f), S.clear[cell]), u), fminf(tf, kFar)), 0.0f);
         const int32_t* off = S.cells + cell;
         list = S.items + off[0];
         cnt = off[1] - off[0];
@@ -1600,10 +1740,17 @@ XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z
     const bool greedy = (c.flags & C_GREEDY) != 0;
     float sum = 0.0f, sabs = 0.0f;
     bool unc = false, done = false;
+    // uniform greedy collections: inside a child (for certain) its exit alone
+    // bounds the curve (see coll_dr_uniform)
+    const bool uniform = (c.flags & C_UNIFORM) != 0;
     for (int k = 0; k < cnt; k++) {
         int slot = list ? list[k] : k;
         float tk;
         float r = item_dc<D>(S, kids[slot], x, y, z, u, tk);
+        if (uniform && !unc && r > 0.0f) {
+            t = tk;
+            return r;
+        }
         t = fminf(t, tk);
         if (done) continue;
         if (isunc(r)) {
