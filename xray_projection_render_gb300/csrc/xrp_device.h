@@ -1436,9 +1436,12 @@ XRP_HD void deform_jvp32(const SceneDev& S, float& x, float& y, float& z, float&
 }
 
 // First tau > 0 at which D - w tau - M tau^2 / 2 can reach 0 (gap D > 0
-// closing at speed w, curvature M > 0): the positive root, stable form.
+// closing at speed w, curvature M > 0): the positive root, in the form
+// without cancellation for each sign of w (moving away, the rationalised
+// form would divide by a difference that FP32 can round to 0).
 XRP_HD float gap_time(float D, float w, float M) {
-    return 2.0f * D / (w + sqrtf(fmaf(w, w, 2.0f * M * D)));
+    const float s = sqrtf(fmaf(w, w, 2.0f * M * D));
+    return w >= 0.0f ? 2.0f * D / (w + s) : (s - w) / M;
 }
 
 // A ball margin m (object units) as a ray-parameter bound along the curve.
