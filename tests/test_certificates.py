@@ -288,3 +288,28 @@ def test_curve_tessellated_lattice_under_gaussian():
     w = W.deformed_lattice()
     c, n = check_curve(w.obj, GAUSS, n=600)
     assert c > n // 3
+
+
+def test_curve_near_faces_moving_away_under_strong_bending():
+    # points just outside a box's faces, moving away, under a sharp sigmoid:
+    # the curve can turn back, and the bound must see it (the root of the
+    # gap equation without cancellation)
+    obj = {"type": "box", "center": [0.0, 0.0, 0.0], "sides": [0.8, 0.8, 0.8], "rho": 1.0}
+    d = {"type": "sigmoid", "amplitude": 0.3, "center": 0.05, "lengthscale": 0.05, "direction": "x"}
+    rng = np.random.default_rng(3)
+    n = 600
+    face = rng.integers(0, 3, n)
+    side = rng.choice([-1.0, 1.0], n)
+    P = rng.uniform(-0.35, 0.35, (n, 3))
+    P[np.arange(n), face] = side * (0.4 + rng.uniform(1e-4, 3e-3, n))
+    D = rng.normal(size=(n, 3))
+    D[np.arange(n), face] = side * np.abs(D[np.arange(n), face])  # away from the face
+    D /= np.linalg.norm(D, axis=1, keepdims=True)
+    rho, t = hostsim.curve_bound(obj, P, D, deformation=d)
+    sc = O.Scene(obj, d)
+    for k in range(n):
+        if not (t[k] > 0) or np.isnan(rho[k]):
+            continue
+        r0 = sc.density(*P[k])
+        for tau in np.linspace(0.0, min(float(t[k]), 4.0), 17):
+            assert sc.density(*(P[k] + D[k] * tau)) == r0, (k, P[k], D[k], float(t[k]), tau)
