@@ -845,956 +845,12 @@ XRP_HD float dens_margin32(const SceneDev& S, float x, float y, float z, float& 
     return rho;
 }
 
-// ---------------------------------------------------------------------------
-// Ray certificates.  When the deformation chain is affine (linear, affine,
-// rigid or none) the samples ahead of a point lie on a straight line in
-// object coordinates, w + u t, with u the chain's linear part applied to the
-// ray direction (per unit of the ray parameter).  Instead of a ball around
-// the sample, the bound is a ray parameter t before which the line cannot
-// come within `eps` of a place where the density changes: the first
-// crossing of each primitive's boundary inflated (outside) or shrunk
-// (inside) by eps, of a tessellation cell face, of a candidate-list cell
-// face.  All points within eps of the segment [w, w + u t] (a capsule) then
-// have the density of the sample.  eps (SceneDev::ray_slack) covers the
-// position error of the FP32 sample, the direction error over the sampled
-// span and the FP32 arithmetic of the crossings, as m_slack does for balls.
-// Every bound is also at least the ball bound (distance - eps) / |u|.
-// ---------------------------------------------------------------------------
-struct RayDir {
-    float x, y, z;     // object-space direction per unit ray parameter
-    float ix, iy, iz;  // reciprocals of the components (0 for a zero component)
-    float a;           // |u|^2
-    float il;          // 1 / |u|
-    float eps;         // capsule radius (object units)
-};
+}  // namespace xrp
 
-constexpr float kFar = 3.0e38f;
-constexpr float kU32 = 5.9604645e-8f;  // 2^-24
+#include "xrp_cert_ray.h"
+#include "xrp_cert_curve.h"
 
-// Reciprocal and reciprocal square root of the crossing arithmetic: the
-// hardware approximations on the device (a few ulp; the final bound is
-// scaled by 1 - 1e-5 and the capsule radius budgets relative errors of the
-// crossings), exact division on the host build.
-XRP_HD float frcp(float x) {
-#if defined(__CUDA_ARCH__)
-    return __fdividef(1.0f, x);
-#else
-    return 1.0f / x;
-#endif
-}
-
-XRP_HD float frsqrt(float x) {
-#if defined(__CUDA_ARCH__)
-    return rsqrtf(x);
-#else
-    return 1.0f / sqrtf(x);
-#endif
-}
-
-// Square root of the crossing arithmetic (relative error within 2^-23 on
-// the device; the bounds that use it budget for it).
-XRP_HD float fsqrt(float x) {
-#if defined(__CUDA_ARCH__)
-    float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-#else
-    return sqrtf(x);
-#endif
-}
-
-// A direction component this small counts as zero (the slab is parallel).
-XRP_HD float rcp_dir(float d) { return fabsf(d) > 1e-30f ? frcp(d) : 0.0f; }
-
-// Object-space direction of a ray (linear parts of an affine chain).
-XRP_HD RayDir ray_dir32(const SceneDev& S, const float* d) {
-    float x = d[0], y = d[1], z = d[2];
-    for (int i = 0; i < S.ndefs; i++) {
-        const DefStep& s = S.defs[i];
-        const float* a = s.f;
-        if (s.type == D_LINEAR) {
-            float nx = fmaf(a[4], z, fmaf(a[5], y, fmaf(a[0], x, x)));
-            float ny = fmaf(a[3], z, fmaf(a[1], y, fmaf(a[5], x, y)));
-            float nz = fmaf(a[2], z, fmaf(a[3], y, fmaf(a[4], x, z)));
-            x = nx; y = ny; z = nz;
-        } else if (s.type == D_AFFINE) {
-            float nx = fmaf(a[2], z, fmaf(a[1], y, a[0] * x));
-            float ny = fmaf(a[5], z, fmaf(a[4], y, a[3] * x));
-            float nz = fmaf(a[8], z, fmaf(a[7], y, a[6] * x));
-            x = nx; y = ny; z = nz;
-        }
-    }
-    RayDir u;
-    u.x = x; u.y = y; u.z = z;
-    u.ix = rcp_dir(x); u.iy = rcp_dir(y); u.iz = rcp_dir(z);
-    u.a = fmaf(z, z, fmaf(y, y, x * x));
-    u.il = 1.0f / sqrtf(u.a);
-    u.eps = S.ray_slack;
-    return u;
-}
-
-// Slab q + dq t inside (lo, hi), idq = 1/dq (0: parallel): exit parameter
-// of the shrunk slab [lo + e, hi - e] for a point inside it.
-XRP_HD float slab_exit(float q, float idq, float lo, float hi, float e) {
-    if (idq > 0.0f) return (hi - e - q) * idq;
-    if (idq < 0.0f) return (lo + e - q) * idq;
-    return kFar;
-}
-
-// Slab q + dq t inside the inflated slab (lo - e, hi + e): narrows [tlo, thi].
-XRP_HD void slab_clip(float q, float idq, float lo, float hi, float e, float& tlo, float& thi) {
-    if (idq != 0.0f) {
-        float a = (lo - e - q) * idq, b = (hi + e - q) * idq;
-        tlo = fmaxf(tlo, fminf(a, b));
-        thi = fminf(thi, fmaxf(a, b));
-    } else if (!(q > lo - e && q < hi + e)) {
-        tlo = kFar;
-    }
-}
-
-// Spheres and cylinders: the line w + u t against a ball (3-D) or a disc
-// (the projection of a cylinder across its axis) of radius R about the
-// origin, from the closest approach tc = -b/a and the half chord
-// sqrt(R^2 - h^2), h^2 = c2/a the squared distance of the line from the
-// origin (c2 = |w x u|^2, stable near tangency).  `err` bounds the FP32
-// error of the half chord (large only when the line is nearly tangent, where
-// the ball bound takes over); a line within eps/2 of tangency to the
-// inflated ball stays clear of the true one.  Outside, R = r + eps and the
-// entry interval is widened by err; inside, R = r - eps and the exit is
-// shrunk by it.
-
-// Every partial bound below is clamped with fmaxf(., 0) before it enters a
-// minimum, so that a NaN (never expected) can only shorten a jump.
-
-// Sphere of radius r, point w from the centre at signed distance g.
-XRP_HD float sphere_ray(float wx, float wy, float wz, float g, float r, const RayDir& u, float tcap) {
-    const float eps = u.eps;
-    const float ag = fabsf(g) - eps;
-    if (!(ag > 0.0f)) return 0.0f;
-    const float tb = ag * u.il;
-    if (tb >= tcap) return tb;  // cannot lower the caller's minimum
-    // inside: exit of the ball shrunk by eps; outside: entry of the ball
-    // inflated by eps (one straight-line computation for both)
-    const bool in = g < 0.0f;
-    const float sg = in ? -1.0f : 1.0f;
-    const float b = fmaf(wz, u.z, fmaf(wy, u.y, wx * u.x));
-    const float cx = fmaf(wy, u.z, -wz * u.y), cy = fmaf(wz, u.x, -wx * u.z), cz = fmaf(wx, u.y, -wy * u.x);
-    const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
-    const float wl1 = fabsf(wx) + fabsf(wy) + fabsf(wz);
-    const float R = fmaf(sg, eps, r);
-    const float ia = u.il * u.il;
-    const float h2 = c2 * ia;
-    const float tc = -b * ia;
-    const float ch = fsqrt(fmaxf(fmaf(R, R, -h2), 0.0f));
-    const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
-    const float half = fmaf(sg, err, ch) * u.il;  // widened outside, shrunk inside
-    float t = in ? tc + half : tc - half;
-    // outside: moving away (the distance only grows), or within eps/2 of
-    // tangency (never reaches the true ball)
-    const float Rt = R - 0.5f * eps;
-    if (!in && (!(b < 0.0f) || !(h2 < Rt * Rt))) t = kFar;
-    return fmaxf(t, tb);
-}
-
-// Finite cylinder: w from p0, axial fraction c, perpendicular part p, radial
-// and axial signed distances gr, ga (negative inside).
-// Inside (g < -eps) the bound is the exit of the cylinder shrunk by eps,
-// outside (g > eps) the entry of the cylinder inflated by eps: the axial
-// slab and the radial chord are intervals of t either way, so both cases run
-// the same straight-line code (lanes of a warp inside and outside struts do
-// not diverge).
-// v: the axis p1 - p0, ivv = 1/|v|^2, vl = |v|, bc: the band of c.
-XRP_HD float cyl_ray(float vx, float vy, float vz, float ivv, float r, float vl, float bc, float c,
-                     float px, float py, float pz, float gr, float ga, const RayDir& u, float tcap) {
-    const float eps = u.eps;
-    const float g = fmaxf(gr, ga);
-    if (!(fabsf(g) > eps)) return 0.0f;
-    const float tb = (fabsf(g) - eps) * u.il;
-    if (tb >= tcap) return tb;  // cannot lower the caller's minimum
-    const bool in = g < 0.0f;
-    const float sg = in ? -1.0f : 1.0f;
-    // axial: c + cu t inside (-es, 1 + es), es = +-(eps / |v| + band of c)
-    const float cu = fmaf(u.z, vz, fmaf(u.y, vy, u.x * vx)) * ivv;
-    const float icu = rcp_dir(cu);
-    const float es = sg * fmaf(eps, vl * ivv, bc);
-    float alo = -kFar, ahi = kFar;
-    if (icu != 0.0f) {
-        const float a1 = (-es - c) * icu, a2 = (1.0f + es - c) * icu;
-        alo = fminf(a1, a2);
-        ahi = fmaxf(a1, a2);
-    } else if (!in && !(c > -es && c < 1.0f + es)) {
-        alo = kFar;
-    }
-    // radial: the line's projection against the disc of radius r +- eps
-    const float qx = fmaf(-cu, vx, u.x), qy = fmaf(-cu, vy, u.y), qz = fmaf(-cu, vz, u.z);
-    const float a = fmaf(qz, qz, fmaf(qy, qy, qx * qx));
-    float rlo = -kFar, rhi = kFar;
-    if (a > 1e-12f * u.a) {
-        const float b = fmaf(pz, qz, fmaf(py, qy, px * qx));
-        const float cx = fmaf(py, qz, -pz * qy), cy = fmaf(pz, qx, -px * qz), cz = fmaf(px, qy, -py * qx);
-        const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
-        const float wl1 = fabsf(px) + fabsf(py) + fabsf(pz);
-        const float R = fmaf(sg, eps, r);
-        const float ia = frcp(a);
-        const float h2 = c2 * ia;
-        const float tc = -b * ia;
-        const float ch = fsqrt(fmaxf(fmaf(R, R, -h2), 0.0f));
-        const float err = 4.0f * kU32 * (fmaf(8.0f * wl1, R, 3.0f * R * R) * frcp(ch) + 4.0f * (wl1 + R));
-        const float half = fmaf(sg, err, ch) * frsqrt(a);  // widened outside, shrunk inside
-        rlo = tc - half;
-        rhi = tc + half;
-        // outside, a line within eps/2 of tangency never reaches the true disc
-        const float Rt = R - 0.5f * eps;
-        if (!in && !(h2 < Rt * Rt)) rlo = kFar;
-    } else if (a > 0.0f) {  // nearly parallel to the axis: the radius changes at rate |u_perp|
-        const float tr = (fabsf(gr) - eps) * frsqrt(a);
-        if (in) rhi = tr;
-        else if (gr > eps) rlo = tr;
-    } else if (!in && gr > eps) {
-        rlo = kFar;
-    }
-    float t;
-    if (in) {
-        t = fminf(ahi, rhi);
-    } else {
-        const float lo = fmaxf(fmaxf(alo, rlo), 0.0f), hi = fminf(ahi, rhi);
-        t = lo <= hi ? lo : kFar;
-    }
-    return fmaxf(fmaxf(t, 0.0f), tb);
-}
-
-// Axis-aligned box of half sides h (F_BAND b): point w from the centre,
-// mn = min(h - |w|).
-XRP_HD float box_ray(const float* h, float wx, float wy, float wz, float mn, float b, const RayDir& u) {
-    const float e = u.eps + b;
-    if (!(fabsf(mn) > e)) return 0.0f;
-    // inside: exit of the box shrunk by e; outside: entry of the box
-    // inflated by e
-    const bool in = mn > 0.0f;
-    const float es = in ? -e : e;
-    float lo = 0.0f, hi = kFar;
-    slab_clip(wx, u.ix, -h[0], h[0], es, lo, hi);
-    slab_clip(wy, u.iy, -h[1], h[1], es, lo, hi);
-    slab_clip(wz, u.iz, -h[2], h[2], es, lo, hi);
-    return in ? fmaxf(hi, 0.0f) : (lo <= hi ? lo : kFar);
-}
-
-// Leaf density (leaf_dm's decisions) and its ray bound t.  `tcap`: the
-// caller's current minimum; a bound at or above it may be returned without
-// its exact value (it cannot lower the minimum).
-XRP_HD float leaf_dr(const Node& n, float x, float y, float z, const RayDir& u, float tcap, float& t) {
-    const float* f = n.f;
-    switch (n.type) {
-    case N_SPHERE: {
-        const F4 a = ld4(f), c4 = ld4(f + 4), tb = ld4(f + 24);  // centre, r^2; r; bands, rho
-        float dx = x - a.x, dy = y - a.y, dz = z - a.z;
-        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        t = sphere_ray(dx, dy, dz, fsqrt(d2) - c4.x, c4.x, u, tcap);
-        float q = d2 - a.w;
-        if (q < -tb.z) return tb.w;
-        if (q > tb.z) return 0.0f;
-        return xnan();
-    }
-    case N_BOX: {
-        const F4 a = ld4(f), c4 = ld4(f + 4), tb = ld4(f + 24);  // centre, half sides; bands, rho
-        const float h[3] = {a.w, c4.x, c4.y};
-        float wx = x - a.x, wy = y - a.y, wz = z - a.z;
-        float mn = fminf(h[0] - fabsf(wx), fminf(h[1] - fabsf(wy), h[2] - fabsf(wz)));
-        float b = tb.z;
-        t = box_ray(h, wx, wy, wz, mn, b, u);
-        if (mn > b) return tb.w;
-        if (mn < -b) return 0.0f;
-        return xnan();
-    }
-    case N_CYL: {
-        // a: p0, v.x; c4: v.y, v.z, 1/|v|^2, r^2; e: r, |v|; tb: bands, rho
-        const F4 a = ld4(f), c4 = ld4(f + 4), e = ld4(f + 8), tb = ld4(f + 24);
-        float wx = x - a.x, wy = y - a.y, wz = z - a.z;
-        float c = fmaf(wz, c4.y, fmaf(wy, c4.x, wx * a.w)) * c4.z;
-        float px = fmaf(-c, a.w, wx), py = fmaf(-c, c4.x, wy), pz = fmaf(-c, c4.y, wz);
-        float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
-        float bc = tb.y;
-        t = cyl_ray(a.w, c4.x, c4.y, c4.z, e.x, e.y, bc, c, px, py, pz, fsqrt(p2) - e.x,
-                    fmaxf(-c, c - 1.0f) * e.y, u, tcap);
-        if (c < -bc || c > 1.0f + bc) return 0.0f;
-        float q = p2 - c4.w;
-        float bd = tb.z;
-        if (q > bd) return 0.0f;
-        if (q < -bd && c > bc && c < 1.0f - bc) return tb.w;
-        return xnan();
-    }
-    case N_PPD: {
-        float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-        float b = f[F_BAND];
-        float q[3], iqu[3], e[3];
-        float mn = 3.0e38f, mrel = 3.0e38f;
-        bool out = false;
-        for (int a = 0; a < 3; a++) {
-            const float* r = f + 3 + 3 * a;
-            q[a] = fmaf(r[2], wz, fmaf(r[1], wy, r[0] * wx));
-            iqu[a] = rcp_dir(fmaf(r[2], u.z, fmaf(r[1], u.y, r[0] * u.x)));
-            e[a] = fmaf(u.eps, f[12 + a], b);
-            float in = fminf(q[a], 1.0f - q[a]);
-            mn = fminf(mn, in);
-            mrel = fminf(mrel, in - e[a]);
-            out = out || in < -e[a];
-        }
-        // inside (every slab at least e inside): exit of the shrunk slabs;
-        // outside (some slab more than e outside): entry of the inflated
-        // ones; else 0
-        if (out || mrel > 0.0f) {
-            float lo = 0.0f, hi = kFar;
-            for (int a = 0; a < 3; a++) slab_clip(q[a], iqu[a], 0.0f, 1.0f, out ? e[a] : -e[a], lo, hi);
-            t = out ? (lo <= hi ? lo : kFar) : fmaxf(hi, 0.0f);
-        } else {
-            t = 0.0f;
-        }
-        if (mn > b) return f[F_RHO];
-        if (mn < -b) return 0.0f;
-        return xnan();
-    }
-    case N_GYROID: {
-        float X = (x - f[0]) * f[3], Y = (y - f[1]) * f[3], Z = (z - f[2]) * f[3];
-        float sx, cx, sy, cy, sz, cz;
-        f_sincos(X, &sx, &cx);
-        f_sincos(Y, &sy, &cy);
-        f_sincos(Z, &sz, &cz);
-        float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
-        float q = f[4] - fabsf(g);
-        float m = fmaxf(fabsf(q) - f[F_BAND], 0.0f) / (2.4494898f * fabsf(f[3]));
-        t = fmaxf(m - u.eps, 0.0f) * u.il;
-        if (q > f[F_BAND]) return f[F_RHO];
-        if (q < -f[F_BAND]) return 0.0f;
-        return xnan();
-    }
-    default: t = 0.0f; return xnan();
-    }
-}
-
-// Box [lo, hi] (per axis, interleaved lo0 hi0 lo1 hi1 ...): exit of the box
-// shrunk by e for a point at least e inside, entry of the box inflated by e
-// for a point more than e outside, else 0.  `in` is the point's smallest
-// distance to a face (negative outside).
-XRP_HD float bounds_ray(const float* b, float x, float y, float z, float in, float e, const RayDir& u) {
-    if (!(fabsf(in) > e)) return 0.0f;
-    const bool inside = in > 0.0f;
-    const float es = inside ? -e : e;
-    float lo = 0.0f, hi = kFar;
-    slab_clip(x, u.ix, b[0], b[1], es, lo, hi);
-    slab_clip(y, u.iy, b[2], b[3], es, lo, hi);
-    slab_clip(z, u.iz, b[4], b[5], es, lo, hi);
-    return inside ? fmaxf(hi, 0.0f) : (lo <= hi ? lo : kFar);
-}
-
-template <int D, bool UNI = false>
-XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float tcap,
-                     float& t);
-
-// item_dm's decisions; t: the ray bound (tessellations: the outer bounds,
-// the cell faces of the fold and the unit-cell bounds cap the collection's).
-template <int D>
-XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const RayDir& u, float tcap,
-                     float& t) {
-    const Node& n = S.nodes[id];
-    if (n.type <= N_GYROID) return leaf_dr(n, x, y, z, u, tcap, t);
-    if (n.type == N_TESS) {
-        if constexpr (D > 0) {
-            // node layout as in item32
-            const F4 f0 = ld4(n.f), f4 = ld4(n.f + 4), f8 = ld4(n.f + 8), f12 = ld4(n.f + 12);
-            const F4 f16 = ld4(n.f + 16), f20 = ld4(n.f + 20);
-            const float ob[6] = {f0.x, f0.y, f0.z, f0.w, f4.x, f4.y};
-            const float ub[6] = {f4.w, f8.x, f8.y, f8.z, f8.w, f12.x};
-            float mo = fminf(fminf(fminf(x - ob[0], ob[1] - x), fminf(y - ob[2], ob[3] - y)),
-                             fminf(z - ob[4], ob[5] - z));
-            const float to = bounds_ray(ob, x, y, z, mo, u.eps + f4.z, u);
-            if (mo < -f4.z) { t = to; return 0.0f; }  // outside: zero up to the bounds
-            if (!(mo > f4.z)) { t = 0.0f; return xnan(); }
-            float qx = (x - f20.x) * f16.y, qy = (y - f20.y) * f16.z, qz = (z - f20.z) * f16.w;
-            float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
-            float bq = f20.w;
-            float frx = qx - nx, fry = qy - ny, frz = qz - nz;
-            float fr = fminf(fminf(fminf(frx, 1.0f - frx), fminf(fry, 1.0f - fry)), fminf(frz, 1.0f - frz));
-            if (!(fr > bq)) { t = 0.0f; return xnan(); }
-            // exit of this tessellation cell (q units; eps scaled by 1/cell
-            // size; 1/(u f17) = (1/u) f14: f14 is the cell size, f17 its
-            // reciprocal)
-            float tc = fminf(fminf(fmaxf(slab_exit(frx, u.ix * f12.z, 0.0f, 1.0f, fmaf(u.eps, fabsf(f16.y), bq)), 0.0f),
-                                   fmaxf(slab_exit(fry, u.iy * f12.w, 0.0f, 1.0f, fmaf(u.eps, fabsf(f16.z), bq)), 0.0f)),
-                             fmaxf(slab_exit(frz, u.iz * f16.x, 0.0f, 1.0f, fmaf(u.eps, fabsf(f16.w), bq)), 0.0f));
-            const float tt = fminf(to, tc);
-            float fx = fmaf(-f12.z, nx, x), fy = fmaf(-f12.w, ny, y), fz = fmaf(-f16.x, nz, z);
-            float mu = fminf(fminf(fminf(fx - ub[0], ub[1] - fx), fminf(fy - ub[2], ub[3] - fy)),
-                             fminf(fz - ub[4], ub[5] - fz));
-            const float tu = bounds_ray(ub, fx, fy, fz, mu, u.eps + f12.y, u);
-            if (mu < -f12.y) { t = fminf(tt, tu); return 0.0f; }  // outside the unit-cell bounds
-            if (!(mu > f12.y)) { t = 0.0f; return xnan(); }
-            float tk;
-            const float tm = fminf(fminf(tt, tu), tcap);
-            // unit cells are where uniform greedy collections occur (lattices)
-            float r = coll_dr<D - 1, true>(S, S.nodes[n.a], fx, fy, fz, u, tm, tk);
-            t = fminf(fminf(tt, tu), tk);
-            return r;
-        }
-    }
-    t = 0.0f;  // voxel grids and anything deeper: density by the plain path
-    if (n.type == N_VOXEL) return voxel32(S.vols[n.a], n.f[0], x, y, z, S.hier_zero_guard);
-    return xnan();
-}
-
-// Uniform greedy collections (every child a leaf of the same density > 0):
-// the decisions of coll_dm; inside a child (for certain) the density is
-// that child's whatever the others do, so its exit alone bounds the ray (no
-// list-cell cap, no other candidate).  `t` holds the list-cell cap on entry.
-XRP_HD float coll_dr_uniform(const SceneDev& S, const int32_t* kids, const int32_t* list, int cnt, float x,
-                             float y, float z, const RayDir& u, float tcap, float& t) {
-    for (int k = 0; k < cnt; k++) {
-        const int slot = list ? list[k] : k;
-        float tk;
-        const float r = leaf_dr(S.nodes[kids[slot]], x, y, z, u, tcap, tk);
-        if (isunc(r)) {  // an undecided child before any certain one
-            t = 0.0f;
-            return r;
-        }
-        if (r > 0.0f) {
-            t = tk;
-            return r;
-        }
-        t = fminf(t, tk);
-    }
-    return 0.0f;  // outside every candidate (greedy sum of zeros, clipped)
-}
-
-// coll_dm's decisions; t: the minimum over the candidates, capped (with
-// candidate lists) by the later of the exit from the point's list cell and
-// the clearance of the unlisted children.
-// UNI: the collection may be uniform (unit cells of tessellations); the
-// uniform path is compiled only there, which keeps it out of the kernels of
-// scenes without tessellations.
-template <int D, bool UNI>
-XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z, const RayDir& u, float tcap,
-                     float& t) {
-    const int32_t* kids = S.child + c.a;
-    int cnt = c.b;
-    const int32_t* list = nullptr;
-    t = kFar;
-    if (c.flags & C_ACCEL) {
-        int G = (c.flags >> 16) & 0xff;
-        // f[0..2] grid origin, f[3..5] 1/cell size, f[6] cell base, f[8..10] cell size
-        const F4 g0 = ld4(c.f), g4 = ld4(c.f + 4), g8 = ld4(c.f + 8);
-        const float cf[11] = {g0.x, g0.y, g0.z, g0.w, g4.x, g4.y, g4.z, g4.w, g8.x, g8.y, g8.z};
-        float ux = (x - cf[0]) * cf[3], uy = (y - cf[1]) * cf[4], uz = (z - cf[2]) * cf[5];
-        int ix = (int)floorf(ux), iy = (int)floorf(uy), iz = (int)floorf(uz);
-        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
-        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
-        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
-        // inner faces only (the outer cells extend to infinity by the clamp)
-        float tc = kFar;
-        {
-            // grid units; 1/(u f3) = (1/u) f8 (f8: the cell size)
-            const float dx = u.ix * cf[8], ex = u.eps * cf[3];
-            if (dx > 0.0f && ix < G - 1) tc = fminf(tc, fmaxf(((float)(ix + 1) - ex - ux) * dx, 0.0f));
-            if (dx < 0.0f && ix > 0) tc = fminf(tc, fmaxf(((float)ix + ex - ux) * dx, 0.0f));
-            const float dy = u.iy * cf[9], ey = u.eps * cf[4];
-            if (dy > 0.0f && iy < G - 1) tc = fminf(tc, fmaxf(((float)(iy + 1) - ey - uy) * dy, 0.0f));
-            if (dy < 0.0f && iy > 0) tc = fminf(tc, fmaxf(((float)iy + ey - uy) * dy, 0.0f));
-            const float dz = u.iz * cf[10], ez = u.eps * cf[5];
-            if (dz > 0.0f && iz < G - 1) tc = fminf(tc, fmaxf(((float)(iz + 1) - ez - uz) * dz, 0.0f));
-            if (dz < 0.0f && iz > 0) tc = fminf(tc, fmaxf(((float)iz + ez - uz) * dz, 0.0f));
-        }
-        int cell_base = f2i(cf[6]);
-        const int cell = cell_base + (iz * G + iy) * G + ix;
-        t = fmaxf(tc, fmaxf(S.clear[cell] - u.eps, 0.0f) * u.il);
-        const int32_t* off = S.cells + cell;
-        int s0 = off[0], s1 = off[1];
-        list = S.items + s0;
-        cnt = s1 - s0;
-    }
-    const bool greedy = (c.flags & C_GREEDY) != 0;
-    if constexpr (UNI) {
-        if (c.flags & C_UNIFORM) return coll_dr_uniform(S, kids, list, cnt, x, y, z, u, tcap, t);
-    }
-    float sum = 0.0f, sabs = 0.0f;
-    bool unc = false, done = false;
-    for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
-        float tk;
-        float r = item_dr<D>(S, kids[slot], x, y, z, u, fminf(t, tcap), tk);
-        t = fminf(t, tk);
-        if (done) continue;  // greedy value fixed; bounds of the rest still count
-        if (isunc(r)) {
-            unc = true;
-            done = true;
-            continue;
-        }
-        if (greedy && r > 0.0f) {
-            sum = r;
-            sabs = fabsf(r);
-            done = true;
-            continue;
-        }
-        sum += r;
-        sabs += fabsf(r);
-    }
-    if (unc) return xnan();
-    if (greedy && done) return sum;
-    if (!(c.flags & C_EXACT_SUM) && sabs > 0.0f && fabsf(sum) <= c.f[7] * sabs) return xnan();
-    if (c.flags & C_CLIP) sum = fminf(fmaxf(sum, 0.0f), 1.0f);
-    return sum;
-}
-
-// density32 at one point and the ray bound t (ray parameter units) of the
-// samples ahead that share its density; affine chains only.  Bounds at or
-// above `tcap` (the end of the caller's range) need not be exact.
-template <int DEPTH, bool DEFS>
-XRP_HD float dens_ray32(const SceneDev& S, float x, float y, float z, const RayDir& u, float tcap, float& t) {
-    if constexpr (DEFS) deform32(S, x, y, z);
-    const Node& r = S.nodes[S.root];
-    float rho;
-    if (r.type <= N_GYROID) rho = leaf_dr(r, x, y, z, u, tcap, t);
-    else if (r.type == N_COLL) rho = coll_dr<DEPTH>(S, r, x, y, z, u, tcap, t);
-    else rho = item_dr<DEPTH>(S, S.root, x, y, z, u, tcap, t);
-    t = fmaxf(t, 0.0f) * 0.99999f;
-    return rho;
-}
-
-// ---------------------------------------------------------------------------
-// Curved-ray certificates (smooth non-affine chains: gaussian, sigmoid).
-// The deformed sample point q(s) of a ray then follows a curve, whose speed
-// |q'| is at most `vmax` (the chain's Lipschitz bound) and whose
-// acceleration |q''| is at most `acc` (host: chain rule over the steps).
-// A ball of radius m around q(s0) holds the curve for s - s0 <= m / vmax;
-// a gyroid leaf does better with a second-order bound on g(q(s)):
-//   |g(s0 + tau) - g0 - g1 tau| <= M tau^2 / 2,  g1 = grad g . q'(s0),
-//   M = |q'|^2 max|H g| + |grad g| |q''| <= 4 is^2 vmax^2 + sqrt(6) is acc,
-// (is = 1/scale; every entry of the Hessian is a sum of at most two
-// products of sines and cosines), so the band |g| < t is entered or left
-// no earlier than the first root of that quadratic.  Near the band edge the
-// bound grows like sqrt(gap / M) where the ball's grows like the gap.
-// Selected by the CURVE flag of the tracing loops (CPU build; the device
-// kernels use ball certificates for these chains).
-// ---------------------------------------------------------------------------
-struct CurveDir {
-    float vx, vy, vz;  // q'(s) at the sample (object units per unit ray parameter)
-    float vmax, acc;   // chain bounds on |q'| and |q''|
-    float eps;         // absolute error allowance (m_slack)
-};
-
-// deform32 with the velocity: (x, y, z) <- def(p), (vx, vy, vz) <- J(p) v.
-XRP_HD void deform_jvp32(const SceneDev& S, float& x, float& y, float& z, float& vx, float& vy, float& vz) {
-    for (int i = 0; i < S.ndefs; i++) {
-        const DefStep& d = S.defs[i];
-        const float* a = d.f;
-        switch (d.type) {
-        case D_GAUSSIAN: {
-            float x0 = x - a[6], y0 = y - a[7], z0 = z - a[8];
-            float r2 = fmaf(z0, z0, fmaf(y0, y0, x0 * x0));
-            float rv = fmaf(z0, vz, fmaf(y0, vy, x0 * vx));
-            float ex = a[0] * f_exp(-r2 * a[3]);
-            float ey = a[1] * f_exp(-r2 * a[4]);
-            float ez = a[2] * f_exp(-r2 * a[5]);
-            vx = fmaf(-2.0f * a[3] * ex, rv, vx);
-            vy = fmaf(-2.0f * a[4] * ey, rv, vy);
-            vz = fmaf(-2.0f * a[5] * ez, rv, vz);
-            x += ex; y += ey; z += ez;
-            break;
-        }
-        case D_LINEAR: {
-            float nx = fmaf(a[4], z, fmaf(a[5], y, fmaf(a[0], x, x)));
-            float ny = fmaf(a[3], z, fmaf(a[1], y, fmaf(a[5], x, y)));
-            float nz = fmaf(a[2], z, fmaf(a[3], y, fmaf(a[4], x, z)));
-            float mx = fmaf(a[4], vz, fmaf(a[5], vy, fmaf(a[0], vx, vx)));
-            float my = fmaf(a[3], vz, fmaf(a[1], vy, fmaf(a[5], vx, vy)));
-            float mz = fmaf(a[2], vz, fmaf(a[3], vy, fmaf(a[4], vx, vz)));
-            x = nx; y = ny; z = nz;
-            vx = mx; vy = my; vz = mz;
-            break;
-        }
-        case D_RIGID: x += a[0]; y += a[1]; z += a[2]; break;
-        case D_SIGMOID: {
-            float* p = d.axis == 0 ? &x : (d.axis == 1 ? &y : &z);
-            float* v = d.axis == 0 ? &vx : (d.axis == 1 ? &vy : &vz);
-            float e = f_exp(-(*p - a[1]) * a[2]);
-            float sg = f_rcp(1.0f + e);
-            *v *= fmaf(a[0] * a[2], sg * (1.0f - sg), 1.0f);  // 1 + A sigma' / L
-            *p += a[0] * sg;
-            break;
-        }
-        case D_AFFINE: {
-            float nx = fmaf(a[2], z, fmaf(a[1], y, a[0] * x));
-            float ny = fmaf(a[5], z, fmaf(a[4], y, a[3] * x));
-            float nz = fmaf(a[8], z, fmaf(a[7], y, a[6] * x));
-            float mx = fmaf(a[2], vz, fmaf(a[1], vy, a[0] * vx));
-            float my = fmaf(a[5], vz, fmaf(a[4], vy, a[3] * vx));
-            float mz = fmaf(a[8], vz, fmaf(a[7], vy, a[6] * vx));
-            x = nx; y = ny; z = nz;
-            vx = mx; vy = my; vz = mz;
-            break;
-        }
-        default: break;
-        }
-    }
-}
-
-// First tau > 0 at which D - w tau - M tau^2 / 2 can reach 0 (gap D > 0
-// closing at speed w, curvature M > 0): the positive root, in the form
-// without cancellation for each sign of w (moving away, the rationalised
-// form would divide by a difference that FP32 can round to 0).
-XRP_HD float gap_time(float D, float w, float M) {
-    const float s = sqrtf(fmaf(w, w, 2.0f * M * D));
-    return w >= 0.0f ? 2.0f * D / (w + s) : (s - w) / M;
-}
-
-// A ball margin m (object units) as a ray-parameter bound along the curve.
-XRP_HD float curve_time(float m, const CurveDir& c) { return fmaxf(m - c.eps, 0.0f) / c.vmax; }
-
-// Box b = (lo0, hi0, lo1, hi1, lo2, hi2) and a point inside it at least
-// eps from every face: the first parameter at which the curve can reach a
-// face, face by face (gap to the face, speed toward it, acceleration bound),
-// at least the ball bound.
-// Box b and a point outside it: entering needs every coordinate inside its
-// slab (grown by eps), so the latest per-axis arrival bounds the entry.
-XRP_HD float box_curve_entry(const float* b, float x, float y, float z, const CurveDir& c) {
-    const float M = c.acc + 1e-20f;
-    const float p[3] = {x, y, z}, v[3] = {c.vx, c.vy, c.vz};
-    float t = 0.0f;
-    for (int a = 0; a < 3; a++) {
-        const float below = b[2 * a] - c.eps - p[a], above = p[a] - b[2 * a + 1] - c.eps;
-        if (below > 0.0f) t = fmaxf(t, gap_time(below, v[a] + 1e-6f * c.vmax, M));
-        if (above > 0.0f) t = fmaxf(t, gap_time(above, -v[a] + 1e-6f * c.vmax, M));
-    }
-    return t;
-}
-
-XRP_HD float box_curve_time(const float* b, float x, float y, float z, const CurveDir& c) {
-    const float M = c.acc + 1e-20f;
-    const float gaps[6] = {x - b[0] - c.eps, b[1] - x - c.eps, y - b[2] - c.eps,
-                           b[3] - y - c.eps, z - b[4] - c.eps, b[5] - z - c.eps};
-    const float w[6] = {-c.vx, c.vx, -c.vy, c.vy, -c.vz, c.vz};
-    float t = kFar;
-    for (int k = 0; k < 6; k++) {
-        if (!(gaps[k] > 0.0f)) return 0.0f;
-        t = fminf(t, gap_time(gaps[k], w[k] + 1e-6f * c.vmax, M));
-    }
-    return t;
-}
-
-// Slab lo < a < hi of a coordinate a(s) with a' = w at the sample and
-// |a''| <= M: inside (at least e from both faces) the first exit, outside
-// the first arrival at the slab (grown by e); 0 within e of a face.
-XRP_HD float slab_curve(float a, float w, float lo, float hi, float e, float M, bool inside) {
-    if (inside) {
-        const float g0 = a - lo - e, g1 = hi - a - e;
-        if (!(g0 > 0.0f && g1 > 0.0f)) return 0.0f;
-        return fminf(gap_time(g0, -w, M), gap_time(g1, w, M));
-    }
-    if (a < lo - e) return gap_time(lo - e - a, w, M);
-    if (a > hi + e) return gap_time(a - hi - e, -w, M);
-    return 0.0f;
-}
-
-// Squared radius f = |w|^2 (3-D, or across a cylinder's axis) against r^2:
-// f' = 2 w.v, |f''| <= 2 vmax^2 + 2 |w| acc with |w| <= r inside.  Inside
-// (|w| < r - e): the first time f can reach (r - e)^2.  Outside the radius
-// d = |w| has |d''| <= vmax^2 / r + acc while d >= r: the first time d can
-// come down to r + e.
-XRP_HD float radius_curve(float w2, float wv, float r, float e, float vmax, float acc, bool inside) {
-    if (inside) {
-        const float ri = r - e;
-        const float gap = ri * ri - w2;
-        if (!(ri > 0.0f && gap > 0.0f)) return 0.0f;
-        return gap_time(gap, 2.0f * wv + 1e-6f * vmax * ri, fmaf(2.0f * r, acc, 2.0f * vmax * vmax) * 1.01f);
-    }
-    const float d = sqrtf(w2);
-    const float gap = d - r - e;
-    if (!(gap > 0.0f && r > 0.0f)) return 0.0f;
-    return gap_time(gap, -wv / d + 1e-6f * vmax, fmaf(vmax, vmax / r, acc) * 1.01f + 1e-20f);
-}
-
-// Leaf density (leaf_dm's decisions) and its curve bound t: the ball bound,
-// or better the second-order bound of the leaf's defining conditions
-// (entry: the latest arrival over the violated conditions; exit: the
-// earliest over all).
-XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t) {
-    float m;
-    const float rho = leaf_dm(n, x, y, z, m);
-    t = curve_time(m, c);
-    if (isunc(rho)) return rho;
-    const float* f = n.f;
-    const float e = c.eps;
-    const float M = c.acc * 1.01f + 1e-20f;
-    switch (n.type) {
-    case N_SPHERE: {
-        const float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-        const float w2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
-        const float wv = fmaf(wz, c.vz, fmaf(wy, c.vy, wx * c.vx));
-        const float r = f[4], b = sqrtf(f[F_BAND]);  // band of d^2 - r^2 as a distance (upper bound)
-        t = fmaxf(t, radius_curve(w2, wv, r, e + b, c.vmax, c.acc, w2 < r * r));
-        return rho;
-    }
-    case N_BOX: {
-        const float bb[6] = {f[0] - f[3], f[0] + f[3], f[1] - f[4], f[1] + f[4], f[2] - f[5], f[2] + f[5]};
-        const float mn = fminf(f[3] - fabsf(x - f[0]), fminf(f[4] - fabsf(y - f[1]), f[5] - fabsf(z - f[2])));
-        const float eb = e + f[F_BAND];
-        float tt;
-        if (mn > eb) {
-            tt = kFar;
-            const float p[3] = {x, y, z}, v[3] = {c.vx, c.vy, c.vz};
-            for (int a = 0; a < 3; a++) tt = fminf(tt, slab_curve(p[a], v[a], bb[2 * a], bb[2 * a + 1], eb, M, true));
-        } else if (mn < -eb) {
-            tt = 0.0f;
-            const float p[3] = {x, y, z}, v[3] = {c.vx, c.vy, c.vz};
-            for (int a = 0; a < 3; a++) tt = fmaxf(tt, slab_curve(p[a], v[a], bb[2 * a], bb[2 * a + 1], eb, M, false));
-        } else {
-            tt = 0.0f;
-        }
-        t = fmaxf(t, tt);
-        return rho;
-    }
-    case N_CYL: {
-        // axis v (f[3..5]), 1/|v|^2 f[6], r f[8], |v| f[9]: axial coordinate
-        // a = (q - p0).v/|v| in [0, |v|], radial part across the axis
-        const float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-        const float il = f[9] * f[6];  // 1/|v|
-        const float a = fmaf(wz, f[5], fmaf(wy, f[4], wx * f[3])) * il;
-        const float va = fmaf(c.vz, f[5], fmaf(c.vy, f[4], c.vx * f[3])) * il;
-        const float cc = a * il;
-        const float px = fmaf(-cc, f[3], wx), py = fmaf(-cc, f[4], wy), pz = fmaf(-cc, f[5], wz);
-        const float ca = va * il;
-        const float qx = fmaf(-ca, f[3], c.vx), qy = fmaf(-ca, f[4], c.vy), qz = fmaf(-ca, f[5], c.vz);
-        const float p2 = fmaf(pz, pz, fmaf(py, py, px * px));
-        const float pv = fmaf(pz, qz, fmaf(py, qy, px * qx));
-        const float r = f[8], br = sqrtf(f[F_BAND]);
-        const float ea = e + f[F_BAND2] * f[9];  // band of c as an axial distance
-        const bool in_r = p2 < r * r, in_a = a > 0.0f && a < f[9];
-        float tt;
-        if (rho != 0.0f || (in_r && in_a)) {  // inside both: the earlier exit
-            tt = fminf(radius_curve(p2, pv, r, e + br, c.vmax, c.acc, true),
-                       slab_curve(a, va, 0.0f, f[9], ea, M, true));
-        } else {  // entering needs both: the later arrival of the violated ones
-            tt = 0.0f;
-            if (!in_r) tt = fmaxf(tt, radius_curve(p2, pv, r, e + br, c.vmax, c.acc, false));
-            if (!in_a) tt = fmaxf(tt, slab_curve(a, va, 0.0f, f[9], ea, M, false));
-        }
-        t = fmaxf(t, tt);
-        return rho;
-    }
-    case N_PPD: {
-        const float wx = x - f[0], wy = y - f[1], wz = z - f[2];
-        const float b = f[F_BAND];
-        float q[3], qv[3], ea[3], Ma[3];
-        float mrel = 3.0e38f;
-        bool out = false;
-        for (int k = 0; k < 3; k++) {
-            const float* rr = f + 3 + 3 * k;
-            q[k] = fmaf(rr[2], wz, fmaf(rr[1], wy, rr[0] * wx));
-            qv[k] = fmaf(rr[2], c.vz, fmaf(rr[1], c.vy, rr[0] * c.vx));
-            ea[k] = fmaf(e, f[12 + k], b);
-            Ma[k] = M * f[12 + k];
-            const float in = fminf(q[k], 1.0f - q[k]);
-            mrel = fminf(mrel, in - ea[k]);
-            out = out || in < -ea[k];
-        }
-        float tt = 0.0f;
-        if (out) {
-            for (int k = 0; k < 3; k++) tt = fmaxf(tt, slab_curve(q[k], qv[k], 0.0f, 1.0f, ea[k], Ma[k], false));
-        } else if (mrel > 0.0f) {
-            tt = kFar;
-            for (int k = 0; k < 3; k++) tt = fminf(tt, slab_curve(q[k], qv[k], 0.0f, 1.0f, ea[k], Ma[k], true));
-        }
-        t = fmaxf(t, tt);
-        return rho;
-    }
-    default: break;
-    }
-    if (n.type != N_GYROID) return rho;
-    const float is = f[3], ais = fabsf(is);
-    float X = (x - f[0]) * is, Y = (y - f[1]) * is, Z = (z - f[2]) * is;
-    float sx, cx, sy, cy, sz, cz;
-    f_sincos(X, &sx, &cx);
-    f_sincos(Y, &sy, &cy);
-    f_sincos(Z, &sz, &cz);
-    const float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
-    const float gX = fmaf(cx, cy, -sz * sx), gY = fmaf(cy, cz, -sx * sy), gZ = fmaf(cz, cx, -sy * sz);
-    const float g1 = is * fmaf(gZ, c.vz, fmaf(gY, c.vy, gX * c.vx));
-    // error of g1 (trigonometry, velocity, position) and of g (position slack)
-    const float dg1 = fmaf(1e-5f, fabsf(g1), ais * c.vmax * fmaf(16.0f * ais, c.eps, 1e-5f));
-    const float eg = 2.4494898f * ais * c.eps;
-    const float Mg = fmaf(4.0f * is * is, c.vmax * c.vmax, 2.4494898f * ais * c.acc) * 1.01f + 1e-20f;
-    const float th = f[4], band = f[F_BAND];
-    float t2 = 0.0f;
-    if (th - fabsf(g) > band) {  // inside |g| < th: both edges of the band
-        const float T = th - band - eg;
-        if (T - fabsf(g) > 0.0f)
-            t2 = fminf(gap_time(T - g, g1 + dg1, Mg), gap_time(T + g, -g1 + dg1, Mg));
-    } else {  // outside: the nearer edge
-        const float T = th + band + eg;
-        if (g > T) t2 = gap_time(g - T, -g1 + dg1, Mg);
-        else if (g < -T) t2 = gap_time(-T - g, g1 + dg1, Mg);
-    }
-    t = fmaxf(t, t2);
-    return rho;
-}
-
-template <int D>
-XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z, const CurveDir& u, float& t);
-
-// item_dm's decisions; the container distances become curve bounds.
-template <int D>
-XRP_HD float item_dc(const SceneDev& S, int id, float x, float y, float z, const CurveDir& u, float& t) {
-    const Node& n = S.nodes[id];
-    if (n.type <= N_GYROID) return leaf_dc(n, x, y, z, u, t);
-    if (n.type == N_TESS) {
-        if constexpr (D > 0) {
-            const float* f = n.f;
-            float mo = fminf(fminf(fminf(x - f[0], f[1] - x), fminf(y - f[2], f[3] - y)),
-                             fminf(z - f[4], f[5] - z));
-            const float ob[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
-            if (mo < -f[6]) {  // outside: zero until the curve can enter the bounds
-                t = fmaxf(curve_time(-mo, u), box_curve_entry(ob, x, y, z, u));
-                return 0.0f;
-            }
-            if (!(mo > f[6])) { t = 0.0f; return xnan(); }
-            float qx = (x - f[20]) * f[17], qy = (y - f[21]) * f[18], qz = (z - f[22]) * f[19];
-            float nx = floorf(qx), ny = floorf(qy), nz = floorf(qz);
-            float bq = f[23];
-            float fr = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)), fminf(qy - ny, 1.0f - (qy - ny))),
-                             fminf(qz - nz, 1.0f - (qz - nz)));
-            if (!(fr > bq)) { t = 0.0f; return xnan(); }
-            float fc = fminf(fminf(fminf(qx - nx, 1.0f - (qx - nx)) * fabsf(f[14]),
-                                   fminf(qy - ny, 1.0f - (qy - ny)) * fabsf(f[15])),
-                             fminf(qz - nz, 1.0f - (qz - nz)) * fabsf(f[16]));
-            float fx = fmaf(-f[14], nx, x), fy = fmaf(-f[15], ny, y), fz = fmaf(-f[16], nz, z);
-            float mu = fminf(fminf(fminf(fx - f[7], f[8] - fx), fminf(fy - f[9], f[10] - fy)),
-                             fminf(fz - f[11], f[12] - fz));
-            if (mu < -f[13]) { t = curve_time(fminf(fminf(mo, fc), -mu), u); return 0.0f; }
-            if (!(mu > f[13])) { t = 0.0f; return xnan(); }
-            float tk;
-            float r = coll_dc<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tk);
-            // the outer bounds, the fold's cell and the unit-cell bounds, face
-            // by face along the curve (their distances alone bound it too)
-            const float ub[6] = {f[7], f[8], f[9], f[10], f[11], f[12]};
-            float cb[6];
-            for (int a = 0; a < 3; a++) {
-                const float q0 = fmaf(a == 0 ? nx : (a == 1 ? ny : nz), f[14 + a], f[20 + a]);
-                const float q1 = q0 + f[14 + a];
-                cb[2 * a] = fminf(q0, q1);
-                cb[2 * a + 1] = fmaxf(q0, q1);
-            }
-            // band of the fold (q units) as a world distance, per axis at most
-            const float bw = bq * fmaxf(fabsf(f[14]), fmaxf(fabsf(f[15]), fabsf(f[16])));
-            for (int a = 0; a < 6; a++) cb[a] += (a & 1) ? -bw : bw;
-            const float tcon = fminf(fminf(box_curve_time(ob, x, y, z, u), box_curve_time(cb, x, y, z, u)),
-                                     box_curve_time(ub, fx, fy, fz, u));
-            t = fminf(fmaxf(tcon, curve_time(fminf(fminf(mo, fc), mu), u)), tk);
-            return r;
-        }
-    }
-    t = 0.0f;
-    if (n.type == N_VOXEL) return voxel32(S.vols[n.a], n.f[0], x, y, z, S.hier_zero_guard);
-    return xnan();
-}
-
-// coll_dm's decisions; the candidates' bounds, capped by the list cell's
-// faces or clearance as curve bounds.
-template <int D>
-XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z, const CurveDir& u, float& t) {
-    const int32_t* kids = S.child + c.a;
-    int cnt = c.b;
-    const int32_t* list = nullptr;
-    t = kFar;
-    if (c.flags & C_ACCEL) {
-        int G = (c.flags >> 16) & 0xff;
-        float ux = (x - c.f[0]) * c.f[3], uy = (y - c.f[1]) * c.f[4], uz = (z - c.f[2]) * c.f[5];
-        int ix = (int)floorf(ux), iy = (int)floorf(uy), iz = (int)floorf(uz);
-        ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
-        iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
-        iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
-        float m = 3.0e38f;
-        if (ix > 0) m = fminf(m, (ux - (float)ix) / c.f[3]);
-        if (ix < G - 1) m = fminf(m, ((float)(ix + 1) - ux) / c.f[3]);
-        if (iy > 0) m = fminf(m, (uy - (float)iy) / c.f[4]);
-        if (iy < G - 1) m = fminf(m, ((float)(iy + 1) - uy) / c.f[4]);
-        if (iz > 0) m = fminf(m, (uz - (float)iz) / c.f[5]);
-        if (iz < G - 1) m = fminf(m, ((float)(iz + 1) - uz) / c.f[5]);
-        // the cell's inner faces along the curve (world distance = grid distance * cell size)
-        float tf = kFar;
-        {
-            const float M = u.acc * 1.01f + 1e-20f;
-            const float gu[3] = {ux, uy, uz}, vv[3] = {u.vx, u.vy, u.vz};
-            const int ii[3] = {ix, iy, iz};
-            for (int a = 0; a < 3; a++) {
-                const float h = c.f[8 + a];
-                if (ii[a] > 0) {
-                    const float gap = (gu[a] - (float)ii[a]) * h - u.eps;
-                    tf = gap > 0.0f ? fminf(tf, gap_time(gap, -vv[a] + 1e-6f * u.vmax, M)) : 0.0f;
-                }
-                if (ii[a] < G - 1) {
-                    const float gap = ((float)(ii[a] + 1) - gu[a]) * h - u.eps;
-                    tf = gap > 0.0f ? fminf(tf, gap_time(gap, vv[a] + 1e-6f * u.vmax, M)) : 0.0f;
-                }
-            }
-        }
-        const int cell = f2i(c.f[6]) + (iz * G + iy) * G + ix;
-        t = fmaxf(fmaxf(curve_time(fmaxf(fmaxf(m, 0.0f), S.clear[cell]), u), fminf(tf, kFar)), 0.0f);
-        const int32_t* off = S.cells + cell;
-        list = S.items + off[0];
-        cnt = off[1] - off[0];
-    }
-    const bool greedy = (c.flags & C_GREEDY) != 0;
-    float sum = 0.0f, sabs = 0.0f;
-    bool unc = false, done = false;
-    // uniform greedy collections: inside a child (for certain) its exit alone
-    // bounds the curve (see coll_dr_uniform)
-    const bool uniform = (c.flags & C_UNIFORM) != 0;
-    for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
-        float tk;
-        float r = item_dc<D>(S, kids[slot], x, y, z, u, tk);
-        if (uniform && !unc && r > 0.0f) {
-            t = tk;
-            return r;
-        }
-        t = fminf(t, tk);
-        if (done) continue;
-        if (isunc(r)) {
-            unc = true;
-            done = true;
-            continue;
-        }
-        if (greedy && r > 0.0f) {
-            sum = r;
-            sabs = fabsf(r);
-            done = true;
-            continue;
-        }
-        sum += r;
-        sabs += fabsf(r);
-    }
-    if (unc) return xnan();
-    if (greedy && done) return sum;
-    if (!(c.flags & C_EXACT_SUM) && sabs > 0.0f && fabsf(sum) <= c.f[7] * sabs) return xnan();
-    if (c.flags & C_CLIP) sum = fminf(fmaxf(sum, 0.0f), 1.0f);
-    return sum;
-}
-
-// density32 at one point and the curve bound t (ray parameter units) of the
-// samples ahead that share its density; d: the world ray direction.
-template <int DEPTH, bool DEFS>
-XRP_HD float dens_curve32(const SceneDev& S, float x, float y, float z, const float* d, float& t) {
-    CurveDir u;
-    u.vx = d[0]; u.vy = d[1]; u.vz = d[2];
-    if constexpr (DEFS) deform_jvp32(S, x, y, z, u.vx, u.vy, u.vz);
-    u.vmax = S.curve_vmax;
-    u.acc = S.curve_acc;
-    u.eps = S.m_slack;
-    const Node& r = S.nodes[S.root];
-    float rho;
-    if (r.type <= N_GYROID) rho = leaf_dc(r, x, y, z, u, t);
-    else if (r.type == N_COLL) rho = coll_dc<DEPTH>(S, r, x, y, z, u, t);
-    else rho = item_dc<DEPTH>(S, S.root, x, y, z, u, t);
-    t = fmaxf(t, 0.0f) * 0.99999f;
-    return rho;
-}
+namespace xrp {
 
 // ---------------------------------------------------------------------------
 // FP64 exact evaluation (reference arithmetic, operation by operation)
