@@ -84,3 +84,13 @@ def test_cameras_bitwise_equal_to_oracle(lib):
 
 def test_version(lib):
     assert lib.xrp_version() >= 100
+
+
+def test_python_flag_constants_match_header():
+    """The bindings' XRP_FLAG_* / XRP_INTEGRATE_* values are the header's."""
+    from xray_projection_render_gb300 import _lib
+    hdr = open(os.path.join(ROOT, "include", "xrp.h")).read()
+    found = dict(re.findall(r"\b(XRP_(?:FLAG|INTEGRATE)_[A-Z_]+)\s*=\s*(\d+)", hdr))
+    assert "XRP_FLAG_BALL" in found and "XRP_FLAG_TRACE" in found
+    for name, value in found.items():
+        assert getattr(_lib, name) == int(value), name
