@@ -1,23 +1,38 @@
-"""Benchmark: Mrays/s of the GB300 projection engine on the voxel-grid workload.
+"""Benchmark: Mrays/s of the GB300 projection engine.
 
-Workload (one step = one pass of the hot path over one batch): the 256^3 FP32
-grid of 64 seeded Gaussians rendered from 180 views (azimuth 0, 2, ..., 358
-degrees, polar 90) at 1024x1024 with the uniform-step integrator, ds = half a
-voxel (2/256/2), R = 4, fov = 40 -- 188.7 M rays per step.
+Default workload (the headline): the deformed lattice -- a unit cell of 12
+edge and 4 body-diagonal cylinders (radius 0.03, rho 1) tessellated
+10 x 10 x 10 over [-1,1]^3 under 5 % axial (zz) strain -- from 360 seeded
+views (azimuth U[0,360), polar U[30,150], seed 3) at 1024 x 1024, ds 0.002,
+R 4, fov 40: 377.5 M rays per step.
 
-value     : device throughput, volume resident in HBM, output to a device
+One step = one pass of the fastest exact path over every view: certificate
+tracing with ray certificates (each evaluated sample certifies how many of
+the following samples share its density; results equal the plain
+integrator's).  The same record carries
+  plain          : the uniform-step integrator (main.go:144-154), same views;
+  speedup_vs_plain
+  proposal       : the segment march routed by the trained 3 x 64 network, on
+                   a view subset (its rate per ray does not depend on which
+                   other views share a call);
+  error_vs_fp64  : for every path, the max relative and absolute
+                   transmittance error against the FP64 oracle on the CPU
+                   baseline leg's seeded rays;
+  gyroid         : the gyroid (scale 8, thickness 0.1) under the sigmoid
+                   deformation (A 0.1, L 0.2, along z), 720 views x 2048^2,
+                   ds 0.001, with the same fields.
+
+value     : device throughput, scene resident in HBM, output to a device
             buffer, L2 flushed (256 MiB write) before every timed step, each
             step timed with CUDA events on the launching stream.
-e2e       : the same metric through the reference ABI call
-            RenderVolumeProjectionsCUDA with pinned host buffers (volume
-            upload and image download inside the timed region).
-roofline  : the voxel kernel is bound by its texture gathers (two tld4 of
-            16 B per sample, the exact sample count from a counter pass):
-            achieved gathered bytes/s against the gather throughput measured
-            in this run (xrp_probe_gather_rate, L1-resident texture).  The
-            FP32 view (58 FLOPs per sample against a CUDA-core SGEMM with
-            TF32 off, measured in this run) is kept under "fp32"; the
-            analytic workloads report the FP32 view.
+e2e       : the same metric through the C ABI with the scene created from
+            its JSON map and the images copied into pinned host memory
+            inside the timed region (RenderVolumeProjectionsCUDA for the
+            voxel grid).
+roofline  : FP32 issue for the analytic scenes (evaluations x FLOPs per
+            evaluation against a CUDA-core SGEMM measured in this run); the
+            voxel grid reports its texture gathers against the gather rate
+            measured in this run.
 cpu_baseline / --impl reference: the FP64 CPU restatement of the reference
             path (oracle/), on all host cores, on a seeded ray subset.
 
@@ -27,6 +42,7 @@ subsets (view k on rank k mod N) with no collective ("scaling": "weak").
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -39,8 +55,23 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FLOPS_PER_SAMPLE = 58  # 8 common (position + accumulate) + 50 trilinear
-METRIC = "Mrays/s on 1 GB300 (uniform-step integrator, voxel grid 256^3, 180 views x 1024^2)"
+HEADLINE_METRIC = ("Mrays/s on 1 GB300 at <=1e-4 error vs FP64: fastest exact path on the deformed "
+                   "lattice, with the plain GPU integrator and the learned proposal in the same record")
+VOXEL_METRIC = "Mrays/s on 1 GB300 (uniform-step integrator, voxel grid 256^3, 180 views x 1024^2)"
+
+# the definitions of the workloads, printed in `config` by both arms
+DEFINITIONS = {
+    "lattice": {"cells": "10x10x10 over [-1,1]^3", "unit_cell": "12 edge + 4 body-diagonal cylinders",
+                "strut_radius": 0.03, "deformation": "linear, strain zz 0.05",
+                "cameras": "azimuth U[0,360), polar U[30,150], seed 3"},
+    "gyroid": {"gyroid": "scale 8, thickness 0.1, rho 1, tessellated over [-1,1]^3",
+               "deformation": "sigmoid A 0.1, center 0, lengthscale 0.2, along z",
+               "cameras": "azimuth 0, 0.5, ..., 359.5, polar 90"},
+    "voxel": {"grid": "256^3 FP32, 64 seeded Gaussians (seed 2)",
+              "cameras": "azimuth 0, 2, ..., 358, polar 90"},
+    "cube": {"scene": "cube side 1 minus sphere r 0.3 and cylinder r 0.2",
+             "cameras": "azimuth 0, polar 90"},
+}
 
 
 def parse():
@@ -49,16 +80,17 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--workload", default="voxel",
-                   choices=["voxel", "cube", "lattice", "gyroid", "batched", "finish", "voxelize"],
-                   help="voxel (default, the headline), one of the analytic scenes, the batch "
-                        "of 64 uneven scenes (one persistent launch replayed from a CUDA graph), "
-                        "device-side image finishing of 64 images of 1024^2, or the volume "
-                        "export of the deformed lattice at 256^3")
+    p.add_argument("--workload", default="lattice",
+                   choices=["lattice", "gyroid", "voxel", "cube", "batched", "finish", "voxelize"],
+                   help="lattice (default, the headline), the gyroid, the voxel grid, the cube minus "
+                        "sphere and cylinder, the batch of 64 uneven scenes (one persistent launch "
+                        "replayed from a CUDA graph), device-side image finishing of 64 images of "
+                        "1024^2, or the volume export of the deformed lattice at 256^3")
     p.add_argument("--scenes", type=int, default=64, help="batched: number of scenes")
-    p.add_argument("--march", default="plain",
-                   choices=["plain", "trace", "ball", "certificate", "proposal"],
-                   help="analytic scenes: plain integrator, per-ray certificate tracing (ray bounds "
+    p.add_argument("--march", default="auto",
+                   choices=["auto", "plain", "trace", "ball", "certificate", "proposal"],
+                   help="auto: certificate tracing for analytic scenes, the plain integrator for "
+                        "the voxel grid; plain integrator, per-ray certificate tracing (ray bounds "
                         "for affine deformation chains), tracing with ball certificates only, "
                         "segment march with certificates and no network, or the trained proposal")
     p.add_argument("--views", type=int, default=0, help="view count (0: the workload's)")
@@ -66,6 +98,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer ABI timing")
+    p.add_argument("--no-compare", action="store_true",
+                   help="skip the plain / proposal comparisons and the gyroid record")
     p.add_argument("--volume-path", default="gather", choices=["gather", "loads"],
                    help="voxel reads: texture gathers (default) or per-tap loads")
     return p.parse_args()
@@ -157,72 +191,128 @@ def fp32_peak_tflops(torch):
     return best
 
 
-def cpu_baseline(workload, seconds, threads=None):
-    """FP64 oracle on a seeded subset of the workload's rays, all host cores."""
+# ---------------------------------------------------------------------------
+# the FP64 oracle: CPU baseline and error against FP64 (test infrastructure:
+# it checks and times the reference algorithm, it never renders a result)
+# ---------------------------------------------------------------------------
+
+def draw_rays(rng, nviews, res, n):
+    return np.stack([rng.integers(0, nviews, n), rng.integers(0, res, n),
+                     rng.integers(0, res, n)], 1).astype(np.int32)
+
+
+def oracle_rays(w, angles, rays, threads=None, integration="simple"):
+    """FP64 transmittance of the (view, i, j) rays of `angles` (the oracle
+    builds its own cameras; nothing here touches the engine library)."""
     from oracle import oracle as O
+    obj = {"type": "voxel_grid", "_voxels": w.volume} if w.volume is not None else w.obj
+    return O.render(O.Scene(obj, w.deformation), angles, w.res, w.ds, R=w.R, fov=w.fov,
+                    integration=integration, rays=rays, nthreads=threads or os.cpu_count() or 1)
+
+
+def cpu_baseline(w, seconds, threads=None, seed=1234):
+    """The oracle on all host cores on seeded random rays of `w` for about
+    `seconds`: (cpu_baseline record, rays, FP64 transmittances)."""
     threads = threads or os.cpu_count() or 1
-    rng = np.random.default_rng(1234)
-    if workload.volume is not None:
-        from xray_projection_render_gb300 import engine  # camera rows only (host code)
-        cams21 = engine.xray_camera_params(workload.angles, workload.R, workload.fov)
-        scene = O.VolumeABIScene(workload.volume)
-
-        def render(rays):
-            scene.render_rays(cams21, workload.res, np.float32(workload.ds), rays, nthreads=threads)
-    else:
-        scene = O.Scene(workload.obj, workload.deformation)
-
-        def render(rays):
-            O.render(scene, workload.angles, workload.res, workload.ds, R=workload.R,
-                     fov=workload.fov, rays=rays, nthreads=threads)
-
-    def run(n):
-        rays = np.stack([rng.integers(0, len(workload.angles), n), rng.integers(0, workload.res, n),
-                         rng.integers(0, workload.res, n)], 1).astype(np.int32)
-        t = time.perf_counter()
-        render(rays)
-        return time.perf_counter() - t
-
+    rng = np.random.default_rng(seed)
     n = 2000
-    dt = run(n)
-    n2 = int(max(2000, min(40_000_000, n * seconds / max(dt, 1e-3))))
-    dt2 = run(n2)
-    return {"value": n2 / dt2 / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{n2} seeded random rays of {workload.name} ({dt2:.1f} s)"}
+    t = time.perf_counter()
+    oracle_rays(w, w.angles, draw_rays(rng, len(w.angles), w.res, n), threads)
+    dt = time.perf_counter() - t
+    n2 = int(max(2000, min(60_000_000, 1.3 * n * seconds / max(dt, 1e-3))))
+    rays = draw_rays(rng, len(w.angles), w.res, n2)
+    t = time.perf_counter()
+    ref = oracle_rays(w, w.angles, rays, threads)
+    dt2 = time.perf_counter() - t
+    return ({"value": n2 / dt2 / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+             "sample": f"{n2} seeded random rays of {w.name} ({dt2:.1f} s)"}, rays, ref)
+
+
+def error_vs_fp64(out, rays, ref, res):
+    """Max relative / absolute error of a device image stack [view][i][j]
+    at the given rays against their FP64 values."""
+    import torch
+    idx = (torch.from_numpy(rays[:, 0].astype(np.int64)) * res * res
+           + torch.from_numpy(rays[:, 1].astype(np.int64)) * res
+           + torch.from_numpy(rays[:, 2].astype(np.int64))).to(out.device)
+    got = out.reshape(-1)[idx].cpu().numpy().astype(np.float64)
+    if not np.all(np.isfinite(got)):
+        return {"max_rel": None, "max_abs": None, "rays": int(len(rays)), "non_finite": True}
+    d = np.abs(got - ref)
+    return {"max_rel": float(np.max(d / ref)), "max_abs": float(np.max(d)), "rays": int(len(rays))}
+
+
+def subset_views(angles, views):
+    return list(angles[:: max(1, len(angles) // views)][:views])
+
+
+def workload_config(w, march, world, name):
+    """`config` of a scene workload: the same dict in both arms."""
+    cfg = {"workload": w.name, "views": len(w.angles), "res": w.res, "ds": w.ds,
+           "integrator": "simple", "R": w.R, "fov": w.fov, "march": march,
+           "l2": "flushed before every timed step (256 MiB write)",
+           "parallelism": f"views k mod {world}"}
+    cfg.update(DEFINITIONS.get(name, {}))
+    return cfg
+
+
+def resolve_march(args, w):
+    if args.march != "auto":
+        return args.march
+    return "plain" if w.volume is not None else "trace"
+
+
+MARCH_PATHS = {
+    "plain": "uniform-step integrator (main.go:144-154)",
+    "trace": "certificate tracing (ray certificates for affine deformation chains, ball "
+             "certificates otherwise)",
+    "ball": "certificate tracing with ball certificates",
+    "certificate": "segment march with certificates, no network",
+    "proposal": "segment march routed by the trained 3 x 64 network (BF16, FP32 accumulate)",
+}
 
 
 def run_reference(args):
+    """The reference's CPU algorithm (the FP64 oracle port) on the host
+    cores, on the engine arm's workload, metric and config; every timed step
+    renders a seeded ray sample of at least 10 s."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from xray_projection_render_gb300 import workloads as W
+    from xray_projection_render_gb300 import workloads as W  # numpy only: no engine library
     if args.workload in ("finish", "voxelize"):
         print(json.dumps({"impl": "reference", "unavailable":
                           "the reference runs this step in Go on the host (PNG / raw writing); "
                           "no CPU arm is timed for it here"}), flush=True)
         return
     if args.workload == "batched":
-        ws = W.batched_scenes(64)[:8]
-        w = W.Workload("batched_scenes_64", None, None, [], 0, 0.005)
-        measure = lambda sec: cpu_baseline_multi(ws, sec)  # noqa: E731
+        ws = W.batched_scenes(args.scenes)[:8]
+        name = f"batched_scenes_{args.scenes}"
+        cfg = batched_config(args.scenes, world)
+
+        def measure(sec):
+            return cpu_baseline_multi(ws, sec)
+        metric = BATCH_METRIC
     else:
         w = make_workload(args.workload, W, args.views, args.res)
-        measure = lambda sec: cpu_baseline(w, sec)  # noqa: E731
+        name = w.name
+        cfg = workload_config(w, resolve_march(args, w), world, args.workload)
+
+        def measure(sec):
+            return cpu_baseline(w, sec)[0]
+        metric = VOXEL_METRIC if args.workload == "voxel" else (
+            HEADLINE_METRIC if args.workload == "lattice" else f"Mrays/s on 1 GB300 ({name})")
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = measure(max(2.0, args.cpu_seconds / max(1, args.steps)))
+        cb = measure(2.0 if i < args.warmup else max(10.0, args.cpu_seconds))
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.median(vals))
     cb["value"] = v
-    line = {"impl": "reference",
-            "metric": METRIC if args.workload == "voxel" else f"Mrays/s on 1 GB300 ({w.name})",
-            "value": v, "unit": "Mrays/s",
+    line = {"impl": "reference", "metric": metric, "value": v, "unit": "Mrays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)",
-            "config": {"workload": w.name, "views": len(w.angles), "res": w.res, "ds": w.ds},
-            "cpu_baseline": cb,
+            "data": "synthetic (seeded)", "config": cfg, "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -236,32 +326,302 @@ FLOPS = {
     "gyroid": 53,    # gyroid 13 (+6 SFU) + sigmoid 5 (+2 SFU) + fold/bounds 27
 }
 
-
-# DRAM bytes (read + write) of the render kernel per view, from the ncu
-# captures summarised in profiles/ (small cases scaled by view count: the
-# grid streams through L2 once per view, so traffic grows with the views).
-TRAFFIC = {
-    "voxel": {"bytes_per_view": (404.93e6 + 47.01e6) / 8,
-              "source": "profiles/k_voxel_gather_voxel256_8x1024.md (8-view capture, x views)"},
-    "lattice": {"bytes_per_view": (0.611e6 + 0.472e6) / 2 * 4,
-                "source": "profiles/k_render_lattice_2x512.md (2 views at 512^2, x views x 4)"},
-}
+# DRAM bytes (read + write) per view of the voxel render kernel: a constant
+# from an ncu capture of 8 views (the grid streams through L2 once per view,
+# so the traffic grows with the views).
+TRAFFIC_PER_VIEW = {"voxel": (404.93e6 + 47.01e6) / 8}
 
 
 def make_workload(name, W, views, res):
     if name == "voxel":
-        return W.voxel_blobs(res or 1024, views or 180)
-    if name == "cube":
-        w = W.cube_minus_sphere_cylinder(res or 512)
+        w = W.voxel_blobs(1024, 180)
+    elif name == "cube":
+        w = W.cube_minus_sphere_cylinder(512)
     elif name == "lattice":
-        w = W.deformed_lattice(res or 1024, 360)
+        w = W.deformed_lattice(1024, 360)
     elif name == "gyroid":
-        w = W.gyroid_sigmoid(res or 2048, 720)
+        w = W.gyroid_sigmoid(2048, 720)
     else:
         raise ValueError(name)
-    if views:
-        w = W.reduced(w, w.res, views)
+    if views or res:
+        w = W.reduced(w, res or w.res, views or None)
     return w
+
+
+def _event_time(torch, step, steps, stream, flush):
+    """Mean seconds of `steps` calls of step(), each bracketed by CUDA events
+    on `stream` after an L2 flush."""
+    times = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    return float(np.mean(times))
+
+
+def scene_step(X, scene, w, angles, march, out, stream, prop=None, volume_path="gather"):
+    """One render of `angles` by `march` into the device buffer `out`."""
+    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov)
+    if march == "plain":
+        return lambda: X.render(scene, angles, out=out, stream=stream, volume_path=volume_path, **kw)
+    trace = {"trace": True, "ball": "ball"}.get(march, False)
+    return lambda: X.render_proposal(scene, prop, angles, segment=64, refine=march == "proposal",
+                                     trace=trace, out=out, stream=stream, **kw)
+
+
+def launches_per_step(march, rays, voxel):
+    """Kernels one step launches: one render launch for the plain
+    integrator; per launch group of at most 8 M rays the march, its FP64
+    pass and the exp pass for the other marches."""
+    if march == "plain" or voxel:
+        return 1
+    return 3 * -(-rays // (1 << 23))
+
+
+def time_path(X, torch, scene, w, angles, march, stream, flush, steps, prop=None, err_rays=4000):
+    """Rate and error vs FP64 of one march on `angles` (at the workload's
+    resolution and step): one warm-up call, then `steps` timed calls."""
+    out = torch.empty((len(angles), w.res, w.res), device="cuda", dtype=torch.float32)
+    step = scene_step(X, scene, w, angles, march, out, stream, prop)
+    step()
+    torch.cuda.synchronize()
+    t = _event_time(torch, step, steps, stream, flush)
+    rec = {"value": len(angles) * w.res * w.res / t / 1e6, "unit": "Mrays/s", "views": len(angles),
+           "res": w.res, "steps": steps, "ms_per_step": t * 1e3, "path": MARCH_PATHS[march],
+           "gpu_launches_per_step": launches_per_step(march, len(angles) * w.res * w.res, False)}
+    rng = np.random.default_rng(4321)
+    rays = draw_rays(rng, len(angles), w.res, err_rays)
+    wa = dataclasses.replace(w, angles=angles)
+    rec["error_vs_fp64"] = error_vs_fp64(out, rays, oracle_rays(wa, angles, rays), w.res)
+    del out
+    return rec
+
+
+def compare_paths(X, torch, scene, w, value, stream, flush, args, full_plain=True):
+    """The plain integrator and the learned proposal on the same scene, with
+    their errors against FP64, and the speed-up of `value` over plain."""
+    steps = max(1, min(args.steps, 2))
+    rec = {}
+    plain_angles = w.angles if full_plain else subset_views(w.angles, 24)
+    rec["plain"] = time_path(X, torch, scene, w, plain_angles, "plain", stream, flush, steps)
+    if not full_plain:
+        rec["plain"]["note"] = "view subset (the per-ray cost does not depend on the other views)"
+    rec["speedup_vs_plain"] = value / rec["plain"]["value"]
+    pv = subset_views(w.angles, 16 if w.res <= 1024 else 8)
+    t0 = time.perf_counter()
+    with X.Proposal(scene, pv, resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, segment=64) as P:
+        train_s = time.perf_counter() - t0
+        pr = time_path(X, torch, scene, w, pv, "proposal", stream, flush, steps, prop=P)
+        _, st = X.render_proposal(scene, P, pv[:1], resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                                  stats=True)
+    pr["train_s"] = train_s
+    pr["speedup_vs_plain"] = pr["value"] / rec["plain"]["value"]
+    pr["counters_one_view"] = st
+    pr["note"] = "view subset; the network routes segments between refinement and dense sampling"
+    rec["proposal"] = pr
+    return rec
+
+
+def secondary_gyroid(X, torch, W, stream, flush, args):
+    """The gyroid under the sigmoid deformation at full size (720 x 2048^2,
+    ds 0.001): certificate tracing over every view, plain and proposal on
+    view subsets, errors against FP64."""
+    w = W.gyroid_sigmoid(2048, 720)
+    steps = max(1, min(args.steps, 3))
+    with X.Scene(w.obj, w.deformation) as s:
+        rec = time_path(X, torch, s, w, w.angles, "trace", stream, flush, steps, err_rays=6000)
+        rec.update({"workload": w.name, "ds": w.ds, "march": "trace"})
+        _, st = X.render_proposal(s, None, w.angles[:1], resolution=w.res, ds=w.ds, R=w.R, fov=w.fov,
+                                  trace=True, stats=True)
+        rec["evaluations_per_ray"] = st["evaluations"] / (w.res * w.res)
+        torch.cuda.empty_cache()
+        rec.update(compare_paths(X, torch, s, w, rec["value"], stream, flush, args, full_plain=False))
+    torch.cuda.empty_cache()
+    return rec
+
+
+def bench_scene(args):
+    import torch
+    import __graft_entry__ as G
+    import xray_projection_render_gb300 as X
+    from xray_projection_render_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    G.build()
+    from xray_projection_render_gb300.sharding import job_time, shard
+    w = make_workload(args.workload, W, args.views, args.res)
+    march = resolve_march(args, w)
+    is_voxel = w.volume is not None
+    my_angles = shard(w.angles, rank, world)  # view k on rank k mod N, no exchange
+    wm = dataclasses.replace(w, angles=my_angles)
+    n_my = len(my_angles)
+    res = w.res
+    img = res * res
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    vols = [torch.from_numpy(w.volume).to(dev)] if is_voxel else []
+    scene = X.Scene(w.obj, w.deformation, vols)
+    out = torch.empty((n_my, res, res), device=dev, dtype=torch.float32)
+    flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)  # 256 MiB > L2
+    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov, volume_path=args.volume_path)
+
+    prop = None
+    if march == "proposal":
+        prop = X.Proposal(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, segment=64)
+    step = scene_step(X, scene, w, my_angles, march, out, stream, prop, args.volume_path)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # exact sample count of one step (counter pass, untimed, on a view subset)
+    nstat = max(1, min(8, n_my))
+    _, samples, fp64 = X.render(scene, my_angles[:nstat], stats=True, **kw)
+    samples_step = samples * n_my / nstat
+    evals_step = None
+    if march != "plain" and not is_voxel:
+        # evaluations the march actually makes (density + certificate per
+        # evaluation, or one density per dense sample)
+        _, pst = X.render_proposal(scene, prop, my_angles[:nstat], resolution=res, ds=w.ds, R=w.R,
+                                   fov=w.fov, segment=64, refine=march == "proposal",
+                                   trace=_trace_mode(march), stats=True)
+        evals_step = (pst["evaluations"] + pst["dense_samples"]) * n_my / nstat
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_local = _event_time(torch, step, args.steps, stream, flush)
+    t_step, rays_total = job_time(t_local, n_my * img, dev)
+    value = rays_total / t_step / 1e6
+
+    # error of the timed step's images against FP64, on the CPU baseline
+    # leg's rays (the oracle renders them once; rank 0's views)
+    cb = None
+    if rank == 0:
+        if args.no_cpu_baseline:
+            rng = np.random.default_rng(1234)
+            rays = draw_rays(rng, n_my, res, 20000)
+            ref = oracle_rays(wm, my_angles, rays)
+        else:
+            cb, rays, ref = cpu_baseline(wm, args.cpu_seconds)
+        err = error_vs_fp64(out, rays, ref, res)
+
+    # end to end through the host-facing C ABI, pinned host buffers, inputs
+    # uploaded and images read back inside the timed region
+    e2e_times = []
+    out_host = None if args.no_e2e else torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
+    if is_voxel:
+        cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
+        h2d = int(w.volume.nbytes + cams21.nbytes)
+        path = "RenderVolumeProjectionsCUDA, pinned host buffers"
+        if not args.no_e2e:
+            vol_host = torch.from_numpy(w.volume).pin_memory()
+
+        def e2e_call():
+            X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
+    else:
+        obj_json = json.dumps(w.obj)
+        def_json = json.dumps(w.deformation) if w.deformation else None
+        h2d = len(obj_json) + (len(def_json) if def_json else 0) + n_my * 192
+        path = ("xrp_scene_create + " + ("xrp_render" if march == "plain" else "xrp_render_proposal")
+                + ", pinned host output")
+
+        def e2e_call():
+            with X.Scene(obj_json, def_json) as s2:
+                if march == "plain":
+                    X.render(s2, my_angles, out=out_host, **kw)
+                else:  # the network trained on the resident scene applies to this copy
+                    X.render_proposal(s2, prop, my_angles, resolution=res, ds=w.ds, R=w.R,
+                                      fov=w.fov, segment=64, refine=march == "proposal",
+                                      trace=_trace_mode(march), out=out_host)
+    if not args.no_e2e:
+        e2e_call()  # warm
+        for _ in range(max(1, min(args.steps, 3))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_call()
+            e2e_times.append(time.perf_counter() - t0)
+    t_e2e, _ = job_time(float(np.mean(e2e_times)) if e2e_times else float("nan"), 0, dev)
+    e2e_value = rays_total / t_e2e / 1e6
+
+    peaks = measured_peaks()
+    fp32_peak = fp32_peak_tflops(torch)
+    fps = FLOPS[args.workload]
+    if evals_step is None:
+        achieved = samples_step * fps / t_step / 1e12
+        work = "lattice samples evaluated x FLOPs per sample"
+    else:
+        # a certificate evaluation adds the bound (about 12 FLOPs beyond the
+        # density, sharing its deformation and geometry)
+        achieved = evals_step * (fps + 12) / t_step / 1e12
+        work = ("evaluations the march makes (counter pass) x (FLOPs per sample + 12 for the "
+                "certificate); the plain integrator would evaluate samples_per_step")
+    fp32_roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                 "frac": achieved / fp32_peak if fp32_peak else None,
+                 "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
+                 "flops_per_sample": fps, "work": work, "evaluations_per_step": evals_step}
+    roof = dict(fp32_roof)
+    if is_voxel and args.volume_path == "gather":
+        # the voxel kernel's binding unit is the texture path: two tld4
+        # gathers (16 B each) per evaluated sample, against the gather rate
+        # measured in this run by xrp_probe_gather_rate
+        import ctypes
+        from xray_projection_render_gb300 import _lib as XL
+        gr = ctypes.c_double(0.0)
+        XL.check(XL.load().xrp_probe_gather_rate(ctypes.byref(gr)), "xrp_probe_gather_rate")
+        g_ach = 2.0 * samples_step / t_step
+        roof = {"bound": "tex", "achieved": g_ach * 16 / 1e9, "peak": gr.value * 16 / 1e9, "unit": "GB/s",
+                "frac": g_ach / gr.value if gr.value else None,
+                "peak_source": "measured in this run: tld4 gathers on an L1-resident layered texture",
+                "note": "gathered bytes (2 x 16 B per sample) vs the measured gather throughput",
+                "fp32": fp32_roof}
+    traffic = TRAFFIC_PER_VIEW.get(args.workload) if march == "plain" else None
+    cfg = workload_config(w, march, world, args.workload)
+    if is_voxel:
+        cfg["volume_path"] = args.volume_path
+    line = {
+        "metric": (VOXEL_METRIC if args.workload == "voxel" else
+                   HEADLINE_METRIC if args.workload == "lattice" else f"Mrays/s on 1 GB300 ({w.name})"),
+        "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": cfg, "path": MARCH_PATHS[march],
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
+        "gpu_launches": args.steps * launches_per_step(march, n_my * img, is_voxel),
+        "roofline": dict(roof, **{
+            "traffic": traffic * n_my if traffic else None,
+            "traffic_note": ("constant: DRAM bytes per view from an ncu capture of the same kernel "
+                             "on 8 views, times the views") if traffic else "not captured for this path",
+            "samples_per_step": samples_step,
+            "fp64_fallback_fraction": fp64 / max(samples, 1),
+            "hbm_peak_gbs_measured": peaks.get("hbm_gbs")}),
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        line["error_vs_fp64"] = err
+        if cb is not None:
+            line["cpu_baseline"] = cb
+    if rank == 0 and world == 1 and not args.no_compare and not is_voxel and march != "plain":
+        del out
+        torch.cuda.empty_cache()
+        line.update(compare_paths(X, torch, scene, w, value, stream, flush, args))
+        if args.workload == "lattice" and not (args.views or args.res):
+            scene.close()
+            line["gyroid"] = secondary_gyroid(X, torch, W, stream, flush, args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if prop is not None:
+        prop.close()
+    scene.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def bench_batched(args):
@@ -288,7 +648,8 @@ def bench_batched(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)
-    trace = _trace_mode(args)
+    march = args.march if args.march != "auto" else "trace"
+    trace = _trace_mode(march)
     b = X.Batch(items, ds=ds, autotune=True, trace=trace)
     info = b.info()
     for _ in range(args.warmup):
@@ -352,19 +713,17 @@ def bench_batched(args):
     t_e2e = float(np.mean(e2e_times)) if e2e_times else float("nan")
     fp32_peak = fp32_peak_tflops(torch)
     line = {
-        "metric": "Mrays/s on 1 GB300 (64 uneven scenes, one persistent launch per step)",
+        "metric": BATCH_METRIC,
         "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 4)",
-        "config": {"workload": "batched_scenes_64", "scenes": len(ws), "rays": rays, "ds": ds,
-                   "integrator": "simple", "R": 4.0, "fov": 40.0,
-                   "l2": "flushed before every timed step (256 MiB write); output > L2",
-                   "tile": f'{info["tile_w"]}x{info["tile_h"]}', "blocks_per_sm": info["blocks_per_sm"],
-                   "autotune_ms": info["tune_ms"], "graph": "one CUDA graph replay per step",
-                   "march": {"trace": "certificate tracing (ray bounds: every scene is affine)",
-                             "ball": "certificate tracing (ball certificates)"}.get(args.march, "plain"),
-                   "per_scene_calls_mrays": info["rays"] / t_seq / 1e6,
-                   "parallelism": f"scenes k mod {world}"},
+        "config": batched_config(args.scenes, world),
+        "batch": {"scenes": len(ws), "rays": rays, "tile": f'{info["tile_w"]}x{info["tile_h"]}',
+                  "blocks_per_sm": info["blocks_per_sm"], "autotune_ms": info["tune_ms"],
+                  "graph": "one CUDA graph replay per step",
+                  "march": {"trace": "certificate tracing (ray bounds: every scene is affine)",
+                            "ball": "certificate tracing (ball certificates)"}.get(march, "plain"),
+                  "per_scene_calls_mrays": info["rays"] / t_seq / 1e6},
         "e2e": {"value": rays / t_e2e / 1e6 if e2e_times else None, "unit": "Mrays/s",
                 "h2d_bytes_per_step": h2d if e2e_times else 0, "d2h_bytes_per_step": d2h,
                 "path": "xrp_scene_create x64 + xrp_batch_create (no tuning) + xrp_batch_render + "
@@ -452,9 +811,21 @@ def ctypes_ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+BATCH_METRIC = "Mrays/s on 1 GB300 (64 uneven scenes, one persistent launch per step)"
+
+
+def batched_config(scenes, world):
+    return {"workload": f"batched_scenes_{scenes}", "scenes": scenes, "ds": 0.005,
+            "integrator": "simple", "R": 4.0, "fov": 40.0,
+            "scene_definition": "collections of 1-200 seeded primitives, resolution 256/512/1024, "
+                                "8-128 views (seed 4)",
+            "l2": "flushed before every timed step (256 MiB write); output > L2",
+            "parallelism": f"scenes k mod {world}"}
+
+
 def cpu_baseline_multi(ws, seconds):
     """The oracle on seeded random rays spread over several scenes."""
-    parts = [cpu_baseline(w, seconds / len(ws)) for w in ws]
+    parts = [cpu_baseline(w, seconds / len(ws))[0] for w in ws]
     rays_s = len(ws) / sum(1.0 / p["value"] for p in parts)  # equal rays per scene
     out = dict(parts[0])
     out["value"] = rays_s
@@ -462,9 +833,9 @@ def cpu_baseline_multi(ws, seconds):
     return out
 
 
-def _trace_mode(args):
+def _trace_mode(march):
     """render_proposal / Batch `trace` argument of a --march choice."""
-    return {"trace": True, "ball": "ball"}.get(args.march, False)
+    return {"trace": True, "ball": "ball"}.get(march, False)
 
 
 def main():
@@ -475,179 +846,7 @@ def main():
         return bench_batched(args)
     if args.workload in ("finish", "voxelize"):
         return bench_small_kernel(args)
-    import torch
-    import __graft_entry__ as G
-    import xray_projection_render_gb300 as X
-    from xray_projection_render_gb300 import workloads as W
-
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    G.build()
-    from xray_projection_render_gb300.sharding import job_time, shard
-    w = make_workload(args.workload, W, args.views, args.res)
-    is_voxel = w.volume is not None
-    my_angles = shard(w.angles, rank, world)  # view k on rank k mod N, no exchange
-    n_my = len(my_angles)
-    res = w.res
-    img = res * res
-    dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
-    vols = [torch.from_numpy(w.volume).to(dev)] if is_voxel else []
-    scene = X.Scene(w.obj, w.deformation, vols)
-    out = torch.empty((n_my, res, res), device=dev, dtype=torch.float32)
-    flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)  # 256 MiB > L2
-    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov, volume_path=args.volume_path)
-
-    prop = None
-    if args.march == "proposal":
-        prop = X.Proposal(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, segment=64)
-
-    def step():
-        if args.march == "plain":
-            X.render(scene, my_angles, out=out, stream=stream, **kw)
-        else:
-            X.render_proposal(scene, prop, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov,
-                              segment=64, refine=args.march == "proposal",
-                              trace=_trace_mode(args), out=out, stream=stream)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    # exact sample count of one step (counter pass, untimed, on a view subset)
-    nstat = max(1, min(8, n_my))
-    _, samples, fp64 = X.render(scene, my_angles[:nstat], stats=True, **kw)
-    samples_step = samples * n_my / nstat
-    evals_step = None
-    if args.march != "plain" and not is_voxel:
-        # evaluations the march actually makes (density + certificate radius
-        # per evaluation, or one density per dense sample)
-        _, pst = X.render_proposal(scene, prop, my_angles[:nstat], resolution=res, ds=w.ds, R=w.R,
-                                   fov=w.fov, segment=64, refine=args.march == "proposal",
-                                   trace=_trace_mode(args), stats=True)
-        evals_step = (pst["evaluations"] + pst["dense_samples"]) * n_my / nstat
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    times = []
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) * 1e-3)
-    t_step, rays_total = job_time(float(np.mean(times)), n_my * img, dev)
-    value = rays_total / t_step / 1e6
-
-    # end to end through the host-facing C ABI, pinned host buffers, inputs
-    # uploaded and images read back inside the timed region
-    e2e_times = []
-    out_host = None if args.no_e2e else torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
-    if is_voxel:
-        cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
-        h2d = int(w.volume.nbytes + cams21.nbytes)
-        path = "RenderVolumeProjectionsCUDA, pinned host buffers"
-        if not args.no_e2e:
-            vol_host = torch.from_numpy(w.volume).pin_memory()
-
-        def e2e_call():
-            X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
-    else:
-        obj_json = json.dumps(w.obj)
-        def_json = json.dumps(w.deformation) if w.deformation else None
-        h2d = len(obj_json) + (len(def_json) if def_json else 0) + n_my * 192
-        path = "xrp_scene_create + xrp_render, pinned host output"
-
-        def e2e_call():
-            with X.Scene(obj_json, def_json) as s2:
-                if args.march == "plain":
-                    X.render(s2, my_angles, out=out_host, **kw)
-                else:  # the network trained on the resident scene applies to this copy
-                    X.render_proposal(s2, prop, my_angles, resolution=res, ds=w.ds, R=w.R,
-                                      fov=w.fov, segment=64, refine=args.march == "proposal",
-                                      trace=_trace_mode(args), out=out_host)
-    if not args.no_e2e:
-        e2e_call()  # warm
-        for _ in range(max(1, min(args.steps, 3))):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            e2e_call()
-            e2e_times.append(time.perf_counter() - t0)
-    t_e2e, _ = job_time(float(np.mean(e2e_times)) if e2e_times else float("nan"), 0, dev)
-    e2e_value = rays_total / t_e2e / 1e6
-
-    peaks = measured_peaks()
-    fp32_peak = fp32_peak_tflops(torch)
-    fps = FLOPS[args.workload]
-    if evals_step is None:
-        achieved = samples_step * fps / t_step / 1e12
-        work = "lattice samples evaluated x FLOPs per sample"
-    else:
-        # a certificate evaluation adds the radius (about 12 FLOPs beyond
-        # the density, sharing its deformation and geometry)
-        achieved = evals_step * (fps + 12) / t_step / 1e12
-        work = ("evaluations the march makes (counter pass) x (FLOPs per sample + 12 for the "
-                "certificate radius); the plain integrator would evaluate samples_per_step")
-    fp32_roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                 "frac": achieved / fp32_peak if fp32_peak else None,
-                 "peak_source": "measured in this run: CUDA-core SGEMM, TF32 off",
-                 "flops_per_sample": fps, "work": work, "evaluations_per_step": evals_step}
-    roof = dict(fp32_roof)
-    if is_voxel and args.volume_path == "gather":
-        # the voxel kernel's binding unit is the texture path: two tld4
-        # gathers (16 B each) per evaluated sample, against the gather rate
-        # measured in this run by xrp_probe_gather_rate
-        import ctypes
-        from xray_projection_render_gb300 import _lib as XL
-        gr = ctypes.c_double(0.0)
-        XL.check(XL.load().xrp_probe_gather_rate(ctypes.byref(gr)), "xrp_probe_gather_rate")
-        g_ach = 2.0 * samples_step / t_step
-        roof = {"bound": "tex", "achieved": g_ach * 16 / 1e9, "peak": gr.value * 16 / 1e9, "unit": "GB/s",
-                "frac": g_ach / gr.value if gr.value else None,
-                "peak_source": "measured in this run: tld4 gathers on an L1-resident layered texture",
-                "note": "gathered bytes (2 x 16 B per sample) vs the measured gather throughput",
-                "fp32": fp32_roof}
-    line = {
-        "metric": METRIC if args.workload == "voxel" else f"Mrays/s on 1 GB300 ({w.name})",
-        "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)",
-        "config": {"workload": w.name, "views": len(w.angles), "res": res, "ds": w.ds,
-                   "integrator": "simple", "R": w.R, "fov": w.fov,
-                   "march": None if is_voxel else args.march,
-                   "l2": "flushed before every timed step (256 MiB write)",
-                   "volume_path": args.volume_path if is_voxel else None,
-                   "parallelism": f"views k mod {world}"},
-        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
-        # plain: one render launch per step (all views); march modes: per
-        # launch group of at most 8 M rays, the march, its FP64 pass and
-        # the exp pass
-        "gpu_launches": args.steps * (1 if (args.march == "plain" or is_voxel)
-                                      else 3 * -(-n_my * img // (1 << 23))),
-        "roofline": dict(roof, **{
-                     "traffic": TRAFFIC.get(args.workload, {}).get("bytes_per_view", 0) * n_my or None,
-                     "traffic_source": TRAFFIC.get(args.workload, {}).get("source"),
-                     "samples_per_step": samples_step,
-                     "fp64_fallback_fraction": fp64 / max(samples, 1),
-                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")}),
-        "clocks": clk.summary(),
-    }
-    if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if prop is not None:
-        prop.close()
-    scene.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    return bench_scene(args)
 
 
 if __name__ == "__main__":

@@ -331,8 +331,8 @@ XRP_API int xrp_render_proposal(xrp_scene* scene, const xrp_proposal* proposal, 
 XRP_API int xrp_render_proposal_device(xrp_scene* scene, const xrp_proposal* proposal, int segment,
                                        const xrp_camera* views, int num_views,
                                        const xrp_render_opts* opts, float* out_device, void* stream);
-/* Counters of the last xrp_render_proposal on this thread with
- * XRP_FLAG_STATS: segments, segments certified, pieces certified in
+/* Counters of the last xrp_render_proposal or xrp_render_proposal_device
+ * call on this thread with XRP_FLAG_STATS: segments, segments certified, pieces certified in
  * refinement, pieces integrated densely, dense samples, certificate
  * evaluations, FP64 re-evaluations, network rounds, candidates routed to
  * dense integration, candidates refined, and 1 when the list of samples left

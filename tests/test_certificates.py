@@ -278,7 +278,9 @@ def test_curve_every_primitive_and_collection():
     ]
     chain = {"type": "composed", "deformations": [
         GAUSS, {"type": "linear", "strains": [0.02, -0.01, 0.05, 0.01, 0.0, 0.03]}, SIGMOID]}
-    for d in (GAUSS, SIGMOID, chain):
+    # None: a scene without deformation traced with curve bounds, as in a
+    # batch whose other scenes have non-affine chains
+    for d in (GAUSS, SIGMOID, chain, None):
         for p in prims:
             check_curve(p, d, n=250, per=6)
         check_curve({"type": "object_collection", "objects": prims}, d, n=300, per=6)

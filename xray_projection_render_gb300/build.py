@@ -25,6 +25,10 @@ LIB = os.path.join(PKG, "libcuda_render.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra nvcc options, e.g. the occupancy knobs of xrp_launch.h
+# (XRP_NVCC_FLAGS="-DXRP_CURVE_MIN_BLOCKS=3"); they take part in the
+# staleness check through the flags file below
+EXTRA = os.environ.get("XRP_NVCC_FLAGS", "").split()
 
 
 def _nvcc():
@@ -39,8 +43,17 @@ def _sources():
             if f.endswith((".cu", ".cuh", ".cpp", ".h"))] + [os.path.join(INCLUDE, "xrp.h")]
 
 
+FLAGS_FILE = os.path.join(BUILD, "nvcc_flags.txt")
+
+
 def _stale(target):
     if not os.path.exists(target):
+        return True
+    try:
+        with open(FLAGS_FILE) as f:
+            if f.read() != " ".join(EXTRA):
+                return True
+    except OSError:
         return True
     t = os.path.getmtime(target)
     return any(os.path.getmtime(s) > t for s in _sources() + [__file__])
@@ -58,7 +71,8 @@ def _run(cmd, verbose):
 
 
 CUDA_UNITS = ["xrp_engine.cu", "xrp_kern_scene.cu", "xrp_kern_batch.cu", "xrp_kern_batch_ball.cu",
-              "xrp_kern_batch_ray.cu", "xrp_kern_export.cu", "xrp_kern_trace.cu", "xrp_kern_trace_ray.cu",
+              "xrp_kern_batch_ray.cu", "xrp_kern_batch_curve.cu", "xrp_kern_export.cu",
+              "xrp_kern_trace.cu", "xrp_kern_trace_ray.cu", "xrp_kern_trace_curve.cu",
               "xrp_kern_prop.cu", "xrp_kern_prop_net.cu", "xrp_kern_train.cu"]
 
 
@@ -76,7 +90,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     for unit in CUDA_UNITS:
         o = os.path.join(BUILD, unit.replace(".cu", ".o"))
         cmd = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", ",".join(common_host),
-               "-I", INCLUDE, "-c", os.path.join(CSRC, unit), "-o", o]
+               "-I", INCLUDE, *EXTRA, "-c", os.path.join(CSRC, unit), "-o", o]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         cmds.append(cmd)
@@ -86,6 +100,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     tmp = LIB + f".tmp{os.getpid()}"
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lpthread"], verbose)
     os.replace(tmp, LIB)
+    with open(FLAGS_FILE, "w") as f:
+        f.write(" ".join(EXTRA))
     if ptxas_info:
         return "".join(r.stderr for r in results[1:])
     return LIB

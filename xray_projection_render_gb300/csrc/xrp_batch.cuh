@@ -25,7 +25,8 @@ struct BatchStage {
 };
 
 // TRACE: 0 plain integrator, 1 certificate tracing with ball certificates,
-// 2 with ray certificates (every scene of the batch has an affine chain).
+// 2 with ray certificates (every scene of the batch has an affine chain),
+// 3 with curve certificates (some scene has a non-affine chain).
 // Resident blocks per SM (register budget) measured on GB300 for tracing:
 // 4 (64 registers). Ray bounds on the 64-scene batch: 4116 Mrays/s with 2
 // blocks, 4591 with 3, 4809 with 4, 4841 with 5; ball certificates: 1678
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 4 : XRP_SCENE_MIN_
             float val;
             if constexpr (TRACE != 0) {
                 unsigned ev = 0;
-                val = trace_pixel<HIER, DEPTH, DEFS, TRACE == 2>(sg.S, L, sg.P, sg.V, i, j, ev);
+                val = trace_pixel<HIER, DEPTH, DEFS, TRACE == 2, TRACE == 3>(sg.S, L, sg.P, sg.V, i, j, ev);
             } else {
                 RayStats st{0, 0};
                 val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);
@@ -106,33 +107,42 @@ cudaError_t launch_batch_t(const BatchLaunch& b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Curve certificates (TRACE 3) serve deformed scenes only: DEFS is always on.
 template <int TRACE>
 cudaError_t launch_batch_mode(const BatchLaunch& b, cudaStream_t st) {
     if (b.depth == 0) {
-        if (b.defs) return b.hier ? launch_batch_t<true, 0, true, TRACE>(b, st) : launch_batch_t<false, 0, true, TRACE>(b, st);
-        return b.hier ? launch_batch_t<true, 0, false, TRACE>(b, st) : launch_batch_t<false, 0, false, TRACE>(b, st);
+        if (TRACE == 3 || b.defs) return b.hier ? launch_batch_t<true, 0, true, TRACE>(b, st) : launch_batch_t<false, 0, true, TRACE>(b, st);
+        if constexpr (TRACE != 3)
+            return b.hier ? launch_batch_t<true, 0, false, TRACE>(b, st) : launch_batch_t<false, 0, false, TRACE>(b, st);
     }
-    if (b.defs) return b.hier ? launch_batch_t<true, 3, true, TRACE>(b, st) : launch_batch_t<false, 3, true, TRACE>(b, st);
-    return b.hier ? launch_batch_t<true, 3, false, TRACE>(b, st) : launch_batch_t<false, 3, false, TRACE>(b, st);
+    if (TRACE == 3 || b.defs) return b.hier ? launch_batch_t<true, 3, true, TRACE>(b, st) : launch_batch_t<false, 3, true, TRACE>(b, st);
+    if constexpr (TRACE != 3)
+        return b.hier ? launch_batch_t<true, 3, false, TRACE>(b, st) : launch_batch_t<false, 3, false, TRACE>(b, st);
+    return cudaErrorInvalidValue;
 }
 
 template <int TRACE>
 const void* batch_fn_mode(int depth, bool defs, bool hier) {
     if (depth == 0) {
-        if (defs) return hier ? (const void*)k_batch<true, 0, true, TRACE> : (const void*)k_batch<false, 0, true, TRACE>;
-        return hier ? (const void*)k_batch<true, 0, false, TRACE> : (const void*)k_batch<false, 0, false, TRACE>;
+        if (TRACE == 3 || defs) return hier ? (const void*)k_batch<true, 0, true, TRACE> : (const void*)k_batch<false, 0, true, TRACE>;
+        if constexpr (TRACE != 3)
+            return hier ? (const void*)k_batch<true, 0, false, TRACE> : (const void*)k_batch<false, 0, false, TRACE>;
     }
-    if (defs) return hier ? (const void*)k_batch<true, 3, true, TRACE> : (const void*)k_batch<false, 3, true, TRACE>;
-    return hier ? (const void*)k_batch<true, 3, false, TRACE> : (const void*)k_batch<false, 3, false, TRACE>;
+    if (TRACE == 3 || defs) return hier ? (const void*)k_batch<true, 3, true, TRACE> : (const void*)k_batch<false, 3, true, TRACE>;
+    if constexpr (TRACE != 3)
+        return hier ? (const void*)k_batch<true, 3, false, TRACE> : (const void*)k_batch<false, 3, false, TRACE>;
+    return nullptr;
 }
 
-// The three instantiations (xrp_kern_batch.cu, xrp_kern_batch_ball.cu,
-// xrp_kern_batch_ray.cu).
+// The four instantiations (xrp_kern_batch.cu, xrp_kern_batch_ball.cu,
+// xrp_kern_batch_ray.cu, xrp_kern_batch_curve.cu).
 cudaError_t launch_batch_plain(const BatchLaunch& b, cudaStream_t st);
 cudaError_t launch_batch_ball(const BatchLaunch& b, cudaStream_t st);
 cudaError_t launch_batch_ray(const BatchLaunch& b, cudaStream_t st);
+cudaError_t launch_batch_curve(const BatchLaunch& b, cudaStream_t st);
 const void* batch_fn_plain(int depth, bool defs, bool hier);
 const void* batch_fn_ball(int depth, bool defs, bool hier);
 const void* batch_fn_ray(int depth, bool defs, bool hier);
+const void* batch_fn_curve(int depth, bool defs, bool hier);
 
 }  // namespace xrp

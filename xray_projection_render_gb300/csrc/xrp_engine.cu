@@ -1110,8 +1110,9 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, E->device);
     const bool hier = oo.integration == XRP_INTEGRATE_HIERARCHICAL;
-    // ray certificates when every scene's chain is affine (and not refused)
-    const int trace = !(oo.flags & XRP_FLAG_TRACE) ? 0 : (affine && !(oo.flags & XRP_FLAG_BALL)) ? 2 : 1;
+    // ray certificates when every scene's chain is affine, curve
+    // certificates otherwise, ball certificates on request
+    const int trace = !(oo.flags & XRP_FLAG_TRACE) ? 0 : (oo.flags & XRP_FLAG_BALL) ? 1 : affine ? 2 : 3;
     const int kdepth = depth == 0 ? 0 : kMaxDepth;
     if ((e = batch_blocks_per_sm(kdepth, defs, hier, trace, &occ)) != cudaSuccess)
         return cuda_fail(7, "batch occupancy", e);
@@ -1582,7 +1583,7 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     std::unique_lock<std::mutex> g(E->mtx, std::defer_lock);
     if (out_host) g.lock();
     cudaStream_t st = out_host ? E->compute : (cudaStream_t)stream;
-    const bool want_stats = out_host && (o->flags & XRP_FLAG_STATS);
+    const bool want_stats = (o->flags & XRP_FLAG_STATS) != 0;
     PoolBuf sb;
     PropLaunch pl;
     memset(&pl.Q, 0, sizeof(pl.Q));

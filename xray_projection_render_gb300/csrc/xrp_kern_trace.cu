@@ -1,20 +1,24 @@
 // xrp_kern_trace.cu -- certificate tracing (k_trace in xrp_proposal.cuh),
 // one thread per ray, specialised on tessellation depth, deformation,
-// integrator and certificate kind (ray bounds for affine chains, balls
-// otherwise).  Its own translation unit so it compiles in parallel with the
+// integrator and certificate kind (ray bounds for affine chains, curve
+// bounds for other deformation chains, balls on request).  Its own translation unit so it compiles in parallel with the
 // segment march.
 #include "xrp_trace.cuh"
 
 namespace xrp {
 
-// Ray-certificate kernels live in xrp_kern_trace_ray.cu.
+// Ray- and curve-certificate kernels live in xrp_kern_trace_ray.cu and
+// xrp_kern_trace_curve.cu.
 cudaError_t launch_trace_ray(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                              cudaStream_t st);
+cudaError_t launch_trace_curve(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                               cudaStream_t st);
 
 cudaError_t launch_trace(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                          cudaStream_t st) {
     if (Q.trace == 1 && pr.S.affine) return launch_trace_ray(pr, view0, nviews, Q, dout, st);
-    return launch_trace_mode<false>(pr, view0, nviews, Q, dout, st);
+    if (Q.trace == 1 && pr.defs) return launch_trace_curve(pr, view0, nviews, Q, dout, st);
+    return launch_trace_mode<0>(pr, view0, nviews, Q, dout, st);
 }
 
 }  // namespace xrp

@@ -1,0 +1,12 @@
+// xrp_kern_trace_curve.cu -- certificate tracing with curve bounds (smooth
+// non-affine deformation chains: gaussian, sigmoid), one thread per ray.
+#include "xrp_trace.cuh"
+
+namespace xrp {
+
+cudaError_t launch_trace_curve(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                               cudaStream_t st) {
+    return launch_trace_mode<2>(pr, view0, nviews, Q, dout, st);
+}
+
+}  // namespace xrp

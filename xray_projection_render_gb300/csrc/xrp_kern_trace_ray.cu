@@ -6,7 +6,7 @@ namespace xrp {
 
 cudaError_t launch_trace_ray(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                              cudaStream_t st) {
-    return launch_trace_mode<true>(pr, view0, nviews, Q, dout, st);
+    return launch_trace_mode<1>(pr, view0, nviews, Q, dout, st);
 }
 
 }  // namespace xrp

@@ -109,7 +109,8 @@ cudaError_t launch_finish(const float* img, int nviews, int res, int transparenc
                           unsigned short* alpha, float* minmax, cudaStream_t st);
 
 // xrp_kern_trace.cu: certificate tracing (k_trace); Q.trace 1: ray
-// certificates where the scene's chain is affine, else ball; 2: ball only.
+// certificates where the scene's chain is affine, curve certificates for
+// other deformation chains; 2: ball only.
 cudaError_t launch_trace(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                          cudaStream_t st);
 

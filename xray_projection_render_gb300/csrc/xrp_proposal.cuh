@@ -435,13 +435,23 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // geometrically; next to it the march steps sample by sample.  RAY (affine
 // deformation chains): the certificate is the ray bound of dens_ray32, the
 // distance along the ray to the next possible density change, so a ray
-// jumps straight to the next boundary instead of approaching it.  Samples
-// FP32 cannot decide go to the FP64 list like the other march modes.
+// jumps straight to the next boundary instead of approaching it.  CURVE
+// (smooth non-affine chains): the certificate is the curve bound of
+// dens_curve32, the first parameter at which the curved path of the
+// deformed samples can reach a boundary.  CERT: 0 ball, 1 ray, 2 curve.
+// Samples FP32 cannot decide go to the FP64 list like the other march modes.
 // Resident blocks per SM for depth < 3, measured: 4 (64 registers; lattice
 // with ray bounds 415 against 382 Mrays/s with 3 and 410 with 5, gyroid with
 // balls 1462 against 1406 with 3).
-template <int DEPTH, bool DEFS, bool HIER, bool RAY>
-__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 4)
+// Resident blocks per SM of the tracing kernel with curve certificates
+// (depth < 3): its Jacobian-vector products and quadratic bounds need more
+// registers than the ball and ray variants (at 64 registers ptxas spills
+// about 370 bytes per thread on the gyroid's depth-1 kernel, at 80 about 240).
+#ifndef XRP_CURVE_MIN_BLOCKS
+#define XRP_CURVE_MIN_BLOCKS 4
+#endif
+template <int DEPTH, bool DEFS, bool HIER, int CERT>
+__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT == 2 ? XRP_CURVE_MIN_BLOCKS : 4))
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
@@ -481,7 +491,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 4)
                 // a coarse sample's value decides refinement: FP64 in place;
                 // fine samples only add, so they go to the list (high bit)
                 const ViewDev& V = views[view0 + v];
-                sum = trace_sum_hier<DEPTH, DEFS, RAY>(
+                sum = trace_sum_hier<DEPTH, DEFS, CERT == 1, CERT == 2>(
                     Sl, L, ray, k0, k1,
                     [&](int q, bool fine) {
                         if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
@@ -491,7 +501,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : 4)
                     },
                     evals);
             } else {
-                sum = trace_sum<DEPTH, DEFS, RAY>(
+                sum = trace_sum<DEPTH, DEFS, CERT == 1, CERT == 2>(
                     Sl, L, ray, k0, k1,
                     [&](int k) {
                         unsigned slot = atomicAdd(Q.fb_count, 1u);

@@ -1,12 +1,13 @@
 // xrp_trace.cuh -- launch helpers of certificate tracing (k_trace in
 // xrp_proposal.cuh), instantiated per certificate kind in
-// xrp_kern_trace.cu (balls) and xrp_kern_trace_ray.cu (ray bounds).
+// xrp_kern_trace.cu (balls), xrp_kern_trace_ray.cu (ray bounds) and
+// xrp_kern_trace_curve.cu (curve bounds).
 #pragma once
 #include "xrp_launch.h"
 
 namespace xrp {
 
-template <int DEPTH, bool DEFS, bool RAY>
+template <int DEPTH, bool DEFS, int CERT>
 cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                     cudaStream_t st) {
     const int tpr = (pr.P.res + 15) / 16;
@@ -15,25 +16,29 @@ cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams&
     if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
     const size_t smem = (size_t)pr.S.nnodes * sizeof(Node);
     if (pr.L.hierarchical)
-        k_trace<DEPTH, DEFS, true, RAY><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
+        k_trace<DEPTH, DEFS, true, CERT><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
                                                                             nviews, Q, dout);
     else
-        k_trace<DEPTH, DEFS, false, RAY><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
+        k_trace<DEPTH, DEFS, false, CERT><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
                                                                              nviews, Q, dout);
     return cudaGetLastError();
 }
 
-template <bool RAY>
+// CERT 2 (curve bounds) serves deformed scenes only: DEFS is always on.
+template <int CERT>
 cudaError_t launch_trace_mode(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                               cudaStream_t st) {
-    if (pr.defs) {
-        if (pr.depth == 0) return trace_r<0, true, RAY>(pr, view0, nviews, Q, dout, st);
-        if (pr.depth == 1) return trace_r<1, true, RAY>(pr, view0, nviews, Q, dout, st);
-        return trace_r<3, true, RAY>(pr, view0, nviews, Q, dout, st);
+    if (CERT == 2 || pr.defs) {
+        if (pr.depth == 0) return trace_r<0, true, CERT>(pr, view0, nviews, Q, dout, st);
+        if (pr.depth == 1) return trace_r<1, true, CERT>(pr, view0, nviews, Q, dout, st);
+        return trace_r<3, true, CERT>(pr, view0, nviews, Q, dout, st);
     }
-    if (pr.depth == 0) return trace_r<0, false, RAY>(pr, view0, nviews, Q, dout, st);
-    if (pr.depth == 1) return trace_r<1, false, RAY>(pr, view0, nviews, Q, dout, st);
-    return trace_r<3, false, RAY>(pr, view0, nviews, Q, dout, st);
+    if constexpr (CERT != 2) {
+        if (pr.depth == 0) return trace_r<0, false, CERT>(pr, view0, nviews, Q, dout, st);
+        if (pr.depth == 1) return trace_r<1, false, CERT>(pr, view0, nviews, Q, dout, st);
+        return trace_r<3, false, CERT>(pr, view0, nviews, Q, dout, st);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace xrp

@@ -316,9 +316,9 @@ def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resoluti
     ``integration``, with ray bounds where the deformation chain is affine
     (``trace="ball"``: ball certificates only); the segment march needs
     "simple").  Host path
-    returns a float32 array [views, res, res]
-    (with ``stats``: (images, dict)); a contiguous float32 CUDA tensor as
-    ``out`` selects the device path."""
+    returns a float32 array [views, res, res]; a contiguous float32 CUDA
+    tensor as ``out`` selects the device path (the call then waits for the
+    stream).  With ``stats`` either path returns (images, dict)."""
     L = _lib.load()
     cams, n = cameras_from_angles(angles, R, fov)
     o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats)
@@ -338,6 +338,10 @@ def render_proposal(scene: Scene, proposal: Proposal | None, angles, *, resoluti
                                            ctypes.c_void_p(out.data_ptr()),
                                            ctypes.c_void_p(st.cuda_stream)),
               "xrp_render_proposal_device")
+        if stats:
+            c = (ctypes.c_uint64 * 11)()
+            L.xrp_proposal_last_stats(c)
+            return out, dict(zip(PROPOSAL_STATS, list(c)))
         return out
     if out is None:
         out = np.empty((n, resolution, resolution), dtype=np.float32)

@@ -163,9 +163,14 @@ def gyroid_sigmoid(res=2048, views=720) -> Workload:
 
 
 def reduced(w: Workload, res: int, views: int | None = None) -> Workload:
-    """The same scene at a smaller resolution / view subset (for parity tests)."""
+    """The same scene at another resolution and/or on an evenly strided
+    subset of its views (parity tests, profiling).  The name says so: the
+    full workload's name with ``_subset<views>x<res>^2`` appended."""
     ang = w.angles if views is None else w.angles[:: max(1, len(w.angles) // views)][:views]
-    return dataclasses.replace(w, res=res, angles=list(ang))
+    if res == w.res and len(ang) == len(w.angles):
+        return w
+    return dataclasses.replace(w, res=res, angles=list(ang),
+                               name=f"{w.name}_subset{len(ang)}x{res}^2")
 
 
 WORKLOADS = {
