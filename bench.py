@@ -264,8 +264,8 @@ def resolve_march(args, w):
 
 MARCH_PATHS = {
     "plain": "uniform-step integrator (main.go:144-154)",
-    "trace": "certificate tracing (ray certificates for affine deformation chains, ball "
-             "certificates otherwise)",
+    "trace": "certificate tracing (ray certificates for affine deformation chains, curve "
+             "certificates for the others)",
     "ball": "certificate tracing with ball certificates",
     "certificate": "segment march with certificates, no network",
     "proposal": "segment march routed by the trained 3 x 64 network (BF16, FP32 accumulate)",

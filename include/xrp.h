@@ -159,6 +159,11 @@ XRP_API void xrp_scene_destroy(xrp_scene* scene);
 /* Support box of the scene (where density may be non-zero), world units. */
 XRP_API int xrp_scene_support(const xrp_scene* scene, double lo[3], double hi[3]);
 
+/* MinFeatureSize() of the scene's object (objects.go:17, per type
+ * objects.go:74-1037): the reference's automatic step is this / 5 when ds < 0
+ * (main.go:350-353).  +inf for an empty collection. */
+XRP_API int xrp_scene_min_feature_size(const xrp_scene* scene, double* out);
+
 /*
  * Renders `num_views` cameras into host memory `out` (num_views*res*res
  * float32).  Same results as the reference CPU path (main.go:429-471) for the
@@ -351,20 +356,21 @@ XRP_API int xrp_mlp_grad(const float* params, const uint16_t* X, const float* y,
 
 /*
  * RenderVolumeProjectionsCUDA for callers that cannot allocate device
- * memory (code running under CUDA graph capture, a framework allocator that
- * owns the device, a fixed memory budget).  No counterpart in the reference
- * library.  `d_volume` ([z][x][y], float32) and `d_out` (num_cameras*res*res
- * float32) are device buffers of the caller; `cameras` stay on the host; the
- * work is queued on `stream` (a cudaStream_t, NULL for the legacy stream) and
- * the call returns after queuing.  It calls no cudaMalloc, cudaFree or other
- * allocating routine: its tables go to one static 1 MiB device array that
- * every GPU loading the library holds until exit.  Limits: the tables of one
+ * memory: a host framework whose allocator owns the device memory, or a
+ * service that runs under a fixed device-memory budget decided up front.
+ * No counterpart in the reference library.  `d_volume` ([z][x][y], float32)
+ * and `d_out` (num_cameras*res*res float32) are device buffers of the
+ * caller; `cameras` stay on the host; the work is queued on `stream` (a
+ * cudaStream_t, NULL for the legacy stream).  It calls no cudaMalloc,
+ * cudaFree or other allocating routine: its tables go to one static 1 MiB
+ * device array that every GPU loading the library holds until exit, copied
+ * there from host memory before the call returns.  Limits: the tables of one
  * call (about 192 B per camera, 8 B per image row and 12 B per sample of
  * the lattice [R-1.74, R+1.74]) must fit in 1 MiB (code 2 otherwise), and
  * every camera of a call must share R.  The first call on each device looks
- * the array up (cudaGetSymbolAddress) and should come before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race:
- * order them on one stream.  Results equal RenderVolumeProjectionsCUDA's.
+ * the array up (cudaGetSymbolAddress).  Calls share the array, so calls that
+ * overlap on the GPU race: order them on one stream.  Results equal
+ * RenderVolumeProjectionsCUDA's.
  */
 XRP_API int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, int nz,
                                       const XRayCameraParams* cameras, int num_cameras,

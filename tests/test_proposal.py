@@ -86,15 +86,31 @@ def _affine_collection():
     return W.Workload("affine_collection", coll, deform, [(10.0, 80.0), (200.0, 120.0)], 48, 0.004)
 
 
-TRACE_CASES = dict(CASES, affine_collection=_affine_collection)
+GAUSS = {"type": "gaussian", "amplitudes": [0.1, -0.05, 0.02], "sigmas": [0.3, 0.3, 0.5],
+         "centers": [0.0, 0.1, 0.0]}
+
+
+def _gaussian_collection():
+    # every primitive under a gaussian chain (curve certificates)
+    w = _affine_collection()
+    return W.Workload("gaussian_collection", w.obj, GAUSS, w.angles, w.res, w.ds)
+
+
+def _gaussian_lattice():
+    base = W.reduced(W.deformed_lattice(), 40, 2)
+    return W.Workload("gaussian_lattice", base.obj, GAUSS, base.angles, base.res, base.ds)
+
+
+TRACE_CASES = dict(CASES, affine_collection=_affine_collection, gaussian_collection=_gaussian_collection,
+                   gaussian_lattice=_gaussian_lattice)
 
 
 @pytest.mark.parametrize("mode", [True, "ball"])
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 @pytest.mark.parametrize("name", sorted(TRACE_CASES))
 def test_certificate_tracing_matches_oracle(X, name, integration, mode):
-    """Tracing with ray bounds (affine chains; the gyroid's sigmoid chain
-    falls back to balls) and with ball certificates only."""
+    """Tracing with ray bounds (affine chains), curve bounds (the gyroid's
+    sigmoid chain, gaussian chains) and with ball certificates only."""
     w = TRACE_CASES[name]()
     ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
                    integration=integration)
@@ -116,6 +132,19 @@ def test_ray_certificates_evaluate_less_than_balls(X):
     assert np.max(np.abs(a - b) / b) <= 2 * REL_TOL
     assert 2 * st_ray["evaluations"] < st_ball["evaluations"]
     print(f"\nevaluations: ray {st_ray['evaluations']}, ball {st_ball['evaluations']}")
+
+
+def test_curve_certificates_evaluate_less_than_balls(X):
+    # the gyroid under the sigmoid: the curve bound reaches the band edge in
+    # a step or two where balls approach it geometrically
+    w = W.reduced(W.gyroid_sigmoid(), 96, 2)
+    with X.Scene(w.obj, w.deformation) as s:
+        kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, stats=True)
+        a, st_curve = X.render_proposal(s, None, w.angles, trace=True, **kw)
+        b, st_ball = X.render_proposal(s, None, w.angles, trace="ball", **kw)
+    assert np.max(np.abs(a - b) / b) <= 2 * REL_TOL
+    assert 2 * st_curve["evaluations"] < st_ball["evaluations"]
+    print(f"\nevaluations: curve {st_curve['evaluations']}, ball {st_ball['evaluations']}")
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -276,7 +305,7 @@ def test_tracing_coarse_step(X):
 
 
 @pytest.mark.parametrize("name", ["deformed_lattice", "cube_minus_sphere_cylinder", "batched_scene0",
-                                  "affine_collection"])
+                                  "affine_collection", "gaussian_collection", "gaussian_lattice"])
 def test_ray_tracing_matches_plain_at_scale(X, name):
     """Ray certificates with the device's approximate reciprocals and square
     roots, on ~0.6 M rays per scene: traced renders equal the plain

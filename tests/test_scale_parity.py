@@ -148,13 +148,15 @@ def test_lattice_hierarchical(X, lattice, march):
            f"lattice hierarchical {march}")
 
 
-def test_gyroid_every_view_traced(X, gyroid):
+@pytest.mark.parametrize("march", ["trace", "ball"])
+def test_gyroid_every_view_traced(X, gyroid, march):
+    """Curve certificates (the sigmoid chain is not affine) and balls."""
     import torch
     w, s = gyroid
     rays = _rays(len(w.angles), w.res, RAYS, seed=51)
-    out, st = _render(X, s, w, w.angles, march="trace")
-    err = _check(_pick(out, rays, w.res), _oracle(w, w.angles, rays), "gyroid trace")
-    print(f"\ngyroid trace (720 x 2048^2): max rel {err:.2e}; counters {st}")
+    out, st = _render(X, s, w, w.angles, march=march)
+    err = _check(_pick(out, rays, w.res), _oracle(w, w.angles, rays), f"gyroid {march}")
+    print(f"\ngyroid {march} (720 x 2048^2): max rel {err:.2e}; counters {st}")
     del out
     torch.cuda.empty_cache()
 

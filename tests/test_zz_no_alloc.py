@@ -1,8 +1,9 @@
 """xrp_render_volume_noalloc: the render entry point for callers that cannot
-allocate device memory (code under CUDA graph capture, a framework allocator
-that owns the device, a fixed memory budget).  It must give the same images
-as RenderVolumeProjectionsCUDA, call after call, while keeping its tables in
-the library's static device array instead of allocating.
+allocate device memory (a host framework whose allocator owns the device, a
+service with a fixed device-memory budget).  It must give the same images as
+RenderVolumeProjectionsCUDA and as the FP64 oracle, call after call, while
+keeping its tables in the library's static device array instead of
+allocating: the device's free memory does not move across a call.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test."""
@@ -40,6 +41,7 @@ def _noalloc(torch, L, dvol, cams, res, ds, flat_field, stream):
 
 
 def test_noalloc_matches_render_volume_projections_two_calls(env):
+    from oracle import oracle as O
     torch, X, L, W = env
     vol = W.gaussian_blob_volume(48, 10, seed=21)[:, :40, :].copy()  # nz=48, nx=40, ny=48
     dvol = torch.from_numpy(vol).cuda()
@@ -53,6 +55,36 @@ def test_noalloc_matches_render_volume_projections_two_calls(env):
         assert np.all(np.isfinite(got))
         rel = np.abs(got.astype(np.float64) - ref) / ref
         assert rel.max() <= REL_TOL, f"max rel difference {rel.max():.3g}"
+        fp64 = O.render_volume_abi(vol, cams, res, ds, ff)
+        rel = np.abs(got.astype(np.float64) - fp64) / fp64
+        assert rel.max() <= REL_TOL, f"max rel error against the oracle {rel.max():.3g}"
+
+
+def test_noalloc_leaves_device_memory_unchanged(env):
+    torch, X, L, W = env
+    vol = W.gaussian_blob_volume(32, 6, seed=5)
+    dvol = torch.from_numpy(vol).cuda()
+    stream = torch.cuda.current_stream()
+    cams = X.xray_camera_params([(10.0, 90.0), (140.0, 70.0)], 4.0, 40.0)
+    out = torch.empty((2, 80, 80), device="cuda")
+
+    def call():
+        rc = L.xrp_render_volume_noalloc(ctypes.c_void_p(dvol.data_ptr()), 32, 32, 32,
+                                         cams.ctypes.data, 2, 80, ctypes.c_float(0.02),
+                                         ctypes.c_float(0.0), ctypes.c_void_p(out.data_ptr()),
+                                         ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, L.xrp_last_error()
+        stream.synchronize()
+
+    call()  # the first call on the device looks up the array
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    for _ in range(3):
+        call()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"device free memory moved by {free0 - free1} bytes"
+    assert torch.cuda.memory_reserved() == reserved0
 
 
 def test_noalloc_rejects_calls_beyond_its_array(env):

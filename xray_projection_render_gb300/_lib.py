@@ -82,6 +82,7 @@ SIGNATURES = {
     "xrp_scene_create": (c_int, [ctypes.c_char_p, ctypes.c_char_p, c_void_p, c_int, c_void_p]),
     "xrp_scene_destroy": (None, [c_void_p]),
     "xrp_scene_support": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "xrp_scene_min_feature_size": (c_int, [c_void_p, c_void_p]),
     "xrp_render": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "xrp_render_device": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "xrp_last_stats": (c_int, [c_void_p, c_void_p]),

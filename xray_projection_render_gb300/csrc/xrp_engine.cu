@@ -427,6 +427,75 @@ void fill_voxparams(const HostPrepared& hp, const float* data, const double* dat
     q.inner_margin = 4.0f * v.band_w + 2e-4f;
 }
 
+// Offsets of one render's tables inside their packed upload.
+struct TableLayout {
+    size_t nodes, n64, child, cells, items, defs, clear, vols, views, xs, xsf, s64, t32, fs, f64, ft32;
+};
+
+// Packs the scene image, the cameras, the pixel table and the sample
+// lattice of a prepared render into one host buffer.
+TableLayout pack_tables(const HostPrepared& hp, const std::vector<ViewDev>& views, Tables& T) {
+    const FlatScene& fs = hp.fs;
+    const HostLattice& hl = hp.hl;
+    TableLayout o;
+    o.nodes = T.add(fs.nodes);
+    o.n64 = T.add(fs.nodes64);
+    o.child = T.add(fs.child);
+    o.cells = T.add(fs.cells);
+    o.items = T.add(fs.items);
+    o.defs = T.add(fs.defs);
+    o.clear = T.add(fs.clear);
+    o.vols = T.add(hp.vols);
+    o.views = T.add(views);
+    o.xs = T.add(hp.xs);
+    o.xsf = T.add(hp.xsf);
+    o.s64 = T.add(hl.s64);
+    o.t32 = T.add(hl.t32);
+    o.fs = T.add(hl.fstart);
+    o.f64 = T.add(hl.f64);
+    o.ft32 = T.add(hl.ft32);
+    return o;
+}
+
+// Points a Prepared render at tables packed by pack_tables and uploaded to
+// the device address `base` (a pool buffer, or the no-allocation array).
+void bind_tables(const HostPrepared& hp, const std::vector<ViewDev>& views, const unsigned char* base,
+                 const TableLayout& o, cudaTextureObject_t tex, const float* vol0, const double* vol64_0,
+                 Prepared& out) {
+    const FlatScene& fs = hp.fs;
+    const HostLattice& hl = hp.hl;
+    out.S = hp.S;
+    SceneDev& S = out.S;
+    S.nodes = (const Node*)(base + o.nodes);
+    S.nodes64 = (const Node64*)(base + o.n64);
+    S.child = (const int32_t*)(base + o.child);
+    S.cells = (const int32_t*)(base + o.cells);
+    S.items = (const int32_t*)(base + o.items);
+    S.clear = (const float*)(base + o.clear);
+    S.defs = (const DefStep*)(base + o.defs);
+    S.vols = (const Volume*)(base + o.vols);
+    // tracing kernels stage node tables of up to 32 KB in shared memory
+    S.nnodes = fs.nodes.size() * sizeof(Node) <= 32768 ? (int32_t)fs.nodes.size() : 0;
+    out.L = hl.hdr;
+    Lattice& L = out.L;
+    L.s64 = (const double*)(base + o.s64);
+    L.t32 = (const float*)(base + o.t32);
+    L.fstart = (const int32_t*)(base + o.fs);
+    L.f64 = (const double*)(base + o.f64);
+    L.ft32 = (const float*)(base + o.ft32);
+    out.P = hp.P;
+    out.P.nviews = (int)views.size();
+    out.P.xs = (const double*)(base + o.xs);
+    out.P.xsf = (const float*)(base + o.xsf);
+    out.views = (const ViewDev*)(base + o.views);
+    out.volume_fast = hp.volume_fast;
+    out.depth = fs.depth;
+    out.defs = !fs.defs.empty();
+    out.tex = hp.volume_fast ? tex : 0;
+    out.empty = hl.hdr.K <= 0;
+    if (hp.volume_fast) fill_voxparams(hp, vol0, vol64_0, out.tex, out.vq);
+}
+
 // Everything a render needs on the device except the volume data.
 int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol_dev,
             const std::vector<const double*>& vol64_dev, const std::vector<ViewDev>& views,
@@ -442,50 +511,14 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
         hp.vols[k].data = vol_dev[k];
         hp.vols[k].data64 = vol64_dev[k];
     }
-    const FlatScene& fs = hp.fs;
-    const HostLattice& hl = hp.hl;
     Tables T;
-    size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
-    size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
-    size_t o_clear = T.add(fs.clear);
-    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs), o_xsf = T.add(hp.xsf);
-    size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
-    size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
+    const TableLayout o = pack_tables(hp, views, T);
     cudaError_t e = tab.alloc(E, T.host.size(), st);
     if (e != cudaSuccess) return cuda_fail(3, "table allocation", e);
     e = cudaMemcpyAsync(tab.p, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(5, "table upload", e);
-    unsigned char* base = (unsigned char*)tab.p;
-    out.S = hp.S;
-    SceneDev& S = out.S;
-    S.nodes = (const Node*)(base + o_nodes);
-    S.nodes64 = (const Node64*)(base + o_n64);
-    S.child = (const int32_t*)(base + o_child);
-    S.cells = (const int32_t*)(base + o_cells);
-    S.items = (const int32_t*)(base + o_items);
-    S.clear = (const float*)(base + o_clear);
-    S.defs = (const DefStep*)(base + o_defs);
-    S.vols = (const Volume*)(base + o_vols);
-    // tracing kernels stage node tables of up to 32 KB in shared memory
-    S.nnodes = fs.nodes.size() * sizeof(Node) <= 32768 ? (int32_t)fs.nodes.size() : 0;
-    out.L = hl.hdr;
-    Lattice& L = out.L;
-    L.s64 = (const double*)(base + o_s64);
-    L.t32 = (const float*)(base + o_t32);
-    L.fstart = (const int32_t*)(base + o_fs);
-    L.f64 = (const double*)(base + o_f64);
-    L.ft32 = (const float*)(base + o_ft32);
-    out.P = hp.P;
-    out.P.nviews = (int)views.size();
-    out.P.xs = (const double*)(base + o_xs);
-    out.P.xsf = (const float*)(base + o_xsf);
-    out.views = (const ViewDev*)(base + o_views);
-    out.volume_fast = hp.volume_fast;
-    out.depth = fs.depth;
-    out.defs = !fs.defs.empty();
-    out.tex = hp.volume_fast ? tex : 0;
-    out.empty = hl.hdr.K <= 0;
-    if (hp.volume_fast) fill_voxparams(hp, vol_dev[0], vol64_dev[0], out.tex, out.vq);
+    bind_tables(hp, views, (const unsigned char*)tab.p, o, tex, vol_dev.empty() ? nullptr : vol_dev[0],
+                vol64_dev.empty() ? nullptr : vol64_dev[0], out);
     return 0;
 }
 
@@ -770,6 +803,12 @@ int xrp_scene_support(const xrp_scene* s, double lo[3], double hi[3]) {
         lo[a] = s->sup_lo[a];
         hi[a] = s->sup_hi[a];
     }
+    return 0;
+}
+
+int xrp_scene_min_feature_size(const xrp_scene* s, double* out) {
+    if (!s || !out) return fail(1, "null pointer");
+    *out = min_feature_size(s->hs);
     return 0;
 }
 
@@ -1739,9 +1778,9 @@ int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
 // render without device allocation
 // ---------------------------------------------------------------------------
 //
-// For callers that must not allocate device memory -- code that runs while
-// a CUDA graph is being captured, allocators that own the whole device, or
-// hosts whose memory budget is fixed up front.  The per-call tables (scene
+// For callers that must not allocate device memory -- host frameworks whose
+// allocator owns the whole device, or services whose device-memory budget is
+// fixed up front.  The per-call tables (scene
 // image, sample lattice, pixel table, cameras) live in the static array
 // below instead of a stream-ordered pool allocation; the volume and the
 // images are the caller's device buffers.  Every GPU that loads the library
@@ -1804,46 +1843,19 @@ extern "C" int xrp_render_volume_noalloc(const float* d_volume, int nx, int ny, 
     }
     hp.vols[0].data = d_volume;
     hp.vols[0].data64 = nullptr;
-    const FlatScene& fs = hp.fs;
-    const HostLattice& hl = hp.hl;
     Tables T;
-    size_t o_nodes = T.add(fs.nodes), o_n64 = T.add(fs.nodes64), o_child = T.add(fs.child);
-    size_t o_cells = T.add(fs.cells), o_items = T.add(fs.items), o_defs = T.add(fs.defs);
-    size_t o_clear = T.add(fs.clear);
-    size_t o_vols = T.add(hp.vols), o_views = T.add(views), o_xs = T.add(hp.xs), o_xsf = T.add(hp.xsf);
-    size_t o_s64 = T.add(hl.s64), o_t32 = T.add(hl.t32), o_fs = T.add(hl.fstart);
-    size_t o_f64 = T.add(hl.f64), o_ft32 = T.add(hl.ft32);
+    const TableLayout o = pack_tables(hp, views, T);
     if (T.host.size() > kNoAllocScratchBytes)
         return fail(2, "this call needs %zu bytes of tables; the no-allocation entry point holds "
                        "at most %zu (fewer cameras, a smaller resolution or a larger ds fit)",
                     T.host.size(), kNoAllocScratchBytes);
-    // every byte the kernel reads is written here, so nothing needs clearing
+    // every byte the kernel reads is written here, so nothing needs clearing;
+    // the copy reads the pageable host buffer before the call returns
     cudaError_t e = cudaMemcpyAsync(base, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(5, "table upload", e);
+    // per-tap loads: a texture would need an array allocation
     Prepared pr;
-    pr.S = hp.S;
-    pr.S.nodes = (const Node*)(base + o_nodes);
-    pr.S.nodes64 = (const Node64*)(base + o_n64);
-    pr.S.child = (const int32_t*)(base + o_child);
-    pr.S.cells = (const int32_t*)(base + o_cells);
-    pr.S.items = (const int32_t*)(base + o_items);
-    pr.S.clear = (const float*)(base + o_clear);
-    pr.S.defs = (const DefStep*)(base + o_defs);
-    pr.S.vols = (const Volume*)(base + o_vols);
-    pr.L = hl.hdr;
-    pr.L.s64 = (const double*)(base + o_s64);
-    pr.L.t32 = (const float*)(base + o_t32);
-    pr.L.fstart = (const int32_t*)(base + o_fs);
-    pr.L.f64 = (const double*)(base + o_f64);
-    pr.L.ft32 = (const float*)(base + o_ft32);
-    pr.P = hp.P;
-    pr.P.nviews = ncams;
-    pr.P.xs = (const double*)(base + o_xs);
-    pr.P.xsf = (const float*)(base + o_xsf);
-    pr.views = (const ViewDev*)(base + o_views);
-    pr.volume_fast = hp.volume_fast;  // per-tap loads: a texture would need an array allocation
-    pr.tex = 0;
-    if (pr.volume_fast) fill_voxparams(hp, d_volume, nullptr, 0, pr.vq);
+    bind_tables(hp, views, base, o, 0, d_volume, nullptr, pr);
     const int tpv = ((res + 15) / 16) * ((res + 15) / 16);
     const int per_launch = std::max(1, (int)(0x7fffffffL / tpv));
     size_t img = (size_t)res * res;

@@ -91,6 +91,10 @@ struct Loader {
             n.d[12] = to_float(need(m, "rho"), "rho is not a float64");
             for (int i = 0; i < 3; i++) n.d[i] = o[i];
             inv3_cols(v0, v1, v2, n.d + 3);
+            // edge lengths (Vec3.Len) for MinFeatureSize (objects.go:257-259)
+            n.d[13] = std::sqrt(v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+            n.d[14] = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+            n.d[15] = std::sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
         } else if (t == "gyroid") {  // objects.go:983-1012
             n.type = N_GYROID;
             to_vec_strict(need(m, "center"), n.d, "center");
@@ -333,6 +337,34 @@ HostScene load_scene(const char* object_json, const char* deformation_json,
     }
     return hs;
 }
+
+// MinFeatureSize of a node (objects.go:74-76, 123-125, 181-183, 257-259,
+// 352-354, 440-446, 584-586, 857-860, 1034-1037): the length the reference's
+// automatic step divides by five (main.go:350-353).
+static double min_feature(const HostScene& hs, int id) {
+    const HNode& n = hs.nodes[id];
+    const double* d = n.d;
+    switch (n.type) {
+    case N_SPHERE: return d[3];
+    case N_BOX: return 0.1 * std::min(d[3], std::min(d[4], d[5]));
+    case N_CYL: return d[6];
+    case N_PPD: return 0.2 * std::min(d[13], std::min(d[14], d[15]));
+    case N_GYROID: return d[3] * d[4] * 0.1;
+    case N_COLL: {
+        double out = INFINITY;
+        for (int k : n.kids) out = std::min(out, min_feature(hs, k));
+        return out;
+    }
+    case N_TESS: return min_feature(hs, n.sub);
+    case N_VOXEL: {
+        const HVolume& v = hs.vols[n.vol];
+        return 2.0 / (double)std::max(v.nx, std::max(v.ny, v.nz));
+    }
+    default: return INFINITY;
+    }
+}
+
+double min_feature_size(const HostScene& hs) { return hs.root < 0 ? INFINITY : min_feature(hs, hs.root); }
 
 HostScene volume_scene(const float* data_dev, int nx, int ny, int nz) {
     HostScene hs;

@@ -58,6 +58,9 @@ HostScene load_scene(const char* object_json, const char* deformation_json,
 // A scene made of one voxel grid (the RenderVolumeProjectionsCUDA path).
 HostScene volume_scene(const float* data_dev, int nx, int ny, int nz);
 
+// MinFeatureSize of the root object (the Object interface, objects.go:17).
+double min_feature_size(const HostScene& hs);
+
 // Inputs of the error analysis that are fixed per render call.
 struct RenderGeometry {
     double R = 4.0;        // camera distance
