@@ -79,7 +79,9 @@ def parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--impl", default="engine", choices=["engine", "reference", "reference_gpu"],
+                   help="engine (this library), reference (the reference's CPU algorithm on the "
+                        "host cores) or reference_gpu (the reference's own GPU kernel, voxel grid only)")
     p.add_argument("--workload", default="lattice",
                    choices=["lattice", "gyroid", "voxel", "cube", "batched", "finish", "voxelize"],
                    help="lattice (default, the headline), the gyroid, the voxel grid, the cube minus "
@@ -314,6 +316,67 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "config": cfg, "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_gpu(args):
+    """The reference's own GPU kernel (render_kernel, cuda_backend.cu:19-80,
+    compiled from its unmodified source into oracle/_ref) on the voxel-grid
+    workload, driven the way RenderVolumeProjectionsCUDA drives it
+    (cuda_backend.cu:82-203): end to end (allocation, upload, per-camera
+    launch, synchronisation and copy back) and kernel only (CUDA events
+    around back-to-back launches, L2 flushed), with its error against FP64
+    on seeded rays.  The reference GPU path supports voxel grids only."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from xray_projection_render_gb300 import workloads as W
+    if args.workload != "voxel":
+        print(json.dumps({"impl": "reference_gpu", "unavailable":
+                          "the reference's GPU kernel renders voxel grids only (--workload voxel)"}),
+              flush=True)
+        return
+    from oracle import oracle as O
+    from oracle import ref_gpu
+    try:
+        ref_gpu.build()
+    except Exception as ex:
+        print(json.dumps({"impl": "reference_gpu", "unavailable": f"harness build failed: {ex}"}))
+        return
+    w = make_workload(args.workload, W, args.views, args.res)
+    cams21 = O.xray_camera_params(w.angles, w.R, w.fov)
+    rng = np.random.default_rng(4321)
+    rays = draw_rays(rng, len(w.angles), w.res, 20000)
+    ref = O.render_volume_abi(w.volume, cams21, w.res, np.float32(w.ds), rays=rays)
+    line = {"impl": "reference_gpu", "metric": VOXEL_METRIC, "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": workload_config(w, "plain", 1, args.workload), "arch": {}}
+    for arch in ("sm_103a", "sm_100"):
+        if not os.path.exists(ref_gpu.CUBINS[arch]):
+            line["arch"][arch] = {"unavailable": "cubin not built (the reference tree was absent)"}
+            continue
+        try:
+            rec = ref_gpu.run(w.volume, cams21, w.res, w.ds, warmup=max(1, args.warmup),
+                              steps=args.steps, arch=arch, images=True)
+        except Exception as ex:
+            line["arch"][arch] = {"unavailable": str(ex)[:300]}
+            continue
+        imgs = rec.pop("images")
+        got = imgs[rays[:, 0], rays[:, 1], rays[:, 2]].astype(np.float64)
+        d = np.abs(got - ref)
+        k_s = float(np.mean(rec["kernel_ms"])) * 1e-3
+        e_s = float(np.mean(rec["e2e_ms"])) * 1e-3
+        line["arch"][arch] = {
+            "value": rec["rays"] / k_s / 1e6, "ms_per_step": k_s * 1e3,
+            "e2e": {"value": rec["rays"] / e_s / 1e6, "unit": "Mrays/s", "ms_per_step": e_s * 1e3},
+            "error_vs_fp64": {"max_rel": float(np.max(d / ref)), "max_abs": float(np.max(d)),
+                              "rays": int(len(rays))}}
+    best = [a for a in line["arch"].values() if "value" in a]
+    if best:
+        line["value"] = best[0]["value"]
+        line["e2e"] = best[0]["e2e"]
+        line["error_vs_fp64"] = best[0]["error_vs_fp64"]
     print(json.dumps(line), flush=True)
 
 
@@ -739,6 +802,22 @@ def bench_batched(args):
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_multi(ws[:8], args.cpu_seconds)
     if rank == 0:
+        # error of the replayed batch against FP64: seeded rays of the first
+        # eight items, from the items' images (copied back after the timing)
+        worst_rel, worst_abs, nrays = 0.0, 0.0, 0
+        rng = np.random.default_rng(4321)
+        for k, w in enumerate(ws[:8]):
+            rays = draw_rays(rng, len(w.angles), w.res, 2500)
+            host = b.item(k)
+            got = host[rays[:, 0], rays[:, 1], rays[:, 2]].astype(np.float64)
+            ref = oracle_rays(dataclasses.replace(w, ds=ds), w.angles, rays)
+            d = np.abs(got - ref)
+            worst_rel = max(worst_rel, float(np.max(d / ref)))
+            worst_abs = max(worst_abs, float(np.max(d)))
+            nrays += len(rays)
+        line["error_vs_fp64"] = {"max_rel": worst_rel, "max_abs": worst_abs, "rays": nrays,
+                                 "items": "first 8 of the batch"}
+    if rank == 0:
         print(json.dumps(line), flush=True)
     b.close()
     for s in scenes:
@@ -842,6 +921,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.impl == "reference_gpu":
+        return run_reference_gpu(args)
     if args.workload == "batched":
         return bench_batched(args)
     if args.workload in ("finish", "voxelize"):

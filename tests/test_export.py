@@ -52,14 +52,22 @@ def test_voxelize_scene_matches_oracle(X, name):
     assert np.array_equal(u, want)
 
 
-def test_finish_images(X):
+@pytest.mark.parametrize("res,offset", [(45, 0), (100, 0), (64, 0), (64, 1)],
+                         ids=["odd_side", "side_4k", "side_64", "misaligned"])
+def test_finish_images(X, res, offset):
+    """Odd sides and misaligned buffers take the scalar kernel, sides that
+    are multiples of 4 with aligned buffers the vectorised one."""
     import torch
     rng = np.random.default_rng(3)
-    n, res = 3, 45
+    n = 3
     img = rng.uniform(0.0, 1.0, (n, res, res)).astype(np.float32)
     img[0, 3, 4] = 1.0
     img[1, 0, 0] = 0.0
-    d = torch.from_numpy(img).cuda()
+    img[2, res - 1, res - 1] = np.float32(1.0) - np.float32(2.0 ** -24)
+    img[2, 5, res - 2] = np.float32(3.0) / np.float32(65535.0)  # near a whole quantum
+    flat = torch.zeros(n * res * res + offset, device="cuda")
+    flat[offset:] = torch.from_numpy(img.reshape(-1)).cuda()
+    d = flat[offset:].view(n, res, res)
     for transparency in (False, True):
         gray, alpha, mm = X.finish_images(d, transparency=transparency)
         torch.cuda.synchronize()

@@ -388,6 +388,30 @@ static bool volume_gathers_enabled() {
     return !(e && strcmp(e, "loads") == 0);
 }
 
+// Host-side fault injection for the error paths (tests only; no GPU work
+// fails): XRP_FAULT holds a comma-separated list of sites -- alloc (volume
+// allocation, code 3), upload (volume upload, 4), tables (table upload, 5),
+// output (image buffer allocation, 6), launch (kernel launch, 7), copy
+// (image copy, 8) -- and each listed site reports the CUDA error it would
+// see instead of calling CUDA.  Unset (the default) it injects nothing.
+static cudaError_t injected(const char* site) {
+    const char* e = getenv("XRP_FAULT");
+    if (!e || !*e) return cudaSuccess;
+    const size_t n = strlen(site);
+    for (const char* p = e; *p;) {
+        const char* q = strchr(p, ',');
+        size_t len = q ? (size_t)(q - p) : strlen(p);
+        if (len == n && strncmp(p, site, n) == 0) {
+            if (!strcmp(site, "alloc") || !strcmp(site, "output")) return cudaErrorMemoryAllocation;
+            if (!strcmp(site, "launch")) return cudaErrorLaunchFailure;
+            return cudaErrorInvalidValue;  // upload, tables, copy
+        }
+        if (!q) break;
+        p = q + 1;
+    }
+    return cudaSuccess;
+}
+
 // Packs small tables into one upload.
 struct Tables {
     std::vector<unsigned char> host;
@@ -515,7 +539,8 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
     const TableLayout o = pack_tables(hp, views, T);
     cudaError_t e = tab.alloc(E, T.host.size(), st);
     if (e != cudaSuccess) return cuda_fail(3, "table allocation", e);
-    e = cudaMemcpyAsync(tab.p, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, st);
+    if ((e = injected("tables")) == cudaSuccess)
+        e = cudaMemcpyAsync(tab.p, T.host.data(), T.host.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(5, "table upload", e);
     bind_tables(hp, views, (const unsigned char*)tab.p, o, tex, vol_dev.empty() ? nullptr : vol_dev[0],
                 vol64_dev.empty() ? nullptr : vol64_dev[0], out);
@@ -587,7 +612,8 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     if (!out_host) {
         for (int v0 = 0; v0 < nviews; v0 += max_views_per_launch) {
             int n = std::min(max_views_per_launch, nviews - v0);
-            if ((e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st, pl)) != cudaSuccess)
+            if ((e = injected("launch")) != cudaSuccess ||
+                (e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st, pl)) != cudaSuccess)
                 return cuda_fail(7, "kernel launch", e);
         }
     } else {
@@ -596,7 +622,8 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
         int nchunks = (int)((nviews + chunk - 1) / chunk);
         PoolBuf buf[2];
         for (int b = 0; b < std::min(2, nchunks); b++)
-            if ((e = buf[b].alloc(E, chunk * img * sizeof(float), st)) != cudaSuccess)
+            if ((e = injected("output")) != cudaSuccess ||
+                (e = buf[b].alloc(E, chunk * img * sizeof(float), st)) != cudaSuccess)
                 return cuda_fail(6, "image buffer allocation", e);
         cudaEvent_t kev[2], cev[2];
         for (int b = 0; b < 2; b++) {
@@ -608,7 +635,8 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
             if (c >= 2) cudaStreamWaitEvent(st, cev[b], 0);
             int v0 = (int)(c * chunk);
             int n = (int)std::min(chunk, (size_t)(nviews - v0));
-            cudaError_t le = launch(pr, v0, n, o.integration, (float*)buf[b].p, stats, st, pl);
+            cudaError_t le = injected("launch");
+            if (le == cudaSuccess) le = launch(pr, v0, n, o.integration, (float*)buf[b].p, stats, st, pl);
             cudaEventRecord(kev[b], st);
             return le;
         };
@@ -623,8 +651,9 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
             int v0 = (int)(c * chunk);
             size_t n = std::min(chunk, (size_t)(nviews - v0));
             cudaStreamWaitEvent(st_copy, kev[b], 0);
-            e = cudaMemcpyAsync(out + (size_t)v0 * img, buf[b].p, n * img * sizeof(float),
-                                cudaMemcpyDeviceToHost, st_copy);
+            if ((e = injected("copy")) == cudaSuccess)
+                e = cudaMemcpyAsync(out + (size_t)v0 * img, buf[b].p, n * img * sizeof(float),
+                                    cudaMemcpyDeviceToHost, st_copy);
             if (e != cudaSuccess) {
                 code = cuda_fail(8, "image copy", e);
                 break;
@@ -904,6 +933,7 @@ int xrp_finish_images(const float* d_images, int nviews, int res, int transparen
                       uint16_t* d_alpha, float* d_minmax, void* stream) {
     if (!d_images || !d_gray || !d_minmax) return fail(1, "null pointer");
     if (nviews <= 0 || res <= 0) return fail(2, "bad sizes");
+    if (nviews > 65535) return fail(2, "at most 65535 views per call");
     cudaError_t e = launch_finish(d_images, nviews, res, transparency, (unsigned short*)d_gray,
                                   (unsigned short*)d_alpha, d_minmax, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(7, "finishing kernel", e);
@@ -1733,9 +1763,10 @@ int RenderVolumeProjectionsCUDA(const float* volume, int nx, int ny, int nz,
         // re-evaluation of uncertain samples reads the linear copy below
         if ((e = tex.create(volume, nx, ny, nz, st)) != cudaSuccess) return cuda_fail(3, "volume texture", e);
     }
-    if ((e = dvol.alloc(E, nvox * sizeof(float), st)) != cudaSuccess)
+    if ((e = injected("alloc")) != cudaSuccess || (e = dvol.alloc(E, nvox * sizeof(float), st)) != cudaSuccess)
         return cuda_fail(3, "volume allocation", e);
-    if ((e = cudaMemcpyAsync(dvol.p, volume, nvox * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    if ((e = injected("upload")) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dvol.p, volume, nvox * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return cuda_fail(4, "volume upload", e);
     HostScene hs = volume_scene((const float*)dvol.p, nx, ny, nz);
     std::vector<const float*> vdev{(const float*)dvol.p};

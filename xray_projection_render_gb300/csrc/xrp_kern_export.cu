@@ -137,6 +137,97 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// The same finishing for images whose side is a multiple of 4 and whose
+// buffers are 16-byte (input) and 8-byte (outputs) aligned: 64x64 tiles,
+// each thread issuing its tile's four 16-byte loads before it touches any
+// (16 KB in flight per block, streaming loads: the images are read once)
+// and writing four output pixels of a row with one 8-byte store.  A block
+// walks kFinishVTiles tiles along j.
+constexpr int kFinishVTiles = 4;
+__global__ void __launch_bounds__(256)
+    k_finish_v4(const float* __restrict__ img, int res, int transparency, unsigned short* __restrict__ gray,
+                unsigned short* __restrict__ alpha, unsigned* __restrict__ minmax_bits) {
+    __shared__ float tile[64][65];
+    __shared__ unsigned red[2][8];
+    const int v = blockIdx.z;
+    const int i0 = blockIdx.y * 64;
+    const float* src = img + (size_t)v * res * res;
+    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;  // 16 x 16 threads
+    unsigned lo = 0xffffffffu, hi = 0u;                       // ordered bits
+    for (int tj = 0; tj < kFinishVTiles; tj++) {
+        const int j0 = (blockIdx.x * kFinishVTiles + tj) * 64;
+        if (j0 >= res) break;
+        const int j = j0 + 4 * lx;  // j < res implies j + 3 < res (res % 4 == 0)
+        float4 q[4];
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int i = i0 + ly + 16 * p;
+            q[p] = (i < res && j < res) ? __ldcs(reinterpret_cast<const float4*>(src + (size_t)i * res + j))
+                                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int i = i0 + ly + 16 * p;
+            const float e[4] = {q[p].x, q[p].y, q[p].z, q[p].w};
+            if (i < res && j < res) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const unsigned b = __float_as_uint(e[k]);
+                    const unsigned ob = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+                    lo = ob < lo ? ob : lo;
+                    hi = ob > hi ? ob : hi;
+                }
+            }
+            float* t = &tile[ly + 16 * p][4 * lx];
+#pragma unroll
+            for (int k = 0; k < 4; k++) t[k] = e[k];
+        }
+        __syncthreads();
+        // output rows y = res-1-j (j = j0 + c), columns x = i0 + 4*lx .. +3
+        const int i = i0 + 4 * lx;
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int c = ly + 16 * p;
+            const int jj = j0 + c;
+            if (jj < res && i < res) {
+                unsigned short g[4], a[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const float val = tile[4 * lx + k][c];
+                    // uint16(float64(val) * 0xffff), as in k_finish
+                    const float pr = val * 65535.0f;
+                    const float er = fmaf(val, 65535.0f, -pr);
+                    float t = truncf(pr);
+                    if (t == pr && er < 0.0f) t -= 1.0f;
+                    t = t <= 0.0f ? 0.0f : (t >= 65535.0f ? 65535.0f : t);
+                    g[k] = (unsigned short)t;
+                    a[k] = transparency ? (val < 1.0f ? 0xffff : 0) : 0xffff;
+                }
+                const size_t o = (size_t)v * res * res + (size_t)(res - 1 - jj) * res + i;
+                *reinterpret_cast<ushort4*>(gray + o) = make_ushort4(g[0], g[1], g[2], g[3]);
+                if (alpha) *reinterpret_cast<ushort4*>(alpha + o) = make_ushort4(a[0], a[1], a[2], a[3]);
+            }
+        }
+        __syncthreads();
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red[0][warp] = lo;
+        red[1][warp] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; w++) {
+            lo = red[0][w] < lo ? red[0][w] : lo;
+            hi = red[1][w] > hi ? red[1][w] : hi;
+        }
+        atomicMin(&minmax_bits[2 * v], lo);
+        atomicMax(&minmax_bits[2 * v + 1], hi);
+    }
+}
+
 __global__ void k_minmax_init(unsigned* mm, int n) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         mm[2 * q] = 0xffffffffu;
@@ -158,8 +249,15 @@ cudaError_t launch_finish(const float* img, int nviews, int res, int transparenc
     unsigned* mm = reinterpret_cast<unsigned*>(minmax);
     int ib = (nviews + 255) / 256;
     k_minmax_init<<<ib, 256, 0, st>>>(mm, nviews);
-    dim3 grid((res + 32 * kFinishTiles - 1) / (32 * kFinishTiles), (res + 31) / 32, nviews);
-    k_finish<<<grid, 256, 0, st>>>(img, res, transparency, gray, alpha, mm);
+    const bool vec = res % 4 == 0 && ((uintptr_t)img & 15) == 0 && ((uintptr_t)gray & 7) == 0 &&
+                     ((uintptr_t)alpha & 7) == 0;
+    if (vec) {
+        dim3 grid((res + 64 * kFinishVTiles - 1) / (64 * kFinishVTiles), (res + 63) / 64, nviews);
+        k_finish_v4<<<grid, 256, 0, st>>>(img, res, transparency, gray, alpha, mm);
+    } else {
+        dim3 grid((res + 32 * kFinishTiles - 1) / (32 * kFinishTiles), (res + 31) / 32, nviews);
+        k_finish<<<grid, 256, 0, st>>>(img, res, transparency, gray, alpha, mm);
+    }
     k_minmax_final<<<(2 * nviews + 255) / 256, 256, 0, st>>>(mm, nviews);
     return cudaGetLastError();
 }
