@@ -95,6 +95,8 @@ def parse():
                         "the voxel grid; plain integrator, per-ray certificate tracing (ray bounds "
                         "for affine deformation chains), tracing with ball certificates only, "
                         "segment march with certificates and no network, or the trained proposal")
+    p.add_argument("--integration", default="simple", choices=["simple", "hierarchical"],
+                   help="integrator (main.go:144-199); the reference CLI's default is hierarchical")
     p.add_argument("--views", type=int, default=0, help="view count (0: the workload's)")
     p.add_argument("--res", type=int, default=0, help="resolution (0: the workload's)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -212,22 +214,28 @@ def oracle_rays(w, angles, rays, threads=None, integration="simple"):
                     integration=integration, rays=rays, nthreads=threads or os.cpu_count() or 1)
 
 
-def cpu_baseline(w, seconds, threads=None, seed=1234):
+def cpu_baseline(w, seconds, threads=None, seed=1234, integration="simple"):
     """The oracle on all host cores on seeded random rays of `w` for about
     `seconds`: (cpu_baseline record, rays, FP64 transmittances)."""
     threads = threads or os.cpu_count() or 1
     rng = np.random.default_rng(seed)
     n = 2000
     t = time.perf_counter()
-    oracle_rays(w, w.angles, draw_rays(rng, len(w.angles), w.res, n), threads)
+    oracle_rays(w, w.angles, draw_rays(rng, len(w.angles), w.res, n), threads, integration)
     dt = time.perf_counter() - t
-    n2 = int(max(2000, min(60_000_000, 1.3 * n * seconds / max(dt, 1e-3))))
-    rays = draw_rays(rng, len(w.angles), w.res, n2)
-    t = time.perf_counter()
-    ref = oracle_rays(w, w.angles, rays, threads)
-    dt2 = time.perf_counter() - t
-    return ({"value": n2 / dt2 / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-             "sample": f"{n2} seeded random rays of {w.name} ({dt2:.1f} s)"}, rays, ref)
+    # batches sized from the probe, until the timed renders reach `seconds`
+    batch = int(max(2000, min(20_000_000, 0.35 * n * seconds / max(dt, 1e-3))))
+    all_rays, all_ref, spent = [], [], 0.0
+    while spent < seconds and sum(len(r) for r in all_rays) < 60_000_000:
+        rays = draw_rays(rng, len(w.angles), w.res, batch)
+        t = time.perf_counter()
+        all_ref.append(oracle_rays(w, w.angles, rays, threads, integration))
+        spent += time.perf_counter() - t
+        all_rays.append(rays)
+    rays = np.concatenate(all_rays)
+    ref = np.concatenate(all_ref)
+    return ({"value": len(rays) / spent / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+             "sample": f"{len(rays)} seeded random rays of {w.name} ({spent:.1f} s)"}, rays, ref)
 
 
 def error_vs_fp64(out, rays, ref, res):
@@ -248,10 +256,10 @@ def subset_views(angles, views):
     return list(angles[:: max(1, len(angles) // views)][:views])
 
 
-def workload_config(w, march, world, name):
+def workload_config(w, march, world, name, integration="simple"):
     """`config` of a scene workload: the same dict in both arms."""
     cfg = {"workload": w.name, "views": len(w.angles), "res": w.res, "ds": w.ds,
-           "integrator": "simple", "R": w.R, "fov": w.fov, "march": march,
+           "integrator": integration, "R": w.R, "fov": w.fov, "march": march,
            "l2": "flushed before every timed step (256 MiB write)",
            "parallelism": f"views k mod {world}"}
     cfg.update(DEFINITIONS.get(name, {}))
@@ -298,10 +306,10 @@ def run_reference(args):
     else:
         w = make_workload(args.workload, W, args.views, args.res)
         name = w.name
-        cfg = workload_config(w, resolve_march(args, w), world, args.workload)
+        cfg = workload_config(w, resolve_march(args, w), world, args.workload, args.integration)
 
         def measure(sec):
-            return cpu_baseline(w, sec)[0]
+            return cpu_baseline(w, sec, integration=args.integration)[0]
         metric = VOXEL_METRIC if args.workload == "voxel" else (
             HEADLINE_METRIC if args.workload == "lattice" else f"Mrays/s on 1 GB300 ({name})")
     vals = []
@@ -426,9 +434,10 @@ def _event_time(torch, step, steps, stream, flush):
     return float(np.mean(times))
 
 
-def scene_step(X, scene, w, angles, march, out, stream, prop=None, volume_path="gather"):
+def scene_step(X, scene, w, angles, march, out, stream, prop=None, volume_path="gather",
+               integration="simple"):
     """One render of `angles` by `march` into the device buffer `out`."""
-    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov)
+    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, integration=integration)
     if march == "plain":
         return lambda: X.render(scene, angles, out=out, stream=stream, volume_path=volume_path, **kw)
     trace = {"trace": True, "ball": "ball"}.get(march, False)
@@ -534,12 +543,14 @@ def bench_scene(args):
     scene = X.Scene(w.obj, w.deformation, vols)
     out = torch.empty((n_my, res, res), device=dev, dtype=torch.float32)
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)  # 256 MiB > L2
-    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov, volume_path=args.volume_path)
+    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov, volume_path=args.volume_path,
+              integration=args.integration)
 
     prop = None
     if march == "proposal":
         prop = X.Proposal(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, segment=64)
-    step = scene_step(X, scene, w, my_angles, march, out, stream, prop, args.volume_path)
+    step = scene_step(X, scene, w, my_angles, march, out, stream, prop, args.volume_path,
+                      args.integration)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -553,7 +564,7 @@ def bench_scene(args):
         # evaluation, or one density per dense sample)
         _, pst = X.render_proposal(scene, prop, my_angles[:nstat], resolution=res, ds=w.ds, R=w.R,
                                    fov=w.fov, segment=64, refine=march == "proposal",
-                                   trace=_trace_mode(march), stats=True)
+                                   trace=_trace_mode(march), stats=True, integration=args.integration)
         evals_step = (pst["evaluations"] + pst["dense_samples"]) * n_my / nstat
     if world > 1:
         torch.distributed.barrier()
@@ -570,9 +581,9 @@ def bench_scene(args):
         if args.no_cpu_baseline:
             rng = np.random.default_rng(1234)
             rays = draw_rays(rng, n_my, res, 20000)
-            ref = oracle_rays(wm, my_angles, rays)
+            ref = oracle_rays(wm, my_angles, rays, integration=args.integration)
         else:
-            cb, rays, ref = cpu_baseline(wm, args.cpu_seconds)
+            cb, rays, ref = cpu_baseline(wm, args.cpu_seconds, integration=args.integration)
         err = error_vs_fp64(out, rays, ref, res)
 
     # end to end through the host-facing C ABI, pinned host buffers, inputs
@@ -602,7 +613,8 @@ def bench_scene(args):
                 else:  # the network trained on the resident scene applies to this copy
                     X.render_proposal(s2, prop, my_angles, resolution=res, ds=w.ds, R=w.R,
                                       fov=w.fov, segment=64, refine=march == "proposal",
-                                      trace=_trace_mode(march), out=out_host)
+                                      trace=_trace_mode(march), out=out_host,
+                                      integration=args.integration)
     if not args.no_e2e:
         e2e_call()  # warm
         for _ in range(max(1, min(args.steps, 3))):
@@ -645,7 +657,7 @@ def bench_scene(args):
                 "note": "gathered bytes (2 x 16 B per sample) vs the measured gather throughput",
                 "fp32": fp32_roof}
     traffic = TRAFFIC_PER_VIEW.get(args.workload) if march == "plain" else None
-    cfg = workload_config(w, march, world, args.workload)
+    cfg = workload_config(w, march, world, args.workload, args.integration)
     if is_voxel:
         cfg["volume_path"] = args.volume_path
     line = {
@@ -671,7 +683,8 @@ def bench_scene(args):
         line["error_vs_fp64"] = err
         if cb is not None:
             line["cpu_baseline"] = cb
-    if rank == 0 and world == 1 and not args.no_compare and not is_voxel and march != "plain":
+    if (rank == 0 and world == 1 and not args.no_compare and not is_voxel and march != "plain"
+            and args.integration == "simple"):
         del out
         torch.cuda.empty_cache()
         line.update(compare_paths(X, torch, scene, w, value, stream, flush, args))

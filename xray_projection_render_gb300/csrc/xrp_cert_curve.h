@@ -162,7 +162,10 @@ XRP_HD float radius_curve(float w2, float wv, float r, float e, float vmax, floa
 // or better the second-order bound of the leaf's defining conditions
 // (entry: the latest arrival over the violated conditions; exit: the
 // earliest over all).
+XRP_HD float gyroid_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t);
+
 XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t) {
+    if (n.type == N_GYROID) return gyroid_dc(n, x, y, z, c, t);
     float m;
     const float rho = leaf_dm(n, x, y, z, m);
     t = curve_time(m, c);
@@ -254,7 +257,13 @@ XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c
     }
     default: break;
     }
-    if (n.type != N_GYROID) return rho;
+    return rho;
+}
+
+// The gyroid leaf: leaf_dm's decision and ball bound and the second-order
+// curve bound from one set of sines and cosines.
+XRP_HD float gyroid_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t) {
+    const float* f = n.f;
     const float is = f[3], ais = fabsf(is);
     float X = (x - f[0]) * is, Y = (y - f[1]) * is, Z = (z - f[2]) * is;
     float sx, cx, sy, cy, sz, cz;
@@ -262,6 +271,14 @@ XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c
     f_sincos(Y, &sy, &cy);
     f_sincos(Z, &sz, &cz);
     const float g = fmaf(sz, cx, fmaf(sy, cz, sx * cy));
+    // leaf_dm (N_GYROID): decision and ball bound
+    const float q = f[4] - fabsf(g);
+    const float m = fmaxf(fabsf(q) - f[F_BAND], 0.0f) / (2.4494898f * ais);
+    t = curve_time(m, c);
+    float rho;
+    if (q > f[F_BAND]) rho = f[F_RHO];
+    else if (q < -f[F_BAND]) rho = 0.0f;
+    else return xnan();
     const float gX = fmaf(cx, cy, -sz * sx), gY = fmaf(cy, cz, -sx * sy), gZ = fmaf(cz, cx, -sy * sz);
     const float g1 = is * fmaf(gZ, c.vz, fmaf(gY, c.vy, gX * c.vx));
     // error of g1 (trigonometry, velocity, position) and of g (position slack)

@@ -1696,8 +1696,9 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 // Certificate tracing of the hierarchical integrator (main.go:159-199):
 // coarse samples k0..k1 (right ends, spacing DS).  A coarse sample whose
 // zero-ness differs from its predecessor's is refined over its fine samples
-// exactly as march_hier does; the coarse samples a certificate covers share
-// the evaluated density, so none of them flips and each adds rho*DS.
+// as march_hier does, the fine samples themselves traced with certificates;
+// the coarse samples a certificate covers share the evaluated density, so
+// none of them flips and each adds rho*DS.
 // `unc(index, fine)` gives the value of an undecided coarse (fine = false,
 // index into s64) or fine (fine = true, index into f64) sample.  Returns
 // sum(w * rho) with w in {DS, DS/10}.
@@ -1707,6 +1708,8 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
     KahanF acc;
     const float step = L.ds32 * 1.00001f;
     const float istep = (1.0f / step) * 0.999999f;  // rounded down
+    const float stepf = L.dsf32 * 1.00001f;          // fine samples, likewise
+    const float istepf = (1.0f / stepf) * 0.999999f;
     RayDir u;
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     bool prev_zero = true;  // coarse samples before k0 are outside the support
@@ -1730,15 +1733,28 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
         }
         const bool zero = (rho == 0.0f);
         if (zero != prev_zero) {
+            // the refinement's fine samples are traced too: a certificate at
+            // fine sample q covers the following fine samples within its
+            // reach, so a boundary costs an evaluation or two on either side
+            // instead of all ten
             const int f0 = L.fstart[k], f1 = L.fstart[k + 1];
-            for (int q = f0; q < f1; q++) {
+            int q = f0;
+            while (q < f1) {
                 const float tf = L.ft32[q];
-                float rf = density32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tf, ray.pc[0]),
-                                                  fmaf(ray.d32[1], tf, ray.pc[1]),
-                                                  fmaf(ray.d32[2], tf, ray.pc[2]));
+                const float xf = fmaf(ray.d32[0], tf, ray.pc[0]);
+                const float yf = fmaf(ray.d32[1], tf, ray.pc[1]);
+                const float zf = fmaf(ray.d32[2], tf, ray.pc[2]);
+                float mf;
+                float rf;
+                if constexpr (RAY) rf = dens_ray32<DEPTH, DEFS>(S, xf, yf, zf, u, (float)(f1 - q) * stepf, mf);
+                else if constexpr (CURVE) rf = dens_curve32<DEPTH, DEFS>(S, xf, yf, zf, ray.d32, mf);
+                else rf = dens_margin32<DEPTH, DEFS>(S, xf, yf, zf, mf);
                 evals++;
+                int jf = 0;
                 if (isunc(rf)) rf = unc(q, true);
-                acc.add(rf * L.dsf32);
+                else jf = (int)fminf(floorf(mf * istepf), (float)(f1 - 1 - q));
+                acc.add(rf * L.dsf32 * (float)(jf + 1));
+                q += jf + 1;
             }
             acc.add(rho * L.dsf32);
         } else {
