@@ -164,7 +164,15 @@ XRP_HD float radius_curve(float w2, float wv, float r, float e, float vmax, floa
 // earliest over all).
 XRP_HD float gyroid_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t);
 
+// The leaf types a curve-bound kernel is compiled for (bit 1 << NodeType):
+// every leaf, or gyroids only (the tessellated gyroid scenes, whose kernel
+// then carries no other leaf's code and fits the instruction cache better).
+constexpr int kLeafAll = (1 << N_SPHERE) | (1 << N_BOX) | (1 << N_CYL) | (1 << N_PPD) | (1 << N_GYROID);
+constexpr int kLeafGyroid = 1 << N_GYROID;
+
+template <int LM = kLeafAll>
 XRP_HD float leaf_dc(const Node& n, float x, float y, float z, const CurveDir& c, float& t) {
+    if constexpr (LM == kLeafGyroid) return gyroid_dc(n, x, y, z, c, t);
     if (n.type == N_GYROID) return gyroid_dc(n, x, y, z, c, t);
     float m;
     const float rho = leaf_dm(n, x, y, z, m);
@@ -300,14 +308,14 @@ XRP_HD float gyroid_dc(const Node& n, float x, float y, float z, const CurveDir&
     return rho;
 }
 
-template <int D>
+template <int D, int LM = kLeafAll>
 XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z, const CurveDir& u, float& t);
 
 // item_dm's decisions; the container distances become curve bounds.
-template <int D>
+template <int D, int LM = kLeafAll>
 XRP_HD float item_dc(const SceneDev& S, int id, float x, float y, float z, const CurveDir& u, float& t) {
     const Node& n = S.nodes[id];
-    if (n.type <= N_GYROID) return leaf_dc(n, x, y, z, u, t);
+    if (n.type <= N_GYROID) return leaf_dc<LM>(n, x, y, z, u, t);
     if (n.type == N_TESS) {
         if constexpr (D > 0) {
             const float* f = n.f;
@@ -334,7 +342,7 @@ XRP_HD float item_dc(const SceneDev& S, int id, float x, float y, float z, const
             if (mu < -f[13]) { t = curve_time(fminf(fminf(mo, fc), -mu), u); return 0.0f; }
             if (!(mu > f[13])) { t = 0.0f; return xnan(); }
             float tk;
-            float r = coll_dc<D - 1>(S, S.nodes[n.a], fx, fy, fz, u, tk);
+            float r = coll_dc<D - 1, LM>(S, S.nodes[n.a], fx, fy, fz, u, tk);
             // the outer bounds, the fold's cell and the unit-cell bounds, face
             // by face along the curve (their distances alone bound it too)
             const float ub[6] = {f[7], f[8], f[9], f[10], f[11], f[12]};
@@ -361,7 +369,7 @@ XRP_HD float item_dc(const SceneDev& S, int id, float x, float y, float z, const
 
 // coll_dm's decisions; the candidates' bounds, capped by the list cell's
 // faces or clearance as curve bounds.
-template <int D>
+template <int D, int LM>
 XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z, const CurveDir& u, float& t) {
     const int32_t* kids = S.child + c.a;
     int cnt = c.b;
@@ -414,7 +422,7 @@ XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z
     for (int k = 0; k < cnt; k++) {
         int slot = list ? list[k] : k;
         float tk;
-        float r = item_dc<D>(S, kids[slot], x, y, z, u, tk);
+        float r = item_dc<D, LM>(S, kids[slot], x, y, z, u, tk);
         if (uniform && !unc && r > 0.0f) {
             t = tk;
             return r;
@@ -444,7 +452,7 @@ XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z
 
 // density32 at one point and the curve bound t (ray parameter units) of the
 // samples ahead that share its density; d: the world ray direction.
-template <int DEPTH, bool DEFS>
+template <int DEPTH, bool DEFS, int LM = kLeafAll>
 XRP_HD float dens_curve32(const SceneDev& S, float x, float y, float z, const float* d, float& t) {
     CurveDir u;
     u.vx = d[0]; u.vy = d[1]; u.vz = d[2];
@@ -454,9 +462,9 @@ XRP_HD float dens_curve32(const SceneDev& S, float x, float y, float z, const fl
     u.eps = S.m_slack;
     const Node& r = S.nodes[S.root];
     float rho;
-    if (r.type <= N_GYROID) rho = leaf_dc(r, x, y, z, u, t);
-    else if (r.type == N_COLL) rho = coll_dc<DEPTH>(S, r, x, y, z, u, t);
-    else rho = item_dc<DEPTH>(S, S.root, x, y, z, u, t);
+    if (r.type <= N_GYROID) rho = leaf_dc<LM>(r, x, y, z, u, t);
+    else if (r.type == N_COLL) rho = coll_dc<DEPTH, LM>(S, r, x, y, z, u, t);
+    else rho = item_dc<DEPTH, LM>(S, S.root, x, y, z, u, t);
     t = fmaxf(t, 0.0f) * 0.99999f;
     return rho;
 }

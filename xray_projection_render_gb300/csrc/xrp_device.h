@@ -1081,6 +1081,20 @@ XRP_HD double leaf_hyb(const SceneDev& S, int id, double x, double y, double z) 
 template <int D>
 XRP_HD double coll_hyb(const SceneDev& S, int id, double x, double y, double z);
 
+// floor(a / b) as the reference forms it (the floor of the correctly rounded
+// FP64 quotient), with ib32 = (float)(1 / b).  The FP32 quotient is within
+// 3 * 2^-24 of a / b relatively ((float)a, ib32 and the product each round
+// once), and the FP64 quotient within 2^-53, so when the FP32 value is more
+// than 8 * 2^-24 |q| from an integer both floors agree; only then is the
+// FP64 division (a long instruction sequence on GB300) skipped.
+XRP_HD double floor_div64(double a, double b, float ib32) {
+    const float qf = (float)a * ib32;
+    const float err = fmaf(fabsf(qf), 8.0f * 5.9604645e-8f, 1e-30f);
+    const float lo = floorf(qf - err), hi = floorf(qf + err);
+    if (lo == hi) return (double)lo;
+    return floor(ddiv(a, b));
+}
+
 template <int D>
 XRP_HD double item_hyb(const SceneDev& S, int id, double x, double y, double z) {
     const Node& n = S.nodes[id];
@@ -1091,12 +1105,13 @@ XRP_HD double item_hyb(const SceneDev& S, int id, double x, double y, double z) 
             const double* t = S.nodes64[id].d;
             if (x < t[0] || x > t[1] || y < t[2] || y > t[3] || z < t[4] || z > t[5]) return 0.0;
             const double* u = &t[6];
+            const float* f = n.f;  // f[17..19]: (float)(1 / cell size) per axis
             double dx = dsub(u[1], u[0]);
-            x = dsub(x, dmul(dx, floor(ddiv(dsub(x, u[0]), dx))));
+            x = dsub(x, dmul(dx, floor_div64(dsub(x, u[0]), dx, f[17])));
             double dy = dsub(u[3], u[2]);
-            y = dsub(y, dmul(dy, floor(ddiv(dsub(y, u[2]), dy))));
+            y = dsub(y, dmul(dy, floor_div64(dsub(y, u[2]), dy, f[18])));
             double dz = dsub(u[5], u[4]);
-            z = dsub(z, dmul(dz, floor(ddiv(dsub(z, u[4]), dz))));
+            z = dsub(z, dmul(dz, floor_div64(dsub(z, u[4]), dz, f[19])));
             if (x < u[0] || x > u[1] || y < u[2] || y > u[3] || z < u[4] || z > u[5]) return 0.0;
             return coll_hyb<D - 1>(S, n.a, x, y, z);
         }
@@ -1659,9 +1674,9 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
 // the certified segment.  `unc(k)` returns the value of a
 // sample FP32 cannot decide (its FP64 density, or 0 when the caller
 // re-evaluates it later).  Returns the Kahan-compensated sum of densities,
-// the same terms as march_simple.  With CURVE (smooth non-affine chains,
-// CPU build) m is the curve bound of dens_curve32.
-template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, class Unc>
+// the same terms as march_simple.  With CURVE (smooth non-affine chains)
+// m is the curve bound of dens_curve32, compiled for the leaf types LM.
+template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, class Unc>
 XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
                        unsigned& evals) {
     KahanF acc;
@@ -1678,7 +1693,7 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
         float m;
         float rho;
         if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
-        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS>(S, x, y, z, ray.d32, m);
+        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         if (isunc(rho)) {
@@ -1696,20 +1711,20 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 // Certificate tracing of the hierarchical integrator (main.go:159-199):
 // coarse samples k0..k1 (right ends, spacing DS).  A coarse sample whose
 // zero-ness differs from its predecessor's is refined over its fine samples
-// as march_hier does, the fine samples themselves traced with certificates;
-// the coarse samples a certificate covers share the evaluated density, so
-// none of them flips and each adds rho*DS.
+// exactly as march_hier does (tracing the fine samples with certificates
+// too, tried, cut the evaluations by a third but ran 12-15 % slower: a
+// certificate costs several plain evaluations); the coarse samples a
+// certificate covers share the evaluated density, so none of them flips and
+// each adds rho*DS.
 // `unc(index, fine)` gives the value of an undecided coarse (fine = false,
 // index into s64) or fine (fine = true, index into f64) sample.  Returns
 // sum(w * rho) with w in {DS, DS/10}.
-template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, class Unc>
+template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, class Unc>
 XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
                             unsigned& evals) {
     KahanF acc;
     const float step = L.ds32 * 1.00001f;
     const float istep = (1.0f / step) * 0.999999f;  // rounded down
-    const float stepf = L.dsf32 * 1.00001f;          // fine samples, likewise
-    const float istepf = (1.0f / stepf) * 0.999999f;
     RayDir u;
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     bool prev_zero = true;  // coarse samples before k0 are outside the support
@@ -1722,7 +1737,7 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
         float m;
         float rho;
         if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
-        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS>(S, x, y, z, ray.d32, m);
+        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         int jmp = 0;
@@ -1733,28 +1748,15 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
         }
         const bool zero = (rho == 0.0f);
         if (zero != prev_zero) {
-            // the refinement's fine samples are traced too: a certificate at
-            // fine sample q covers the following fine samples within its
-            // reach, so a boundary costs an evaluation or two on either side
-            // instead of all ten
             const int f0 = L.fstart[k], f1 = L.fstart[k + 1];
-            int q = f0;
-            while (q < f1) {
+            for (int q = f0; q < f1; q++) {
                 const float tf = L.ft32[q];
-                const float xf = fmaf(ray.d32[0], tf, ray.pc[0]);
-                const float yf = fmaf(ray.d32[1], tf, ray.pc[1]);
-                const float zf = fmaf(ray.d32[2], tf, ray.pc[2]);
-                float mf;
-                float rf;
-                if constexpr (RAY) rf = dens_ray32<DEPTH, DEFS>(S, xf, yf, zf, u, (float)(f1 - q) * stepf, mf);
-                else if constexpr (CURVE) rf = dens_curve32<DEPTH, DEFS>(S, xf, yf, zf, ray.d32, mf);
-                else rf = dens_margin32<DEPTH, DEFS>(S, xf, yf, zf, mf);
+                float rf = density32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tf, ray.pc[0]),
+                                                  fmaf(ray.d32[1], tf, ray.pc[1]),
+                                                  fmaf(ray.d32[2], tf, ray.pc[2]));
                 evals++;
-                int jf = 0;
                 if (isunc(rf)) rf = unc(q, true);
-                else jf = (int)fminf(floorf(mf * istepf), (float)(f1 - 1 - q));
-                acc.add(rf * L.dsf32 * (float)(jf + 1));
-                q += jf + 1;
+                acc.add(rf * L.dsf32);
             }
             acc.add(rho * L.dsf32);
         } else {

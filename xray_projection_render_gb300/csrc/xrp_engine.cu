@@ -517,6 +517,9 @@ void bind_tables(const HostPrepared& hp, const std::vector<ViewDev>& views, cons
     out.defs = !fs.defs.empty();
     out.tex = hp.volume_fast ? tex : 0;
     out.empty = hl.hdr.K <= 0;
+    out.leaves = 0;
+    for (const Node& n : fs.nodes)
+        if (n.type >= N_SPHERE && n.type <= N_GYROID) out.leaves |= 1 << n.type;
     if (hp.volume_fast) fill_voxparams(hp, vol0, vol64_0, out.tex, out.vq);
 }
 

@@ -50,6 +50,7 @@ struct Prepared {
     int depth = kMaxDepth;        // kernel specialisation of general scenes
     bool defs = true;
     bool empty = false;  // no sample lattice or no support: every pixel is exp(-ff)
+    int leaves = 0;      // leaf types of the scene, bit 1 << NodeType
 };
 
 // A proposal-march launch (see xrp_proposal.cuh); Q's scene-independent

@@ -438,7 +438,8 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // jumps straight to the next boundary instead of approaching it.  CURVE
 // (smooth non-affine chains): the certificate is the curve bound of
 // dens_curve32, the first parameter at which the curved path of the
-// deformed samples can reach a boundary.  CERT: 0 ball, 1 ray, 2 curve.
+// deformed samples can reach a boundary.  CERT: 0 ball, 1 ray, 2 curve,
+// 3 curve for scenes whose leaves are all gyroids (a smaller kernel).
 // Samples FP32 cannot decide go to the FP64 list like the other march modes.
 // Resident blocks per SM for depth < 3, measured: 4 (64 registers; lattice
 // with ray bounds 415 against 382 Mrays/s with 3 and 410 with 5, gyroid with
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 #define XRP_CURVE_MIN_BLOCKS 4
 #endif
 template <int DEPTH, bool DEFS, bool HIER, int CERT>
-__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT == 2 ? XRP_CURVE_MIN_BLOCKS : 4))
+__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_MIN_BLOCKS : 4))
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT == 2 ? XRP_CURVE_M
                 // a coarse sample's value decides refinement: FP64 in place;
                 // fine samples only add, so they go to the list (high bit)
                 const ViewDev& V = views[view0 + v];
-                sum = trace_sum_hier<DEPTH, DEFS, CERT == 1, CERT == 2>(
+                sum = trace_sum_hier<DEPTH, DEFS, CERT == 1, CERT >= 2, CERT == 3 ? kLeafGyroid : kLeafAll>(
                     Sl, L, ray, k0, k1,
                     [&](int q, bool fine) {
                         if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT == 2 ? XRP_CURVE_M
                     },
                     evals);
             } else {
-                sum = trace_sum<DEPTH, DEFS, CERT == 1, CERT == 2>(
+                sum = trace_sum<DEPTH, DEFS, CERT == 1, CERT >= 2, CERT == 3 ? kLeafGyroid : kLeafAll>(
                     Sl, L, ray, k0, k1,
                     [&](int k) {
                         unsigned slot = atomicAdd(Q.fb_count, 1u);

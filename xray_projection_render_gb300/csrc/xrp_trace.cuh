@@ -24,16 +24,16 @@ cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams&
     return cudaGetLastError();
 }
 
-// CERT 2 (curve bounds) serves deformed scenes only: DEFS is always on.
+// CERT 2 and 3 (curve bounds) serve deformed scenes only: DEFS is always on.
 template <int CERT>
 cudaError_t launch_trace_mode(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                               cudaStream_t st) {
-    if (CERT == 2 || pr.defs) {
+    if (CERT >= 2 || pr.defs) {
         if (pr.depth == 0) return trace_r<0, true, CERT>(pr, view0, nviews, Q, dout, st);
         if (pr.depth == 1) return trace_r<1, true, CERT>(pr, view0, nviews, Q, dout, st);
         return trace_r<3, true, CERT>(pr, view0, nviews, Q, dout, st);
     }
-    if constexpr (CERT != 2) {
+    if constexpr (CERT < 2) {
         if (pr.depth == 0) return trace_r<0, false, CERT>(pr, view0, nviews, Q, dout, st);
         if (pr.depth == 1) return trace_r<1, false, CERT>(pr, view0, nviews, Q, dout, st);
         return trace_r<3, false, CERT>(pr, view0, nviews, Q, dout, st);
