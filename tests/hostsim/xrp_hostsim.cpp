@@ -34,7 +34,7 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
             view_from_camera(p, p + 3, p[19], views[c]);
             fov_max = std::max(fov_max, std::fabs(p[19]));
         }
-        HostPrepared hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max);
+        HostPrepared hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max, trace != 0);
         for (size_t k = 0; k < hp.vols.size(); k++) {
             hp.vols[k].data = hs.vols[k].data.data();
             hp.vols[k].data64 = hs.vols[k].data64.empty() ? nullptr : hs.vols[k].data64.data();

@@ -1666,6 +1666,32 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
     return acc.s;
 }
 
+// One step of certificate tracing at lattice sample k (k <= k1): evaluates
+// the density and its certificate there, adds the covered samples' terms to
+// `acc` and advances k past them.  u: the ray's object-space direction (RAY).
+template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, class Unc>
+XRP_HD void trace_step(const SceneDev& S, const Lattice& L, const Ray& ray, const RayDir& u, int& k, int k1,
+                       float step, float istep, Unc&& unc, KahanF& acc, unsigned& evals) {
+    const float tk = lattice_t(L, k);
+    const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
+    const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
+    const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
+    float m;
+    float rho;
+    if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
+    else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
+    else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+    evals++;
+    if (isunc(rho)) {
+        acc.add(unc(k));
+        k++;
+        return;
+    }
+    const int jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
+    acc.add(rho * (float)(jmp + 1));
+    k += jmp + 1;
+}
+
 // Certificate tracing of one ray over lattice samples [k0, k1]: at sample k
 // the density and the certificate radius m (dens_margin32); the samples
 // k..k+j with j*ds <= m lie inside the ball around sample k, so they share
@@ -1685,26 +1711,7 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
     RayDir u;
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     int k = k0;
-    while (k <= k1) {
-        const float tk = lattice_t(L, k);
-        const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
-        const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
-        const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
-        float m;
-        float rho;
-        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
-        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
-        else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
-        evals++;
-        if (isunc(rho)) {
-            acc.add(unc(k));
-            k++;
-            continue;
-        }
-        const int jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
-        acc.add(rho * (float)(jmp + 1));
-        k += jmp + 1;
-    }
+    while (k <= k1) trace_step<DEPTH, DEFS, RAY, CURVE, LM>(S, L, ray, u, k, k1, step, istep, unc, acc, evals);
     return acc.s - acc.c;
 }
 

@@ -527,10 +527,10 @@ void bind_tables(const HostPrepared& hp, const std::vector<ViewDev>& views, cons
 int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol_dev,
             const std::vector<const double*>& vol64_dev, const std::vector<ViewDev>& views,
             int res, int integration, double ds, double R, double ff, double dm, double fov_max,
-            cudaStream_t st, PoolBuf& tab, Prepared& out, cudaTextureObject_t tex) {
+            cudaStream_t st, PoolBuf& tab, Prepared& out, cudaTextureObject_t tex, bool tracing = false) {
     HostPrepared hp;
     try {
-        hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max);
+        hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max, tracing);
     } catch (const std::exception& ex) {
         return fail(2, "%s", ex.what());
     }
@@ -599,7 +599,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     Prepared pr;
     int rc = prepare(E, hs, vdev, v64, views, res, o.integration, o.ds, o.R, o.flat_field,
                      o.density_multiplier, fov_max, st, tab, pr,
-                     (o.flags & XRP_FLAG_VOLUME_LOADS) ? 0 : tex);
+                     (o.flags & XRP_FLAG_VOLUME_LOADS) ? 0 : tex, pl && pl->Q.trace);
     if (rc) return rc;
     unsigned long long* stats = nullptr;
     cudaError_t e;
@@ -1077,7 +1077,8 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
                 vws[q] = views_from(it.views, it.num_views, &fov_max);
                 try {
                     hps[q] = prepare_host(it.scene->hs, it.resolution, oo.integration, oo.ds, oo.R,
-                                          oo.flat_field, oo.density_multiplier, fov_max);
+                                          oo.flat_field, oo.density_multiplier, fov_max,
+                                          (oo.flags & XRP_FLAG_TRACE) != 0);
                 } catch (const std::exception& ex) {
                     errs[q] = ex.what();
                     if (errs[q].empty()) errs[q] = "flattening failed";

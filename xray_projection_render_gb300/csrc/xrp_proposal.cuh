@@ -443,7 +443,11 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // Samples FP32 cannot decide go to the FP64 list like the other march modes.
 // Resident blocks per SM for depth < 3, measured: 4 (64 registers; lattice
 // with ray bounds 415 against 382 Mrays/s with 3 and 410 with 5, gyroid with
-// balls 1462 against 1406 with 3).
+// balls 1462 against 1406 with 3).  Tried and dropped: four pixels per
+// thread in one flattened loop (a lane starts its next ray when one ends, to
+// recover the ~13 % of lane slots lost to warps' longest rays): the lanes'
+// rays drift apart and evaluations diverge, lattice 464 -> 411 Mrays/s,
+// gyroid 2041 -> 1396.
 // Resident blocks per SM of the tracing kernel with curve certificates
 // (depth < 3): its Jacobian-vector products and quadratic bounds need more
 // registers than the ball and ray variants (at 64 registers ptxas spills
@@ -456,6 +460,8 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_M
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
+    constexpr bool RAY = CERT == 1, CURVE = CERT >= 2;
+    constexpr int LM = CERT == 3 ? kLeafGyroid : kLeafAll;
     const int res = P.res;
     const int tpr = (res + 15) >> 4;
     const int tpv = tpr * tpr;
@@ -492,7 +498,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_M
                 // a coarse sample's value decides refinement: FP64 in place;
                 // fine samples only add, so they go to the list (high bit)
                 const ViewDev& V = views[view0 + v];
-                sum = trace_sum_hier<DEPTH, DEFS, CERT == 1, CERT >= 2, CERT == 3 ? kLeafGyroid : kLeafAll>(
+                sum = trace_sum_hier<DEPTH, DEFS, RAY, CURVE, LM>(
                     Sl, L, ray, k0, k1,
                     [&](int q, bool fine) {
                         if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
@@ -502,7 +508,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_M
                     },
                     evals);
             } else {
-                sum = trace_sum<DEPTH, DEFS, CERT == 1, CERT >= 2, CERT == 3 ? kLeafGyroid : kLeafAll>(
+                sum = trace_sum<DEPTH, DEFS, RAY, CURVE, LM>(
                     Sl, L, ray, k0, k1,
                     [&](int k) {
                         unsigned slot = atomicAdd(Q.fb_count, 1u);

@@ -91,7 +91,9 @@ struct FlatScene {
     double curve_acc = 0.0;       // bound on |d^2 q/ds^2| of the deformed point along a unit ray
 };
 
-FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical);
+// `tracing`: the scene is rendered by certificate tracing (coarser candidate
+// lists for uniform collections, see Flattener::coll).
+FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical, bool tracing = false);
 
 // mathgl restatement for the host-side camera (main.go:226-239).
 void camera_from_angles(double az_deg, double polar_deg, double R, double eye[3], double m[16]);
@@ -124,6 +126,6 @@ struct HostPrepared {
     bool volume_fast = false;
 };
 HostPrepared prepare_host(const HostScene& hs, int res, int integration, double ds, double R,
-                          double flat_field, double density_multiplier, double fov_max);
+                          double flat_field, double density_multiplier, double fov_max, bool tracing = false);
 
 }  // namespace xrp
