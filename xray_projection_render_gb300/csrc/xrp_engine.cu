@@ -1474,6 +1474,9 @@ int xrp_mlp_grad(const float* params, const uint16_t* X, const float* y, int row
     if (logits && (e = cudaMemcpyAsync(logits, dlog.p, (size_t)rows * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(7, "logit read", e);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(7, "training kernel", e);
+    unsigned tc_err = 0;
+    if ((e = mlp_tc_error(&tc_err)) != cudaSuccess) return cuda_fail(7, "training status", e);
+    if (tc_err) return fail(7, "a tensor-core training step timed out waiting for its products");
     return 0;
 }
 
@@ -1577,6 +1580,9 @@ int xrp_proposal_train(xrp_scene* s, const xrp_camera* views, int nviews, const 
         if ((e = cudaMemcpyAsync(hl.data(), lossb.p, (size_t)steps * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
             (e = cudaStreamSynchronize(st)) != cudaSuccess)
             return cuda_fail(7, "training", e);
+        unsigned tc_err = 0;
+        if ((e = mlp_tc_error(&tc_err)) != cudaSuccess) return cuda_fail(7, "training status", e);
+        if (tc_err) return fail(7, "a tensor-core training step timed out waiting for its products");
         int tail = std::max(1, steps / 10);
         double sl = 0;
         for (int k = steps - tail; k < steps; k++) sl += hl[k];

@@ -134,6 +134,9 @@ cudaError_t mlp_adam_launch(cudaStream_t st, float* params, float* grad, float* 
                             float lr, float b1, float b2, float eps, float c1, float c2);
 cudaError_t mlp_logits_launch(cudaStream_t st, const float* params, const __nv_bfloat16* X, int rows,
                               float* logits);
+// Whether a tensor-core training step gave up waiting for its products since
+// the last call (synchronous; clears the flag).
+cudaError_t mlp_tc_error(unsigned* out);
 
 constexpr int kMaxDevices = 64;  // per-device launch caches
 
