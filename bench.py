@@ -106,6 +106,9 @@ def parse():
                    help="skip the plain / proposal comparisons and the gyroid record")
     p.add_argument("--volume-path", default="gather", choices=["gather", "loads"],
                    help="voxel reads: texture gathers (default) or per-tap loads")
+    p.add_argument("--plain-fp64", default="auto", choices=["auto", "list", "inplace"],
+                   help="plain integrator over analytic scenes: undecided samples to one FP64 list "
+                        "pass, or re-evaluated inside the march (auto: the list from 2^22 rays a call)")
     return p.parse_args()
 
 
@@ -435,23 +438,30 @@ def _event_time(torch, step, steps, stream, flush):
 
 
 def scene_step(X, scene, w, angles, march, out, stream, prop=None, volume_path="gather",
-               integration="simple"):
+               integration="simple", plain_fp64="auto"):
     """One render of `angles` by `march` into the device buffer `out`."""
     kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, integration=integration)
     if march == "plain":
-        return lambda: X.render(scene, angles, out=out, stream=stream, volume_path=volume_path, **kw)
+        return lambda: X.render(scene, angles, out=out, stream=stream, volume_path=volume_path,
+                                plain_fp64=plain_fp64, **kw)
     trace = {"trace": True, "ball": "ball"}.get(march, False)
     return lambda: X.render_proposal(scene, prop, angles, segment=64, refine=march == "proposal",
                                      trace=trace, out=out, stream=stream, **kw)
 
 
-def launches_per_step(march, rays, voxel):
-    """Kernels one step launches: one render launch for the plain
-    integrator; per launch group of at most 8 M rays the march, its FP64
-    pass and the exp pass for the other marches."""
-    if march == "plain" or voxel:
+def launches_per_step(march, rays, voxel, integration="simple", plain_fp64="auto"):
+    """Kernels one step launches: one render launch for a voxel-grid root
+    and for the plain integrator re-evaluating in place (below 2^22 rays a
+    call unless told otherwise); otherwise, per launch group of at most 8 M
+    rays (2 M for the hierarchical integrator), the march, its FP64 pass and
+    the exp pass, and for the plain integrator the re-march of rays that
+    found the FP64 list full."""
+    if voxel:
         return 1
-    return 3 * -(-rays // (1 << 23))
+    if march == "plain" and (plain_fp64 == "inplace" or (plain_fp64 == "auto" and rays < (1 << 22))):
+        return 1
+    group = 1 << (21 if integration == "hierarchical" else 23)
+    return (4 if march == "plain" else 3) * -(-rays // group)
 
 
 def time_path(X, torch, scene, w, angles, march, stream, flush, steps, prop=None, err_rays=4000):
@@ -550,7 +560,7 @@ def bench_scene(args):
     if march == "proposal":
         prop = X.Proposal(scene, my_angles, resolution=res, ds=w.ds, R=w.R, fov=w.fov, segment=64)
     step = scene_step(X, scene, w, my_angles, march, out, stream, prop, args.volume_path,
-                      args.integration)
+                      args.integration, args.plain_fp64)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -660,6 +670,8 @@ def bench_scene(args):
     cfg = workload_config(w, march, world, args.workload, args.integration)
     if is_voxel:
         cfg["volume_path"] = args.volume_path
+    elif march == "plain":
+        cfg["plain_fp64"] = args.plain_fp64
     line = {
         "metric": (VOXEL_METRIC if args.workload == "voxel" else
                    HEADLINE_METRIC if args.workload == "lattice" else f"Mrays/s on 1 GB300 ({w.name})"),
@@ -669,7 +681,8 @@ def bench_scene(args):
         "data": "synthetic (seeded)", "config": cfg, "path": MARCH_PATHS[march],
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
-        "gpu_launches": args.steps * launches_per_step(march, n_my * img, is_voxel),
+        "gpu_launches": args.steps * launches_per_step(march, n_my * img, is_voxel, args.integration,
+                                                       args.plain_fp64),
         "roofline": dict(roof, **{
             "traffic": traffic * n_my if traffic else None,
             "traffic_note": ("constant: DRAM bytes per view from an ncu capture of the same kernel "

@@ -116,7 +116,10 @@ enum {
     XRP_FLAG_VOLUME_LOADS = 2, /* voxel-grid roots: per-tap loads instead of texture gathers */
     XRP_FLAG_NO_REFINE = 4,    /* proposal march: no certificate refinement of segments */
     XRP_FLAG_TRACE = 8,        /* per-ray certificate tracing (proposal march without network, batches) */
-    XRP_FLAG_BALL = 16         /* tracing: ball certificates only, even for affine deformation chains */
+    XRP_FLAG_BALL = 16,        /* tracing: ball certificates only, even for affine deformation chains */
+    XRP_FLAG_PLAIN_INPLACE = 32, /* plain integrator, general scene: FP64 re-evaluation inside the march */
+    XRP_FLAG_PLAIN_LIST = 64     /* plain integrator, general scene: the FP64 list pass after the march;
+                                    with neither flag the list serves calls of at least 2^22 rays */
 };
 
 /* Per-call options: the globals and flags of the reference CLI
@@ -177,7 +180,12 @@ XRP_API int xrp_render(xrp_scene* scene, const xrp_camera* views, int num_views,
  * As xrp_render, but `out_device` is device memory and the work is queued on
  * `stream` (a cudaStream_t, NULL for the legacy default stream); returns
  * after queuing.  The scene and the cameras must not change until the stream
- * has passed this call.
+ * has passed this call.  Over a general scene (anything but a lone voxel
+ * grid) a call of at least 2^22 rays leaves the samples FP32 cannot decide to
+ * one FP64 pass over a list after the march (a ray with a sample that finds
+ * the list full is marched again); smaller calls re-evaluate them inside the
+ * march, in one launch.  XRP_FLAG_PLAIN_LIST / XRP_FLAG_PLAIN_INPLACE pick
+ * one way for every call.
  */
 XRP_API int xrp_render_device(xrp_scene* scene, const xrp_camera* views, int num_views,
                       const xrp_render_opts* opts, float* out_device, void* stream);

@@ -46,8 +46,15 @@ def test_batch_equals_single_renders(X, integration, autotune):
             if autotune:
                 assert info["tune_candidates"] >= 4
             for k, (s, w) in enumerate(zip(scenes, ws)):
-                single = X.render(s, w.angles, resolution=w.res, ds=ds, integration=integration)
+                # the batch kernel re-evaluates undecided samples in FP64
+                # inside the march, like plain_fp64="inplace": bit for bit
+                single = X.render(s, w.angles, resolution=w.res, ds=ds, integration=integration,
+                                  plain_fp64="inplace")
                 assert np.array_equal(b.item(k), single), w.name
+                # the FP64 list adds those samples after the march
+                listed = X.render(s, w.angles, resolution=w.res, ds=ds, integration=integration,
+                                  plain_fp64="list")
+                np.testing.assert_allclose(b.item(k), listed, rtol=2e-6, atol=1e-7, err_msg=w.name)
     finally:
         for s in scenes:
             s.close()

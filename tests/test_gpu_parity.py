@@ -78,6 +78,59 @@ def test_gyroid_sigmoid_reduced(X, integration):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+@pytest.mark.parametrize("name", ["deformed_lattice", "gyroid_sigmoid", "cube_minus_sphere_cylinder"])
+def test_plain_fp64_list_matches_inplace(X, name, integration):
+    """The plain integrator's two FP64 passes: the list after the march
+    (default) and the re-evaluation inside it.  The FP32 decisions are the
+    same, so they count the same samples; the images agree to FP32 rounding
+    (the list's values are added to the optical depth after the march), on
+    the host path and the device path alike, and match the oracle."""
+    import torch
+    w = getattr(W(), name)()
+    w = W().reduced(w, 96, 3)
+    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, integration=integration)
+    with X.Scene(w.obj, w.deformation) as s:
+        a, na, fa = X.render(s, w.angles, stats=True, plain_fp64="list", **kw)
+        b, nb, fb = X.render(s, w.angles, stats=True, plain_fp64="inplace", **kw)
+        auto = X.render(s, w.angles, **kw)  # a small call: in place
+        dev = torch.empty((len(w.angles), w.res, w.res), dtype=torch.float32, device="cuda")
+        X.render(s, w.angles, out=dev, plain_fp64="list", **kw)
+        torch.cuda.synchronize()
+        d = dev.cpu().numpy()
+    assert (na, fa) == (nb, fb)
+    assert np.array_equal(auto, b)
+    if name == "deformed_lattice":
+        assert fa > 0
+    np.testing.assert_allclose(a, b, rtol=2e-6, atol=1e-7)
+    np.testing.assert_allclose(d, a, rtol=2e-6, atol=1e-7)
+    ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                   integration=integration)
+    _compare(a, ref)
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_fp64_list_overflow_paths(X, integration, monkeypatch):
+    """A 16-entry FP64 list (the XRP_FALLBACK_LIST test hook) overflows on
+    the lattice.  The plain mode marches the rays that lost a sample again
+    (FP64 inside the march): the result equals the in-place re-evaluation to
+    FP32 rounding.  Tracing renders the call again with the plain kernel and
+    reports the overflow.  Both match the oracle."""
+    w = W().reduced(W().deformed_lattice(), 96, 2)
+    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, integration=integration)
+    with X.Scene(w.obj, w.deformation) as s:
+        inplace = X.render(s, w.angles, plain_fp64="inplace", **kw)
+        monkeypatch.setenv("XRP_FALLBACK_LIST", "16")
+        listed, ns, nf = X.render(s, w.angles, stats=True, plain_fp64="list", **kw)
+        traced, st = X.render_proposal(s, None, w.angles, trace=True, stats=True, **kw)
+    assert nf > 16 and st["fp64_list_overflow"] == 1
+    np.testing.assert_allclose(listed, inplace, rtol=2e-6, atol=1e-7)
+    ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                   integration=integration)
+    _compare(listed, ref)
+    _compare(traced, ref)
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 @pytest.mark.parametrize("path", ["gather", "loads"])
 def test_voxel_scene_reduced(X, integration, path):
     w = W().reduced(W().voxel_blobs(n=64), 128, 6)

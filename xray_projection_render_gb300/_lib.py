@@ -68,6 +68,8 @@ XRP_FLAG_VOLUME_LOADS = 2
 XRP_FLAG_NO_REFINE = 4
 XRP_FLAG_TRACE = 8
 XRP_FLAG_BALL = 16
+XRP_FLAG_PLAIN_INPLACE = 32
+XRP_FLAG_PLAIN_LIST = 64
 
 # Every symbol include/xrp.h declares, with (restype, argtypes).
 SIGNATURES = {

@@ -73,6 +73,7 @@ def _run(cmd, verbose):
 CUDA_UNITS = ["xrp_engine.cu", "xrp_kern_scene.cu", "xrp_kern_batch.cu", "xrp_kern_batch_ball.cu",
               "xrp_kern_batch_ray.cu", "xrp_kern_batch_curve.cu", "xrp_kern_export.cu",
               "xrp_kern_trace.cu", "xrp_kern_trace_ray.cu", "xrp_kern_trace_curve.cu",
+              "xrp_kern_trace_plain.cu",
               "xrp_kern_prop.cu", "xrp_kern_prop_net.cu", "xrp_kern_train.cu"]
 
 

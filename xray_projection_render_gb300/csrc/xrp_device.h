@@ -1638,30 +1638,41 @@ XRP_HD float march_hier(const Lattice& L, const float* lo, const float* hi, cons
     KahanF acc;
     if (!sample_range(L, t0, t1, L.K, k0, k1)) return 0.0f;
     bool prev_zero = true;  // coarse samples before k0 are outside the support
-    for (int k = k0; k <= k1; k++) {
-        float rho = smp.f32(lattice_t(L, k));
+    // One sample per iteration: a coarse sample that flips queues its
+    // interval's fine samples m..me-1 (rho_c: its density), evaluated by the
+    // next iterations, so lanes that flip at different coarse indices do not
+    // serialise the warp on a nested loop.  Same terms, same order.
+    int k = k0, m = 0, me = 0;
+    float rho_c = 0.0f;
+    while (k <= k1) {
+        const bool fine = m < me;
+        float rho = smp.f32(fine ? L.ft32[m] : lattice_t(L, k));
         if (isunc(rho)) {
-            rho = (float)smp.f64(L.s64[k]);
+            rho = (float)smp.f64(fine ? L.f64[m] : L.s64[k]);
             st.fallbacks++;
         }
         st.samples++;
-        bool zero = (rho == 0.0f);
+        if (fine) {
+            acc.add(rho * L.dsf32);
+            if (++m < me) continue;
+            acc.add(rho_c * L.dsf32);
+            k++;
+            continue;
+        }
+        const bool zero = (rho == 0.0f);
         if (zero != prev_zero) {
-            int f0 = L.fstart[k], f1 = L.fstart[k + 1];
-            for (int m = f0; m < f1; m++) {
-                float rf = smp.f32(L.ft32[m]);
-                if (isunc(rf)) {
-                    rf = (float)smp.f64(L.f64[m]);
-                    st.fallbacks++;
-                }
-                acc.add(rf * L.dsf32);
+            prev_zero = zero;
+            m = L.fstart[k];
+            me = L.fstart[k + 1];
+            if (m < me) {
+                rho_c = rho;
+                continue;
             }
-            st.samples += (uint32_t)(f1 - f0);
             acc.add(rho * L.dsf32);
         } else {
             acc.add(rho * L.ds32);
         }
-        prev_zero = zero;
+        k++;
     }
     return acc.s;
 }
@@ -1715,6 +1726,25 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
     return acc.s - acc.c;
 }
 
+// The plain integrator's sum over lattice samples [k0, k1] (main.go:144-154)
+// without certificates: every sample is evaluated in FP32; `unc(k)` gives
+// the value of a sample FP32 cannot decide (0 when it goes to the FP64
+// list).  The loop holds no FP64 state, so it stays in registers.
+template <int DEPTH, bool DEFS, class Unc>
+XRP_HD float plain_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
+                       unsigned& evals) {
+    KahanF acc;
+    for (int k = k0; k <= k1; k++) {
+        const float tk = lattice_t(L, k);
+        float rho = density32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tk, ray.pc[0]), fmaf(ray.d32[1], tk, ray.pc[1]),
+                                           fmaf(ray.d32[2], tk, ray.pc[2]));
+        if (isunc(rho)) rho = unc(k);
+        acc.add(rho);
+    }
+    evals += (unsigned)(k1 - k0 + 1);
+    return acc.s - acc.c;
+}
+
 // Certificate tracing of the hierarchical integrator (main.go:159-199):
 // coarse samples k0..k1 (right ends, spacing DS).  A coarse sample whose
 // zero-ness differs from its predecessor's is refined over its fine samples
@@ -1725,8 +1755,9 @@ XRP_HD float trace_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 // each adds rho*DS.
 // `unc(index, fine)` gives the value of an undecided coarse (fine = false,
 // index into s64) or fine (fine = true, index into f64) sample.  Returns
-// sum(w * rho) with w in {DS, DS/10}.
-template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, class Unc>
+// sum(w * rho) with w in {DS, DS/10}.  PLAIN: no certificates (every coarse
+// sample evaluated), the plain hierarchical integrator.
+template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, bool PLAIN = false, class Unc>
 XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
                             unsigned& evals) {
     KahanF acc;
@@ -1736,41 +1767,59 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     bool prev_zero = true;  // coarse samples before k0 are outside the support
     int k = k0;
+    // One sample per iteration, coarse or fine: a coarse sample that flips
+    // queues its interval's fine samples q..qe-1, which the next iterations
+    // evaluate before the march moves on (rho_c, jmp_c: the coarse sample's
+    // density and jump).  Nested, the fine loop ran once per lane that
+    // flipped at a given coarse index, serialising the warp.
+    int q = 0, qe = 0;
+    float rho_c = 0.0f;
+    int jmp_c = 0;
     while (k <= k1) {
-        const float tk = lattice_t(L, k);
+        const bool fine = q < qe;
+        const float tk = fine ? L.ft32[q] : lattice_t(L, k);
         const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
         const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
         const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
-        float m;
+        float m = 0.0f;
         float rho;
-        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
+        if constexpr (PLAIN) rho = density32<DEPTH, DEFS>(S, x, y, z);
+        else if (fine) rho = density32<DEPTH, DEFS>(S, x, y, z);
+        else if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
         else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
+        if (fine) {
+            if (isunc(rho)) rho = unc(q, true);
+            acc.add(rho * L.dsf32);
+            if (++q < qe) continue;
+            // interval refined: the coarse sample's own term and its jump
+            acc.add(rho_c * L.dsf32);
+            if (jmp_c > 0) acc.add(rho_c * L.ds32 * (float)jmp_c);
+            k += jmp_c + 1;
+            continue;
+        }
         int jmp = 0;
         if (isunc(rho)) {
             rho = unc(k, false);
-        } else {
+        } else if constexpr (!PLAIN) {
             jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
         }
         const bool zero = (rho == 0.0f);
         if (zero != prev_zero) {
-            const int f0 = L.fstart[k], f1 = L.fstart[k + 1];
-            for (int q = f0; q < f1; q++) {
-                const float tf = L.ft32[q];
-                float rf = density32<DEPTH, DEFS>(S, fmaf(ray.d32[0], tf, ray.pc[0]),
-                                                  fmaf(ray.d32[1], tf, ray.pc[1]),
-                                                  fmaf(ray.d32[2], tf, ray.pc[2]));
-                evals++;
-                if (isunc(rf)) rf = unc(q, true);
-                acc.add(rf * L.dsf32);
+            prev_zero = zero;
+            q = L.fstart[k];
+            qe = L.fstart[k + 1];
+            if (q < qe) {
+                rho_c = rho;
+                jmp_c = jmp;
+                continue;
             }
             acc.add(rho * L.dsf32);
         } else {
             acc.add(rho * L.ds32);
         }
         if (jmp > 0) acc.add(rho * L.ds32 * (float)jmp);
-        prev_zero = zero;
         k += jmp + 1;
     }
     return acc.s - acc.c;
@@ -1805,15 +1854,31 @@ XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams
     return expf(-T);
 }
 
+// Optical depth T = flat_field + multiplier * (sum) of pixel (i, j) of a
+// general scene (main.go:146, 153, 175, 198), FP64 for undecided samples in
+// the march.
+template <bool HIER, int DEPTH, bool DEFS>
+XRP_HD float depth_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P, const ViewDev& V, int i,
+                         int j, RayStats& st) {
+    Ray r;
+    setup_ray_march(V, P, L, i, j, r);
+    PixelRef px{&V, P.xs, i, j};
+    SceneSampler<DEPTH, DEFS> smp{S, r, px};
+    float acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st) : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+    float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+    return fmaf(w, acc, P.flat_field);
+}
+
 // One pixel: optical depth T = flat_field + multiplier * (sum), as
 // transmittance exp(-T) (main.go:146, 153, 175, 198).
 template <bool HIER, bool VOLUME, int DEPTH = kMaxDepth, bool DEFS = true>
 XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P,
                           const ViewDev& V, int i, int j, RayStats& st) {
-    Ray r;
-    float acc;
-    PixelRef px{&V, P.xs, i, j};
-    if constexpr (VOLUME) {
+    if constexpr (!VOLUME) {
+        return expf(-depth_pixel<HIER, DEPTH, DEFS>(S, L, P, V, i, j, st));
+    } else {
+        Ray r;
+        PixelRef px{&V, P.xs, i, j};
         const Volume& vol = S.vols[0];
         VolRay vr;
         {
@@ -1825,17 +1890,12 @@ XRP_HD float render_pixel(const SceneDev& S, const Lattice& L, const RenderParam
         VolumeSampler smp{S, vol, vr, px,
                           {1.0f / vol.scale[0], 1.0f / vol.scale[1], 1.0f / vol.scale[2]},
                           S.nodes[S.root].f[0]};
-        acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
-                   : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st, 4.0f * vol.band_w + 2e-4f);
-    } else {
-        setup_ray_march(V, P, L, i, j, r);
-        SceneSampler<DEPTH, DEFS> smp{S, r, px};
-        acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
-                   : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st);
+        float acc = HIER ? march_hier(L, S.sup_lo, S.sup_hi, r, smp, st)
+                         : march_simple(L, S.sup_lo, S.sup_hi, r, smp, st, 4.0f * vol.band_w + 2e-4f);
+        float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
+        float T = fmaf(w, acc, P.flat_field);
+        return expf(-T);
     }
-    float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
-    float T = fmaf(w, acc, P.flat_field);
-    return expf(-T);
 }
 
 }  // namespace xrp

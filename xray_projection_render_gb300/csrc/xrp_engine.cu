@@ -556,6 +556,28 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
 // launch
 // ---------------------------------------------------------------------------
 
+// The list of samples a march leaves to FP64 (k_prop_fallback), reused by
+// every launch of a call: four (ray, sample) entries per ray of a launch of
+// pl.max_rays rays, with its counter and overflow flag.
+// XRP_FALLBACK_LIST (a test hook) sets a smaller capacity, which exercises
+// the overflow paths.
+static int alloc_fallback_list(Engine* E, PropLaunch& pl, PoolBuf& fb, PoolBuf& fbc, cudaStream_t st) {
+    unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, (1LL << 23) * 4);
+    if (const char* c = getenv("XRP_FALLBACK_LIST"))
+        if (*c) fb_cap = (unsigned)std::min<long long>(fb_cap, std::max(1LL, atoll(c)));
+    cudaError_t e;
+    if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
+        (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)
+        return cuda_fail(3, "fallback list", e);
+    if ((e = cudaMemsetAsync(fbc.p, 0, 2 * sizeof(unsigned), st)) != cudaSuccess)
+        return cuda_fail(7, "fallback list reset", e);
+    pl.Q.fb = (uint2*)fb.p;
+    pl.Q.fb_count = (unsigned*)fbc.p;
+    pl.Q.fb_overflow = (unsigned*)fbc.p + 1;
+    pl.Q.fb_cap = fb_cap;
+    return 0;
+}
+
 static cudaError_t launch_prop(const Prepared& pr, int view0, int nviews, const PropLaunch& pl,
                                float* dout, cudaStream_t st) {
     return pl.train ? launch_prop_train(pr, view0, nviews, pl.Q, st)
@@ -588,22 +610,61 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
 // Renders `views` into `out` (device or host memory).  Host output goes
 // through two device chunk buffers so the copy of chunk c overlaps the
 // rendering of chunk c+1.
+//
+// plain_list: the plain integrator over a general scene (not the voxel-grid
+// fast path) marches in the tracing kernel's plain mode, which leaves the
+// samples FP32 cannot decide on a list for one FP64 pass instead of
+// re-evaluating them inside the march (k_render: the FP64 state held across
+// the loop costs registers and spills, and a warp waits on each lane's FP64
+// evaluation).  Samples that find the list full are evaluated in place, so
+// the call needs no overflow check and stays asynchronous.
 static int render_views(Engine* E, const HostScene& hs, const std::vector<const float*>& vdev,
                         const std::vector<const double*>& v64, const std::vector<ViewDev>& views,
                         const xrp_render_opts& o, double fov_max, float* out, bool out_host,
                         cudaStream_t st, cudaStream_t st_copy, bool want_stats,
-                        cudaTextureObject_t tex, const PropLaunch* pl = nullptr) {
+                        cudaTextureObject_t tex, const PropLaunch* pl = nullptr, bool plain_list = false) {
     const int res = o.resolution;
     const int nviews = (int)views.size();
     PoolBuf tab;
     Prepared pr;
     int rc = prepare(E, hs, vdev, v64, views, res, o.integration, o.ds, o.R, o.flat_field,
                      o.density_multiplier, fov_max, st, tab, pr,
-                     (o.flags & XRP_FLAG_VOLUME_LOADS) ? 0 : tex, pl && pl->Q.trace);
+                     (o.flags & XRP_FLAG_VOLUME_LOADS) ? 0 : tex, pl && pl->Q.trace && pl->Q.trace != 4);
     if (rc) return rc;
     unsigned long long* stats = nullptr;
     cudaError_t e;
-    if (want_stats) {
+    PropLaunch plain;
+    PoolBuf lbuf, lcnt, lstats, rbuf, rcnt;
+    // below 2^22 rays the list's extra launches cost more than the in-place
+    // re-evaluation (one 512^2 view: 785 against 994 Mrays/s)
+    const bool big = (long long)nviews * res * res >= (1LL << 22);
+    const bool listed = plain_list && !pl && !pr.volume_fast && !(o.flags & XRP_FLAG_PLAIN_INPLACE) &&
+                        ((o.flags & XRP_FLAG_PLAIN_LIST) || big);
+    if (listed) {
+        memset(&plain.Q, 0, sizeof(plain.Q));
+        plain.Q.trace = 4;
+        if (o.integration == XRP_INTEGRATE_HIERARCHICAL) plain.max_rays = 1LL << 21;
+        if ((rc = alloc_fallback_list(E, plain, lbuf, lcnt, st))) return rc;
+        // one slot per ray of the largest launch (the view split below)
+        const long long img_rays = (long long)res * res;
+        const long long redo_rays =
+            std::min<long long>(nviews, std::max<long long>(1, plain.max_rays / img_rays)) * img_rays;
+        if (redo_rays > 0xffffffffLL) return fail(2, "too many rays per launch for the redo list");
+        if ((e = rbuf.alloc(E, (size_t)redo_rays * sizeof(unsigned), st)) != cudaSuccess ||
+            (e = rcnt.alloc(E, sizeof(unsigned), st)) != cudaSuccess)
+            return cuda_fail(3, "redo list", e);
+        plain.Q.redo = (unsigned*)rbuf.p;
+        plain.Q.redo_count = (unsigned*)rcnt.p;
+        plain.Q.redo_cap = (unsigned)redo_rays;
+        if (want_stats) {
+            if ((e = lstats.alloc(E, kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
+                return cuda_fail(3, "stats buffer", e);
+            if ((e = cudaMemsetAsync(lstats.p, 0, kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
+                return cuda_fail(7, "stats reset", e);
+            plain.Q.stats = (unsigned long long*)lstats.p;
+        }
+        pl = &plain;
+    } else if (want_stats) {
         if ((e = cudaMemsetAsync(E->stats, 0, 2 * sizeof(unsigned long long), st)) != cudaSuccess)
             return cuda_fail(7, "stats reset", e);
         stats = E->stats;
@@ -672,6 +733,17 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
         if (code) return code;
         if (e2 != cudaSuccess) return cuda_fail(7, "kernel execution", e2);
         if (e1 != cudaSuccess) return cuda_fail(8, "image copy", e1);
+    }
+    if (listed) {
+        if (want_stats) {
+            unsigned long long h[kStatCount];
+            if ((e = cudaMemcpyAsync(h, lstats.p, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(st)) != cudaSuccess)
+                return cuda_fail(7, "stats read", e);
+            t_stats[0] = h[kStatEvaluations];
+            t_stats[1] = h[kStatFallbacks];
+        }
+        return 0;
     }
     if (want_stats) {
         unsigned long long h[2] = {0, 0};
@@ -859,7 +931,7 @@ int xrp_render(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_rend
     int rc = scene_texture(s, E->compute);
     if (rc) return rc;
     return render_views(E, s->hs, s->vdev, s->v64, v, *o, fov_max, out, true, E->compute, E->copy,
-                        (o->flags & XRP_FLAG_STATS) != 0, s->tex ? s->tex->tex : 0);
+                        (o->flags & XRP_FLAG_STATS) != 0, s->tex ? s->tex->tex : 0, nullptr, true);
 }
 
 int xrp_render_device(xrp_scene* s, const xrp_camera* views, int nviews, const xrp_render_opts* o,
@@ -879,7 +951,7 @@ int xrp_render_device(xrp_scene* s, const xrp_camera* views, int nviews, const x
     // stats use the engine's shared counters and need a synchronisation
     return render_views(E, s->hs, s->vdev, s->v64, v, *o, fov_max, out_device, false,
                         (cudaStream_t)stream, (cudaStream_t)stream, false,
-                        s->tex ? s->tex->tex : 0);
+                        s->tex ? s->tex->tex : 0, nullptr, true);
 }
 
 int xrp_last_stats(uint64_t* samples, uint64_t* fp64_samples) {
@@ -1694,17 +1766,9 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     // where undecided samples gather (several per ray on the lattice): the
     // same list for a quarter of the rays, sixteen entries per ray.
     if (o->integration == XRP_INTEGRATE_HIERARCHICAL) pl.max_rays = 1LL << 21;
-    const unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, (1LL << 23) * 4);
     PoolBuf fb, fbc;
-    if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
-        (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)
-        return cuda_fail(3, "fallback list", e);
-    if ((e = cudaMemsetAsync(fbc.p, 0, 2 * sizeof(unsigned), st)) != cudaSuccess)
-        return cuda_fail(7, "fallback list reset", e);
-    pl.Q.fb = (uint2*)fb.p;
-    pl.Q.fb_count = (unsigned*)fbc.p;
-    pl.Q.fb_overflow = (unsigned*)fbc.p + 1;
-    pl.Q.fb_cap = fb_cap;
+    int lrc = alloc_fallback_list(E, pl, fb, fbc, st);
+    if (lrc) return lrc;
     xrp_render_opts oo = *o;
     int rc = render_views(E, s->hs, s->vdev, s->v64, v, oo, fov_max, out, out_host, st,
                           out_host ? E->copy : st, false, 0, &pl);

@@ -8,14 +8,17 @@
 namespace xrp {
 
 // Ray- and curve-certificate kernels live in xrp_kern_trace_ray.cu and
-// xrp_kern_trace_curve.cu.
+// xrp_kern_trace_curve.cu, the plain kernels in xrp_kern_trace_plain.cu.
 cudaError_t launch_trace_ray(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                              cudaStream_t st);
 cudaError_t launch_trace_curve(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                                cudaStream_t st);
+cudaError_t launch_trace_plain(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                               cudaStream_t st);
 
 cudaError_t launch_trace(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                          cudaStream_t st) {
+    if (Q.trace == 4) return launch_trace_plain(pr, view0, nviews, Q, dout, st);
     if (Q.trace == 1 && pr.S.affine) return launch_trace_ray(pr, view0, nviews, Q, dout, st);
     if (Q.trace == 1 && pr.defs) return launch_trace_curve(pr, view0, nviews, Q, dout, st);
     return launch_trace_mode<0>(pr, view0, nviews, Q, dout, st);

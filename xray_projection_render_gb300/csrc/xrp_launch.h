@@ -58,7 +58,8 @@ struct Prepared {
 struct PropLaunch {
     PropParams Q;
     bool train = false;
-    long long max_rays = 1LL << 23;  // rays per launch (bounds the FP64 list: 4 entries per ray)
+    long long max_rays = 1LL << 23;  // rays per launch (bounds the FP64 list: 4 entries per ray,
+                                     // and the plain mode's redo list: one per ray)
 };
 
 // xrp_kern_scene.cu: k_render for general scenes.
@@ -114,6 +115,12 @@ cudaError_t launch_finish(const float* img, int nviews, int res, int transparenc
 // other deformation chains; 2: ball only.
 cudaError_t launch_trace(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                          cudaStream_t st);
+
+// xrp_kern_trace_plain.cu: the rays of the plain mode (Q.trace 4) whose
+// samples found the FP64 list full, marched again into the optical depths
+// `dout` (at most `cap` of the listed ones; `grid` blocks).
+cudaError_t launch_plain_redo(const Prepared& pr, int view0, const PropParams& Q, float* dout, unsigned cap,
+                              int grid, cudaStream_t st);
 
 // xrp_kern_prop.cu: the proposal march (rendering).
 cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,

@@ -31,7 +31,8 @@ struct PropParams {
     int mc;                        // samples per segment (multiple of 32)
     float tau;                     // logits above tau send a candidate to dense integration
     int refine;                    // 1: refine candidates by certificates; 0: dense
-    int trace;                     // 1: per-ray certificate tracing (k_trace) instead
+    int trace;                     // per-ray tracing (k_trace) instead: 1 ray/curve
+                                   // certificates, 2 balls, 4 plain (every sample)
     int min_piece;                 // pieces of at most this many samples go dense
     float fc[3], fs[3];            // feature normalisation (p - fc) * fs
     const int* rays;               // optional ray list: (view, i, j) triples, views absolute
@@ -48,6 +49,11 @@ struct PropParams {
     unsigned* fb_count;
     unsigned fb_cap;
     unsigned* fb_overflow;
+    // plain mode: rays to march again (a sample found the list full), one
+    // slot per ray of a launch, and their counter
+    unsigned* redo;
+    unsigned* redo_count;
+    unsigned redo_cap;
 };
 
 enum : int {
@@ -439,8 +445,12 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 // (smooth non-affine chains): the certificate is the curve bound of
 // dens_curve32, the first parameter at which the curved path of the
 // deformed samples can reach a boundary.  CERT: 0 ball, 1 ray, 2 curve,
-// 3 curve for scenes whose leaves are all gyroids (a smaller kernel).
-// Samples FP32 cannot decide go to the FP64 list like the other march modes.
+// 3 curve for scenes whose leaves are all gyroids (a smaller kernel), 4 no
+// certificate: the plain integrator, every sample evaluated.
+// Samples FP32 cannot decide go to the FP64 list like the other march modes
+// (in the plain mode a ray with a sample that found the list full is marched
+// again by k_plain_redo, so the plain integrator never needs the host's
+// overflow check).
 // Resident blocks per SM for depth < 3, measured: 4 (64 registers; lattice
 // with ray bounds 415 against 382 Mrays/s with 3 and 410 with 5, gyroid with
 // balls 1462 against 1406 with 3).  Tried and dropped: four pixels per
@@ -455,12 +465,19 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 #ifndef XRP_CURVE_MIN_BLOCKS
 #define XRP_CURVE_MIN_BLOCKS 4
 #endif
+// Resident blocks per SM of the plain mode (depth < 3).
+#ifndef XRP_PLAIN_MIN_BLOCKS
+#define XRP_PLAIN_MIN_BLOCKS 4
+#endif
 template <int DEPTH, bool DEFS, bool HIER, int CERT>
-__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_MIN_BLOCKS : 4))
+__global__ void __launch_bounds__(256, DEPTH >= 3 ? 2
+                                                  : (CERT == 2 || CERT == 3) ? XRP_CURVE_MIN_BLOCKS
+                                                  : CERT == 4                ? XRP_PLAIN_MIN_BLOCKS
+                                                                             : 4)
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
-    constexpr bool RAY = CERT == 1, CURVE = CERT >= 2;
+    constexpr bool RAY = CERT == 1, CURVE = CERT == 2 || CERT == 3, PLAIN = CERT == 4;
     constexpr int LM = CERT == 3 ? kLeafGyroid : kLeafAll;
     const int res = P.res;
     const int tpr = (res + 15) >> 4;
@@ -472,7 +489,8 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_M
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = (ti << 4) + ((warp >> 1) << 2) + (lane >> 3);
     const int j = (tj << 4) + ((warp & 1) << 3) + (lane & 7);
-    unsigned evals = 0;
+    unsigned evals = 0, inplace = 0;  // evaluations; FP64 re-evaluations in place
+    bool lost = false;                // a sample found the FP64 list full
     // the scene's node table in shared memory (S.nnodes > 0: it fits); the
     // FP64 re-evaluation keeps the global table
     extern __shared__ __align__(16) unsigned char trace_smem[];
@@ -498,32 +516,49 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2 : (CERT >= 2 ? XRP_CURVE_M
                 // a coarse sample's value decides refinement: FP64 in place;
                 // fine samples only add, so they go to the list (high bit)
                 const ViewDev& V = views[view0 + v];
-                sum = trace_sum_hier<DEPTH, DEFS, RAY, CURVE, LM>(
+                sum = trace_sum_hier<DEPTH, DEFS, RAY, CURVE, LM, PLAIN>(
                     Sl, L, ray, k0, k1,
                     [&](int q, bool fine) {
-                        if (!fine) return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
+                        if (!fine) {
+                            inplace++;
+                            return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[q]);
+                        }
                         unsigned slot = atomicAdd(Q.fb_count, 1u);
                         if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)q | 0x80000000u);
+                        else lost = true;
                         return 0.0f;
                     },
                     evals);
             } else {
-                sum = trace_sum<DEPTH, DEFS, RAY, CURVE, LM>(
-                    Sl, L, ray, k0, k1,
-                    [&](int k) {
-                        unsigned slot = atomicAdd(Q.fb_count, 1u);
-                        if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);
-                        return 0.0f;
-                    },
-                    evals);
+                auto unc = [&](int k) {
+                    unsigned slot = atomicAdd(Q.fb_count, 1u);
+                    if (slot < Q.fb_cap) Q.fb[slot] = make_uint2((unsigned)r, (unsigned)k);
+                    else lost = true;
+                    return 0.0f;
+                };
+                if constexpr (PLAIN) sum = plain_sum<DEPTH, DEFS>(Sl, L, ray, k0, k1, unc, evals);
+                else sum = trace_sum<DEPTH, DEFS, RAY, CURVE, LM>(Sl, L, ray, k0, k1, unc, evals);
             }
         }
         const float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;
         out[r] = fmaf(w, sum, P.flat_field);
+        if constexpr (PLAIN) {
+            // a sample found the list full: the whole ray is marched again
+            // (k_plain_redo, after the FP64 pass); the redo list holds every
+            // ray of the launch
+            if (lost) {
+                const unsigned q = atomicAdd(Q.redo_count, 1u);
+                if (q < Q.redo_cap) Q.redo[q] = (unsigned)r;
+            }
+        }
     }
     if (Q.stats) {
         unsigned s = __reduce_add_sync(0xffffffffu, evals);
         if (lane == 0 && s) atomicAdd(&Q.stats[kStatEvaluations], (unsigned long long)s);
+        if constexpr (HIER) {
+            unsigned f = __reduce_add_sync(0xffffffffu, inplace);
+            if (lane == 0 && f) atomicAdd(&Q.stats[kStatFallbacks], (unsigned long long)f);
+        }
     }
 }
 

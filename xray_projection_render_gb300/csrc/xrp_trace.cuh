@@ -1,7 +1,8 @@
 // xrp_trace.cuh -- launch helpers of certificate tracing (k_trace in
 // xrp_proposal.cuh), instantiated per certificate kind in
-// xrp_kern_trace.cu (balls), xrp_kern_trace_ray.cu (ray bounds) and
-// xrp_kern_trace_curve.cu (curve bounds).
+// xrp_kern_trace.cu (balls), xrp_kern_trace_ray.cu (ray bounds),
+// xrp_kern_trace_curve.cu (curve bounds) and xrp_kern_trace_plain.cu (no
+// certificate: the plain integrator).
 #pragma once
 #include "xrp_launch.h"
 
@@ -28,12 +29,13 @@ cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams&
 template <int CERT>
 cudaError_t launch_trace_mode(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
                               cudaStream_t st) {
-    if (CERT >= 2 || pr.defs) {
+    constexpr bool kCurve = CERT == 2 || CERT == 3;
+    if (kCurve || pr.defs) {
         if (pr.depth == 0) return trace_r<0, true, CERT>(pr, view0, nviews, Q, dout, st);
         if (pr.depth == 1) return trace_r<1, true, CERT>(pr, view0, nviews, Q, dout, st);
         return trace_r<3, true, CERT>(pr, view0, nviews, Q, dout, st);
     }
-    if constexpr (CERT < 2) {
+    if constexpr (!kCurve) {
         if (pr.depth == 0) return trace_r<0, false, CERT>(pr, view0, nviews, Q, dout, st);
         if (pr.depth == 1) return trace_r<1, false, CERT>(pr, view0, nviews, Q, dout, st);
         return trace_r<3, false, CERT>(pr, view0, nviews, Q, dout, st);

@@ -105,13 +105,17 @@ def camera_arrays(angles, R=4.0, fov=40.0):
 
 
 def _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats,
-          volume_path="gather"):
+          volume_path="gather", plain_fp64="auto"):
     if integration not in ("simple", "hierarchical"):
         raise ValueError(f"Unknown integration method: {integration}")
     if volume_path not in ("gather", "loads"):
         raise ValueError(f"Unknown volume path: {volume_path}")
+    if plain_fp64 not in ("auto", "list", "inplace"):
+        raise ValueError(f"Unknown FP64 pass: {plain_fp64}")
     flags = (_lib.XRP_FLAG_STATS if stats else 0) | \
-        (_lib.XRP_FLAG_VOLUME_LOADS if volume_path == "loads" else 0)
+        (_lib.XRP_FLAG_VOLUME_LOADS if volume_path == "loads" else 0) | \
+        (_lib.XRP_FLAG_PLAIN_INPLACE if plain_fp64 == "inplace" else 0) | \
+        (_lib.XRP_FLAG_PLAIN_LIST if plain_fp64 == "list" else 0)
     return XrpRenderOpts(int(resolution),
                          _lib.XRP_INTEGRATE_HIERARCHICAL if integration == "hierarchical"
                          else _lib.XRP_INTEGRATE_SIMPLE,
@@ -121,19 +125,25 @@ def _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats,
 
 def render(scene: Scene, angles, *, resolution, ds, R=4.0, fov=40.0, flat_field=0.0,
            density_multiplier=1.0, integration="simple", out=None, stream=None, stats=False,
-           volume_path="gather"):
+           volume_path="gather", plain_fp64="auto"):
     """Render the views given by ``angles`` ((azimuthal, polar) degrees).
 
     Host path (default): returns a float32 numpy array [views, res, res];
     ``out`` may be a preallocated (ideally pinned) host array.  Device path:
     pass ``out`` as a contiguous float32 CUDA tensor; the work is queued on
-    ``stream`` (default: torch's current stream) and the call returns at once.
+    ``stream`` (default: torch's current stream) and the call returns once it
+    is queued.
     With ``stats`` (host path) returns (images, samples, fp64_samples).
     ``volume_path`` picks how a voxel-grid root is read: texture gathers
-    (default) or per-tap loads; both give the same results."""
+    (default) or per-tap loads; both give the same results.  ``plain_fp64``
+    (general scenes): "list" leaves the samples FP32 cannot decide to one FP64
+    pass after the march; "inplace" re-evaluates them inside the march;
+    "auto" takes the list for calls of at least 2^22 rays.  Both agree to FP32
+    rounding."""
     L = _lib.load()
     cams, n = cameras_from_angles(angles, R, fov)
-    o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats, volume_path)
+    o = _opts(resolution, ds, R, flat_field, density_multiplier, integration, stats, volume_path,
+              plain_fp64)
     if out is not None and _is_torch_cuda(out):
         import torch
         if out.dtype != torch.float32 or not out.is_contiguous() or out.numel() < n * resolution ** 2:
