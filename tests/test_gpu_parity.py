@@ -97,7 +97,7 @@ def test_plain_fp64_list_matches_inplace(X, name, integration):
         X.render(s, w.angles, out=dev, plain_fp64="list", **kw)
         torch.cuda.synchronize()
         d = dev.cpu().numpy()
-    assert (na, fa) == (nb, fb)
+    assert (na, fa) == (nb, fb)  # the same FP32 decisions
     assert np.array_equal(auto, b)
     if name == "deformed_lattice":
         assert fa > 0

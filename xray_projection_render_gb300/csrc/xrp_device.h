@@ -1747,16 +1747,20 @@ XRP_HD float plain_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 
 // Certificate tracing of the hierarchical integrator (main.go:159-199):
 // coarse samples k0..k1 (right ends, spacing DS).  A coarse sample whose
-// zero-ness differs from its predecessor's is refined over its fine samples
-// exactly as march_hier does (tracing the fine samples with certificates
-// too, tried, cut the evaluations by a third but ran 12-15 % slower: a
-// certificate costs several plain evaluations); the coarse samples a
-// certificate covers share the evaluated density, so none of them flips and
-// each adds rho*DS.
+// zero-ness differs from its predecessor's is refined over every one of its
+// fine samples, as march_hier does (letting certificates skip fine samples,
+// tried in the nested loop, cut the evaluations by a third but ran 12-15 %
+// slower); the coarse samples a certificate covers share the evaluated
+// density, so none of them flips and each adds rho*DS.
 // `unc(index, fine)` gives the value of an undecided coarse (fine = false,
 // index into s64) or fine (fine = true, index into f64) sample.  Returns
 // sum(w * rho) with w in {DS, DS/10}.  PLAIN: no certificates (every coarse
 // sample evaluated), the plain hierarchical integrator.
+// Tried and dropped: leaving an undecided coarse sample to the FP64 pass
+// (refining the intervals on both sides of it whatever its zero-ness, and
+// choosing the terms there) instead of re-evaluating it in place: the extra
+// loop state spilled and grew the kernel (lattice 64.7 -> 61.0 Mrays/s,
+// gyroid 364 -> 185).
 template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, bool PLAIN = false, class Unc>
 XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
                             unsigned& evals) {
@@ -1783,8 +1787,12 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
         const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
         float m = 0.0f;
         float rho;
+        // fine samples go through the certificate evaluation too (radius
+        // unused): one call site per iteration.  With a plain evaluation for
+        // them, a warp whose lanes mix coarse and fine samples ran both
+        // every iteration (hierarchical lattice 53.8 against 64.7 Mrays/s,
+        // gyroid 342 against 364).
         if constexpr (PLAIN) rho = density32<DEPTH, DEFS>(S, x, y, z);
-        else if (fine) rho = density32<DEPTH, DEFS>(S, x, y, z);
         else if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
         else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);

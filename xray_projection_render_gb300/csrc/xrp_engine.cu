@@ -279,6 +279,7 @@ namespace {
 struct Engine {
     int device = -1;
     cudaStream_t compute = nullptr, copy = nullptr;
+    cudaStream_t side = nullptr;  // highest priority: FP64 passes beside the next march
     cudaMemPool_t pool = nullptr;
     std::mutex mtx;
     unsigned long long* stats = nullptr;  // 2 counters
@@ -307,8 +308,11 @@ Engine* engine_for_current(int* code) {
     props.handleTypes = cudaMemHandleTypeNone;
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = dev;
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
     if ((e = cudaStreamCreateWithFlags(&E->compute, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&E->copy, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithPriority(&E->side, cudaStreamNonBlocking, prio_greatest)) != cudaSuccess ||
         (e = cudaMemPoolCreate(&E->pool, &props)) != cudaSuccess ||
         (e = cudaMalloc(&E->stats, 2 * sizeof(unsigned long long))) != cudaSuccess) {
         *code = cuda_fail(3, "engine initialisation", e);
@@ -561,31 +565,110 @@ int prepare(Engine* E, const HostScene& hs, const std::vector<const float*>& vol
 // pl.max_rays rays, with its counter and overflow flag.
 // XRP_FALLBACK_LIST (a test hook) sets a smaller capacity, which exercises
 // the overflow paths.
-static int alloc_fallback_list(Engine* E, PropLaunch& pl, PoolBuf& fb, PoolBuf& fbc, cudaStream_t st) {
+// With `slots` 2 the list, counter and flag come twice (pl.fb_slot,
+// pl.cnt_slot), for the overlapped launch groups.
+static int alloc_fallback_list(Engine* E, PropLaunch& pl, PoolBuf& fb, PoolBuf& fbc, cudaStream_t st,
+                               int slots = 1) {
     unsigned fb_cap = (unsigned)std::max<long long>(1 << 20, (1LL << 23) * 4);
     if (const char* c = getenv("XRP_FALLBACK_LIST"))
         if (*c) fb_cap = (unsigned)std::min<long long>(fb_cap, std::max(1LL, atoll(c)));
     cudaError_t e;
-    if ((e = fb.alloc(E, (size_t)fb_cap * sizeof(uint2), st)) != cudaSuccess ||
-        (e = fbc.alloc(E, 2 * sizeof(unsigned), st)) != cudaSuccess)
+    if ((e = fb.alloc(E, (size_t)slots * fb_cap * sizeof(uint2), st)) != cudaSuccess ||
+        (e = fbc.alloc(E, (size_t)slots * 2 * sizeof(unsigned), st)) != cudaSuccess)
         return cuda_fail(3, "fallback list", e);
-    if ((e = cudaMemsetAsync(fbc.p, 0, 2 * sizeof(unsigned), st)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(fbc.p, 0, (size_t)slots * 2 * sizeof(unsigned), st)) != cudaSuccess)
         return cuda_fail(7, "fallback list reset", e);
-    pl.Q.fb = (uint2*)fb.p;
-    pl.Q.fb_count = (unsigned*)fbc.p;
-    pl.Q.fb_overflow = (unsigned*)fbc.p + 1;
+    for (int k = 0; k < slots; k++) {
+        pl.fb_slot[k] = (uint2*)fb.p + (size_t)k * fb_cap;
+        pl.cnt_slot[k] = (unsigned*)fbc.p + 2 * k;
+    }
+    pl.Q.fb = pl.fb_slot[0];
+    pl.Q.fb_count = pl.cnt_slot[0];
+    pl.Q.fb_overflow = pl.cnt_slot[0] + 1;
     pl.Q.fb_cap = fb_cap;
     return 0;
 }
 
-static cudaError_t launch_prop(const Prepared& pr, int view0, int nviews, const PropLaunch& pl,
-                               float* dout, cudaStream_t st) {
-    return pl.train ? launch_prop_train(pr, view0, nviews, pl.Q, st)
-                    : launch_prop_render(pr, view0, nviews, pl.Q, dout, st);
+// Whether a launch group found the FP64 list full (either slot).
+static cudaError_t list_overflowed(const PropLaunch& pl, cudaStream_t st, unsigned* ovf) {
+    unsigned h[2] = {0, 0};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 2 && e == cudaSuccess; k++)
+        if (pl.cnt_slot[k]) e = cudaMemcpyAsync(&h[k], pl.cnt_slot[k] + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    *ovf = h[0] | h[1];
+    return e;
+}
+
+// Events of the overlapped launch groups (PropLaunch::side).
+struct OverlapEvents {
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaError_t create(PropLaunch& pl, cudaStream_t side) {
+        for (auto& x : ev) {
+            cudaError_t e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
+        pl.marched = ev[0];
+        pl.done[0] = ev[1];
+        pl.done[1] = ev[2];
+        pl.side = side;
+        return cudaSuccess;
+    }
+    ~OverlapEvents() {
+        for (auto x : ev)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
+// Overlapping each launch group's FP64 pass with the next group's march:
+// on unless XRP_FB_OVERLAP is 0.
+static bool overlap_enabled() {
+    const char* c = getenv("XRP_FB_OVERLAP");
+    return !(c && c[0] == '0');
+}
+
+static cudaError_t launch_prop(const Prepared& pr, int view0, int nviews, PropLaunch& pl, float* dout,
+                               cudaStream_t st) {
+    if (pl.train) return launch_prop_train(pr, view0, nviews, pl.Q, st);
+    if (!pl.side) return launch_prop_render(pr, view0, nviews, pl.Q, dout, st);
+    // group g uses list slot g & 1; its march waits until the FP64 pass of
+    // group g - 2 (the slot's previous user) is done with the list, and its
+    // tail runs on the side stream once the march is
+    const int k = pl.groups & 1;
+    PropParams Q = pl.Q;
+    Q.fb = pl.fb_slot[k];
+    Q.fb_count = pl.cnt_slot[k];
+    Q.fb_overflow = pl.cnt_slot[k] + 1;
+    if (Q.trace == 4) {
+        Q.redo = pl.redo_slot[k];
+        Q.redo_count = pl.redo_cnt_slot[k];
+    }
+    cudaError_t e;
+    if (pl.groups >= 2 && (e = cudaStreamWaitEvent(st, pl.done[k], 0)) != cudaSuccess) return e;
+    if ((e = launch_prop_march(pr, view0, nviews, Q, dout, st)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(pl.marched, st)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(pl.side, pl.marched, 0)) != cudaSuccess)
+        return e;
+    // one block of the FP64 pass per SM: it takes the registers one march
+    // block frees, and the next group's march keeps the rest
+    if ((e = launch_prop_tail(pr, view0, nviews, Q, dout, pl.side, 1)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(pl.done[k], pl.side)) != cudaSuccess) return e;
+    pl.groups++;
+    return cudaSuccess;
+}
+
+// The call's stream waits for every tail still on the side stream.
+static cudaError_t join_side(const PropLaunch* pl, cudaStream_t st) {
+    if (!pl || !pl->side) return cudaSuccess;
+    for (int k = 0; k < 2 && k < pl->groups; k++) {
+        cudaError_t e = cudaStreamWaitEvent(st, pl->done[k], 0);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integration, float* dout,
-                          unsigned long long* stats, cudaStream_t st, const PropLaunch* pl = nullptr) {
+                          unsigned long long* stats, cudaStream_t st, PropLaunch* pl = nullptr) {
     if (pl) return launch_prop(pr, view0, nviews, *pl, dout, st);
     const ViewDev* dviews = pr.views;
     const int res = pr.P.res;
@@ -608,8 +691,8 @@ static cudaError_t launch(const Prepared& pr, int view0, int nviews, int integra
 }
 
 // Renders `views` into `out` (device or host memory).  Host output goes
-// through two device chunk buffers so the copy of chunk c overlaps the
-// rendering of chunk c+1.
+// through two or three device chunk buffers so the copy of chunk c overlaps
+// the rendering of the next chunks.
 //
 // plain_list: the plain integrator over a general scene (not the voxel-grid
 // fast path) marches in the tracing kernel's plain mode, which leaves the
@@ -622,7 +705,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
                         const std::vector<const double*>& v64, const std::vector<ViewDev>& views,
                         const xrp_render_opts& o, double fov_max, float* out, bool out_host,
                         cudaStream_t st, cudaStream_t st_copy, bool want_stats,
-                        cudaTextureObject_t tex, const PropLaunch* pl = nullptr, bool plain_list = false) {
+                        cudaTextureObject_t tex, PropLaunch* pl = nullptr, bool plain_list = false) {
     const int res = o.resolution;
     const int nviews = (int)views.size();
     PoolBuf tab;
@@ -644,17 +727,22 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
         memset(&plain.Q, 0, sizeof(plain.Q));
         plain.Q.trace = 4;
         if (o.integration == XRP_INTEGRATE_HIERARCHICAL) plain.max_rays = 1LL << 21;
-        if ((rc = alloc_fallback_list(E, plain, lbuf, lcnt, st))) return rc;
+        const int slots = (long long)nviews * res * res > plain.max_rays ? 2 : 1;
+        if ((rc = alloc_fallback_list(E, plain, lbuf, lcnt, st, slots))) return rc;
         // one slot per ray of the largest launch (the view split below)
         const long long img_rays = (long long)res * res;
         const long long redo_rays =
             std::min<long long>(nviews, std::max<long long>(1, plain.max_rays / img_rays)) * img_rays;
         if (redo_rays > 0xffffffffLL) return fail(2, "too many rays per launch for the redo list");
-        if ((e = rbuf.alloc(E, (size_t)redo_rays * sizeof(unsigned), st)) != cudaSuccess ||
-            (e = rcnt.alloc(E, sizeof(unsigned), st)) != cudaSuccess)
+        if ((e = rbuf.alloc(E, (size_t)slots * redo_rays * sizeof(unsigned), st)) != cudaSuccess ||
+            (e = rcnt.alloc(E, (size_t)slots * sizeof(unsigned), st)) != cudaSuccess)
             return cuda_fail(3, "redo list", e);
-        plain.Q.redo = (unsigned*)rbuf.p;
-        plain.Q.redo_count = (unsigned*)rcnt.p;
+        for (int k = 0; k < slots; k++) {
+            plain.redo_slot[k] = (unsigned*)rbuf.p + (size_t)k * redo_rays;
+            plain.redo_cnt_slot[k] = (unsigned*)rcnt.p + k;
+        }
+        plain.Q.redo = plain.redo_slot[0];
+        plain.Q.redo_count = plain.redo_cnt_slot[0];
         plain.Q.redo_cap = (unsigned)redo_rays;
         if (want_stats) {
             if ((e = lstats.alloc(E, kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
@@ -673,35 +761,51 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     const int tpv = ((res + 15) / 16) * ((res + 15) / 16);
     int max_views_per_launch = std::max(1, (int)(0x7fffffffL / tpv));
     if (pl) max_views_per_launch = std::max(1, std::min<int>(max_views_per_launch, (int)(pl->max_rays / (long long)img)));
+    // two list slots: each launch group's FP64 pass beside the next march
+    OverlapEvents ovl;
+    if (pl && !pl->train && pl->fb_slot[1] && nviews > max_views_per_launch && overlap_enabled()) {
+        pl->groups = 0;
+        if ((e = ovl.create(*pl, E->side)) != cudaSuccess) return cuda_fail(7, "overlap events", e);
+    }
     if (!out_host) {
         for (int v0 = 0; v0 < nviews; v0 += max_views_per_launch) {
             int n = std::min(max_views_per_launch, nviews - v0);
             if ((e = injected("launch")) != cudaSuccess ||
-                (e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st, pl)) != cudaSuccess)
+                (e = launch(pr, v0, n, o.integration, out + (size_t)v0 * img, stats, st, pl)) != cudaSuccess) {
+                join_side(pl, st);
                 return cuda_fail(7, "kernel launch", e);
+            }
         }
+        if ((e = join_side(pl, st)) != cudaSuccess) return cuda_fail(7, "kernel launch", e);
     } else {
         size_t chunk = std::max<size_t>(1, std::min<size_t>((size_t)nviews, ((size_t)64 << 20) / (img * 4)));
         chunk = std::min<size_t>(chunk, (size_t)max_views_per_launch);
         int nchunks = (int)((nviews + chunk - 1) / chunk);
-        PoolBuf buf[2];
-        for (int b = 0; b < std::min(2, nchunks); b++)
+        // chunk buffers: two, or three when the FP64 passes run on the side
+        // stream (a chunk is copied only after its pass, and the march that
+        // reuses its buffer would wait for that copy with two)
+        const int nbuf = (pl && pl->side) ? 3 : 2;
+        PoolBuf buf[3];
+        for (int b = 0; b < std::min(nbuf, nchunks); b++)
             if ((e = injected("output")) != cudaSuccess ||
-                (e = buf[b].alloc(E, chunk * img * sizeof(float), st)) != cudaSuccess)
+                (e = buf[b].alloc(E, chunk * img * sizeof(float), st)) != cudaSuccess) {
+                join_side(pl, st);
                 return cuda_fail(6, "image buffer allocation", e);
-        cudaEvent_t kev[2], cev[2];
-        for (int b = 0; b < 2; b++) {
+            }
+        cudaEvent_t kev[3], cev[3];
+        for (int b = 0; b < 3; b++) {
             cudaEventCreateWithFlags(&kev[b], cudaEventDisableTiming);
             cudaEventCreateWithFlags(&cev[b], cudaEventDisableTiming);
         }
         auto launch_chunk = [&](int c) -> cudaError_t {
-            int b = c & 1;
-            if (c >= 2) cudaStreamWaitEvent(st, cev[b], 0);
+            int b = c % nbuf;
+            if (c >= nbuf) cudaStreamWaitEvent(st, cev[b], 0);
             int v0 = (int)(c * chunk);
             int n = (int)std::min(chunk, (size_t)(nviews - v0));
             cudaError_t le = injected("launch");
             if (le == cudaSuccess) le = launch(pr, v0, n, o.integration, (float*)buf[b].p, stats, st, pl);
-            cudaEventRecord(kev[b], st);
+            // overlapped groups finish on the side stream
+            cudaEventRecord(kev[b], (pl && pl->side) ? pl->side : st);
             return le;
         };
         int code = 0;
@@ -711,7 +815,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
                 code = cuda_fail(7, "kernel launch", e);
                 break;
             }
-            int b = c & 1;
+            int b = c % nbuf;
             int v0 = (int)(c * chunk);
             size_t n = std::min(chunk, (size_t)(nviews - v0));
             cudaStreamWaitEvent(st_copy, kev[b], 0);
@@ -724,9 +828,11 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
             }
             cudaEventRecord(cev[b], st_copy);
         }
+        cudaError_t e0 = join_side(pl, st);
         cudaError_t e1 = cudaStreamSynchronize(st_copy);
         cudaError_t e2 = cudaStreamSynchronize(st);
-        for (int b = 0; b < 2; b++) {
+        if (e2 == cudaSuccess) e2 = e0;
+        for (int b = 0; b < 3; b++) {
             cudaEventDestroy(kev[b]);
             cudaEventDestroy(cev[b]);
         }
@@ -1767,7 +1873,8 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     // same list for a quarter of the rays, sixteen entries per ray.
     if (o->integration == XRP_INTEGRATE_HIERARCHICAL) pl.max_rays = 1LL << 21;
     PoolBuf fb, fbc;
-    int lrc = alloc_fallback_list(E, pl, fb, fbc, st);
+    const int slots = (long long)nviews * o->resolution * o->resolution > pl.max_rays ? 2 : 1;
+    int lrc = alloc_fallback_list(E, pl, fb, fbc, st, slots);
     if (lrc) return lrc;
     xrp_render_opts oo = *o;
     int rc = render_views(E, s->hs, s->vdev, s->v64, v, oo, fov_max, out, out_host, st,
@@ -1776,9 +1883,7 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     // an overflowed list (more undecided samples in one launch than it
     // holds) is not expected; the plain integrator then renders the call
     unsigned ovf = 0;
-    if ((e = cudaMemcpyAsync(&ovf, pl.Q.fb_overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess)
-        return cuda_fail(7, "proposal march", e);
+    if ((e = list_overflowed(pl, st, &ovf)) != cudaSuccess) return cuda_fail(7, "proposal march", e);
     if (ovf) {
         rc = render_views(E, s->hs, s->vdev, s->v64, v, oo, fov_max, out, out_host, st,
                           out_host ? E->copy : st, false, 0, nullptr);

@@ -60,6 +60,18 @@ struct PropLaunch {
     bool train = false;
     long long max_rays = 1LL << 23;  // rays per launch (bounds the FP64 list: 4 entries per ray,
                                      // and the plain mode's redo list: one per ray)
+    // With `side`, the FP64 pass and exp of launch group g run on `side`
+    // while group g + 1 marches on the call's stream: the lists alternate
+    // between two slots (list, counter + overflow flag, redo list and its
+    // counter), `done[s]` marks slot s's last tail, `groups` counts the
+    // groups launched.  Null: one stream.
+    cudaStream_t side = nullptr;
+    uint2* fb_slot[2] = {nullptr, nullptr};
+    unsigned* cnt_slot[2] = {nullptr, nullptr};
+    unsigned* redo_slot[2] = {nullptr, nullptr};
+    unsigned* redo_cnt_slot[2] = {nullptr, nullptr};
+    cudaEvent_t marched = nullptr, done[2] = {nullptr, nullptr};
+    int groups = 0;
 };
 
 // xrp_kern_scene.cu: k_render for general scenes.
@@ -123,6 +135,10 @@ cudaError_t launch_plain_redo(const Prepared& pr, int view0, const PropParams& Q
                               int grid, cudaStream_t st);
 
 // xrp_kern_prop.cu: the proposal march (rendering).
+cudaError_t launch_prop_march(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                              cudaStream_t st);
+cudaError_t launch_prop_tail(const Prepared& pr, int view0, int nviews, const PropParams& Q, float* dout,
+                             cudaStream_t st, int blocks_per_sm);
 cudaError_t launch_prop_render(const Prepared& pr, int view0, int nviews, const PropParams& Q,
                                float* dout, cudaStream_t st);
 

@@ -469,11 +469,16 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 #ifndef XRP_PLAIN_MIN_BLOCKS
 #define XRP_PLAIN_MIN_BLOCKS 4
 #endif
+// Resident blocks per SM of the hierarchical integrator (depth < 3).
+#ifndef XRP_HIER_MIN_BLOCKS
+#define XRP_HIER_MIN_BLOCKS 4
+#endif
 template <int DEPTH, bool DEFS, bool HIER, int CERT>
 __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2
-                                                  : (CERT == 2 || CERT == 3) ? XRP_CURVE_MIN_BLOCKS
-                                                  : CERT == 4                ? XRP_PLAIN_MIN_BLOCKS
-                                                                             : 4)
+                                       : HIER     ? XRP_HIER_MIN_BLOCKS
+                                       : (CERT == 2 || CERT == 3) ? XRP_CURVE_MIN_BLOCKS
+                                       : CERT == 4                ? XRP_PLAIN_MIN_BLOCKS
+                                                                  : 4)
     k_trace(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
             const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views, int view0, int nviews,
             const __grid_constant__ PropParams Q, float* __restrict__ out) {
@@ -566,7 +571,13 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2
 // FP64 re-evaluation of the samples the march left undecided: adds
 // w * density (reference arithmetic at the reference's position) to the
 // ray's optical depth.  Rays are numbered within the launch (view0 first).
-__global__ void __launch_bounds__(256)
+// Four blocks per SM (64 registers): a block fits the registers one block of
+// the tracing kernel frees, so the FP64 pass of one launch group can run
+// beside the next group's march.
+#ifndef XRP_FB_MIN_BLOCKS
+#define XRP_FB_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(256, XRP_FB_MIN_BLOCKS)
     k_prop_fallback(const __grid_constant__ SceneDev S, const __grid_constant__ Lattice L,
                     const __grid_constant__ RenderParams P, const ViewDev* __restrict__ views,
                     int view0, const uint2* __restrict__ fb, const unsigned* __restrict__ fb_count,
