@@ -1747,11 +1747,11 @@ XRP_HD float plain_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 
 // Certificate tracing of the hierarchical integrator (main.go:159-199):
 // coarse samples k0..k1 (right ends, spacing DS).  A coarse sample whose
-// zero-ness differs from its predecessor's is refined over every one of its
-// fine samples, as march_hier does (letting certificates skip fine samples,
-// tried in the nested loop, cut the evaluations by a third but ran 12-15 %
-// slower); the coarse samples a certificate covers share the evaluated
-// density, so none of them flips and each adds rho*DS.
+// zero-ness differs from its predecessor's is refined over its fine samples
+// as march_hier does, each fine sample's certificate covering the fine
+// samples after it that lie within its radius; the coarse samples a
+// certificate covers share the evaluated density, so none of them flips and
+// each adds rho*DS.
 // `unc(index, fine)` gives the value of an undecided coarse (fine = false,
 // index into s64) or fine (fine = true, index into f64) sample.  Returns
 // sum(w * rho) with w in {DS, DS/10}.  PLAIN: no certificates (every coarse
@@ -1767,6 +1767,8 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
     KahanF acc;
     const float step = L.ds32 * 1.00001f;
     const float istep = (1.0f / step) * 0.999999f;  // rounded down
+    const float stepf = L.dsf32 * 1.00001f;          // the fine samples' spacing, rounded up
+    const float istepf = (1.0f / stepf) * 0.999999f;
     RayDir u;
     if constexpr (RAY) u = ray_dir32(S, ray.d32);
     bool prev_zero = true;  // coarse samples before k0 are outside the support
@@ -1787,20 +1789,25 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
         const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
         float m = 0.0f;
         float rho;
-        // fine samples go through the certificate evaluation too (radius
-        // unused): one call site per iteration.  With a plain evaluation for
-        // them, a warp whose lanes mix coarse and fine samples ran both
-        // every iteration (hierarchical lattice 53.8 against 64.7 Mrays/s,
-        // gyroid 342 against 364).
+        // fine samples go through the certificate evaluation too: one call
+        // site per iteration (with a plain evaluation for them, a warp whose
+        // lanes mix coarse and fine samples ran both every iteration:
+        // hierarchical lattice 53.8 against 64.7 Mrays/s, gyroid 342 against
+        // 364), and their radius skips the fine samples it covers.
         if constexpr (PLAIN) rho = density32<DEPTH, DEFS>(S, x, y, z);
-        else if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
+        else if constexpr (RAY)
+            rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, fine ? (float)(qe - q) * stepf : (float)(k1 - k + 1) * step, m);
         else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
         else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
         evals++;
         if (fine) {
+            // the fine samples its certificate covers share its density
+            int jf = 0;
             if (isunc(rho)) rho = unc(q, true);
-            acc.add(rho * L.dsf32);
-            if (++q < qe) continue;
+            else if constexpr (!PLAIN) jf = (int)fminf(floorf(m * istepf), (float)(qe - 1 - q));
+            acc.add(rho * L.dsf32 * (float)(jf + 1));
+            q += jf + 1;
+            if (q < qe) continue;
             // interval refined: the coarse sample's own term and its jump
             acc.add(rho_c * L.dsf32);
             if (jmp_c > 0) acc.add(rho_c * L.ds32 * (float)jmp_c);
