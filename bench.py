@@ -600,7 +600,8 @@ def bench_scene(args):
     # uploaded and images read back inside the timed region
     e2e_times = []
     out_host = None if args.no_e2e else torch.empty((n_my, res, res), dtype=torch.float32).pin_memory()
-    if is_voxel:
+    if is_voxel and args.integration == "simple":
+        # the reference's own entry point (uniform-step integrator only)
         cams21 = X.xray_camera_params(my_angles, w.R, w.fov)
         h2d = int(w.volume.nbytes + cams21.nbytes)
         path = "RenderVolumeProjectionsCUDA, pinned host buffers"
@@ -609,6 +610,15 @@ def bench_scene(args):
 
         def e2e_call():
             X.render_volume_projections(vol_host.numpy(), cams21, res, w.ds, out=out_host)
+    elif is_voxel:
+        h2d = int(w.volume.nbytes) + n_my * 192
+        path = "xrp_scene_create (host volume) + xrp_render, pinned host buffers"
+        if not args.no_e2e:
+            vol_host = torch.from_numpy(w.volume).pin_memory()
+
+        def e2e_call():
+            with X.Scene(w.obj, w.deformation, [vol_host.numpy()]) as s2:
+                X.render(s2, my_angles, out=out_host, **kw)
     else:
         obj_json = json.dumps(w.obj)
         def_json = json.dumps(w.deformation) if w.deformation else None

@@ -334,8 +334,12 @@ XRP_API void xrp_proposal_destroy(xrp_proposal* p);
  * whose zero-ness changes).  When the deformation chain is affine (linear,
  * affine, rigid or none) the certificate is a ray bound, the distance along
  * the ray to the next place where the density can change (the samples lie
- * on a line in object coordinates); otherwise, or with XRP_FLAG_BALL, it is
- * the radius of a ball around the sample.  The device variant queues the work on `stream`
+ * on a line in object coordinates).  Otherwise the simple integrator uses a
+ * curve bound (how far along the ray the curved path of the deformed samples
+ * stays clear of every boundary) and the hierarchical one the radius of a
+ * ball around the sample; XRP_FLAG_BALL forces balls.  A call of several
+ * launch groups runs each group's FP64 pass on a side stream beside the next
+ * group's march.  The device variant queues the work on `stream`
  * and then waits for it (it reads back whether the list of samples left to
  * FP64 overflowed, in which case the plain integrator renders the call). */
 XRP_API int xrp_render_proposal(xrp_scene* scene, const xrp_proposal* proposal, int segment,

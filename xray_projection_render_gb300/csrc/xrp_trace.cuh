@@ -16,10 +16,13 @@ cudaError_t trace_r(const Prepared& pr, int view0, int nviews, const PropParams&
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffL) return cudaErrorInvalidConfiguration;
     const size_t smem = (size_t)pr.S.nnodes * sizeof(Node);
-    if (pr.L.hierarchical)
-        k_trace<DEPTH, DEFS, true, CERT><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
-                                                                            nviews, Q, dout);
-    else
+    if (pr.L.hierarchical) {
+        // curve certificates serve the simple integrator only
+        if constexpr (CERT == 2 || CERT == 3) return cudaErrorInvalidValue;
+        else
+            k_trace<DEPTH, DEFS, true, CERT><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views,
+                                                                                view0, nviews, Q, dout);
+    } else
         k_trace<DEPTH, DEFS, false, CERT><<<(unsigned)blocks, 256, smem, st>>>(pr.S, pr.L, pr.P, pr.views, view0,
                                                                              nviews, Q, dout);
     return cudaGetLastError();
