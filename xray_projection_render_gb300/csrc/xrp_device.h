@@ -1761,9 +1761,24 @@ XRP_HD float plain_sum(const SceneDev& S, const Lattice& L, const Ray& ray, int 
 // choosing the terms there) instead of re-evaluating it in place: the extra
 // loop state spilled and grew the kernel (lattice 64.7 -> 61.0 Mrays/s,
 // gyroid 364 -> 185).
-template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, bool PLAIN = false, class Unc>
+// Merging the in-place FP64 re-evaluations of the hierarchical march
+// (MERGE): a lane whose coarse sample FP32 cannot decide waits, and the
+// warp's waiting lanes are served together, in one call, once
+// XRP_MERGE_LANES of them wait, no other lane is still marching, or the
+// first has waited XRP_MERGE_WAIT iterations.  On GB300 a warp's FP64
+// instruction holds the narrow FP64 pipe however few lanes execute it, so
+// one call for several lanes costs about what one call for one lane does.
+#ifndef XRP_MERGE_LANES
+#define XRP_MERGE_LANES 4
+#endif
+#ifndef XRP_MERGE_WAIT
+#define XRP_MERGE_WAIT 32
+#endif
+
+template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, bool PLAIN = false,
+          bool MERGE = false, class Unc>
 XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray, int k0, int k1, Unc&& unc,
-                            unsigned& evals) {
+                            unsigned& evals, unsigned wmask = 0u) {
     KahanF acc;
     const float step = L.ds32 * 1.00001f;
     const float istep = (1.0f / step) * 0.999999f;  // rounded down
@@ -1781,49 +1796,82 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
     int q = 0, qe = 0;
     float rho_c = 0.0f;
     int jmp_c = 0;
-    while (k <= k1) {
-        const bool fine = q < qe;
-        const float tk = fine ? L.ft32[q] : lattice_t(L, k);
-        const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
-        const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
-        const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
-        float m = 0.0f;
-        float rho;
-        // fine samples go through the certificate evaluation too: one call
-        // site per iteration (with a plain evaluation for them, a warp whose
-        // lanes mix coarse and fine samples ran both every iteration:
-        // hierarchical lattice 53.8 against 64.7 Mrays/s, gyroid 342 against
-        // 364), and with ray and ball certificates their radius skips the
-        // fine samples it covers.
-        if constexpr (PLAIN) rho = density32<DEPTH, DEFS>(S, x, y, z);
-        else if constexpr (RAY)
-            rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, fine ? (float)(qe - q) * stepf : (float)(k1 - k + 1) * step, m);
-        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
-        else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
-        evals++;
-        if (fine) {
-            // the fine samples its certificate covers share its density (not
-            // with curve certificates: there the skips ran slower, gyroid
-            // 346 -> 319 Mrays/s, while the ball and ray certificates gained:
-            // lattice 66.6 -> 77.6, cube 837 -> 917)
-            int jf = 0;
-            if (isunc(rho)) rho = unc(q, true);
-            else if constexpr (!PLAIN && !CURVE) jf = (int)fminf(floorf(m * istepf), (float)(qe - 1 - q));
-            acc.add(rho * L.dsf32 * (float)(jf + 1));
-            q += jf + 1;
-            if (q < qe) continue;
-            // interval refined: the coarse sample's own term and its jump
-            acc.add(rho_c * L.dsf32);
-            if (jmp_c > 0) acc.add(rho_c * L.ds32 * (float)jmp_c);
-            k += jmp_c + 1;
-            continue;
+    bool pend = false;  // MERGE: coarse sample k waits for its FP64 value
+    int waited = 0;     // MERGE: iterations the warp's waiting lanes have waited
+    (void)wmask;
+    (void)waited;
+    for (;;) {
+        bool serve = false;
+#if defined(__CUDA_ARCH__)
+        if constexpr (MERGE) {
+            if (!__any_sync(wmask, k <= k1)) break;
+            const unsigned pm = __ballot_sync(wmask, pend);
+            if (pm) {
+                const unsigned busy = __ballot_sync(wmask, k <= k1 && !pend);
+                serve = __popc(pm) >= XRP_MERGE_LANES || busy == 0u || ++waited >= XRP_MERGE_WAIT;
+                if (serve) waited = 0;
+            }
+            if (k > k1) continue;
+        } else
+#endif
+        if (k > k1) {
+            break;
+        }
+        float rho, m = 0.0f;
+        bool certified = true;  // rho came with a certificate radius m
+        if (MERGE && pend) {
+            if (!serve) continue;
+            pend = false;
+            rho = unc(k, false);  // every waiting lane of the warp at once
+            certified = false;
+        } else {
+            const bool fine = q < qe;
+            const float tk = fine ? L.ft32[q] : lattice_t(L, k);
+            const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
+            const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
+            const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
+            // fine samples go through the certificate evaluation too: one call
+            // site per iteration (with a plain evaluation for them, a warp whose
+            // lanes mix coarse and fine samples ran both every iteration:
+            // hierarchical lattice 53.8 against 64.7 Mrays/s, gyroid 342 against
+            // 364), and with ray and ball certificates their radius skips the
+            // fine samples it covers.
+            if constexpr (PLAIN) rho = density32<DEPTH, DEFS>(S, x, y, z);
+            else if constexpr (RAY)
+                rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, fine ? (float)(qe - q) * stepf : (float)(k1 - k + 1) * step,
+                                              m);
+            else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
+            else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+            evals++;
+            if (fine) {
+                // the fine samples its certificate covers share its density (not
+                // with curve certificates: there the skips ran slower, gyroid
+                // 346 -> 319 Mrays/s, while the ball and ray certificates gained:
+                // lattice 66.6 -> 77.6, cube 837 -> 917)
+                int jf = 0;
+                if (isunc(rho)) rho = unc(q, true);
+                else if constexpr (!PLAIN && !CURVE) jf = (int)fminf(floorf(m * istepf), (float)(qe - 1 - q));
+                acc.add(rho * L.dsf32 * (float)(jf + 1));
+                q += jf + 1;
+                if (q < qe) continue;
+                // interval refined: the coarse sample's own term and its jump
+                acc.add(rho_c * L.dsf32);
+                if (jmp_c > 0) acc.add(rho_c * L.ds32 * (float)jmp_c);
+                k += jmp_c + 1;
+                continue;
+            }
+            if (isunc(rho)) {
+                if constexpr (MERGE) {
+                    pend = true;
+                    continue;
+                }
+                rho = unc(k, false);
+                certified = false;
+            }
         }
         int jmp = 0;
-        if (isunc(rho)) {
-            rho = unc(k, false);
-        } else if constexpr (!PLAIN) {
-            jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
-        }
+        if constexpr (!PLAIN)
+            if (certified) jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
         const bool zero = (rho == 0.0f);
         if (zero != prev_zero) {
             prev_zero = zero;
