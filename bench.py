@@ -64,6 +64,10 @@ DEFINITIONS = {
     "lattice": {"cells": "10x10x10 over [-1,1]^3", "unit_cell": "12 edge + 4 body-diagonal cylinders",
                 "strut_radius": 0.03, "deformation": "linear, strain zz 0.05",
                 "cameras": "azimuth U[0,360), polar U[30,150], seed 3"},
+    "gyroid_fine": {"gyroid": "scale 0.1, thickness 0.2, rho 1 (the reference's example scene), unit cell "
+                              "[-1,1]^3, outer bounds [-0.8,0.8]^3",
+                    "deformation": "sigmoid A 0.1, center 0, lengthscale 0.2, along z",
+                    "cameras": "64 of azimuth 0, 0.5, ..., 359.5 (evenly strided), polar 90"},
     "gyroid": {"gyroid": "scale 8, thickness 0.1, rho 1, tessellated over [-1,1]^3",
                "deformation": "sigmoid A 0.1, center 0, lengthscale 0.2, along z",
                "cameras": "azimuth 0, 0.5, ..., 359.5, polar 90"},
@@ -83,8 +87,10 @@ def parse():
                    help="engine (this library), reference (the reference's CPU algorithm on the "
                         "host cores) or reference_gpu (the reference's own GPU kernel, voxel grid only)")
     p.add_argument("--workload", default="lattice",
-                   choices=["lattice", "gyroid", "voxel", "cube", "batched", "finish", "voxelize"],
-                   help="lattice (default, the headline), the gyroid, the voxel grid, the cube minus "
+                   choices=["lattice", "gyroid", "gyroid_fine", "voxel", "cube", "batched", "finish",
+                            "voxelize"],
+                   help="lattice (default, the headline), the gyroid (scale 8), the example scene's "
+                        "gyroid (scale 0.1, 64 views), the voxel grid, the cube minus "
                         "sphere and cylinder, the batch of 64 uneven scenes (one persistent launch "
                         "replayed from a CUDA graph), device-side image finishing of 64 images of "
                         "1024^2, or the volume export of the deformed lattice at 256^3")
@@ -301,10 +307,10 @@ def run_reference(args):
     if args.workload == "batched":
         ws = W.batched_scenes(args.scenes)[:8]
         name = f"batched_scenes_{args.scenes}"
-        cfg = batched_config(args.scenes, world)
+        cfg = batched_config(args.scenes, world, args.integration)
 
         def measure(sec):
-            return cpu_baseline_multi(ws, sec)
+            return cpu_baseline_multi(ws, sec, args.integration)
         metric = BATCH_METRIC
     else:
         w = make_workload(args.workload, W, args.views, args.res)
@@ -398,6 +404,7 @@ FLOPS = {
     "cube": 54,      # sphere 9 + box 9 + cylinder 23 + collection 3 + clip 2
     "lattice": 437,  # linear deformation 18 + fold/bounds 27 + 16 cylinders x 23 + 16
     "gyroid": 53,    # gyroid 13 (+6 SFU) + sigmoid 5 (+2 SFU) + fold/bounds 27
+    "gyroid_fine": 53,
 }
 
 # DRAM bytes (read + write) per view of the voxel render kernel: a constant
@@ -415,6 +422,8 @@ def make_workload(name, W, views, res):
         w = W.deformed_lattice(1024, 360)
     elif name == "gyroid":
         w = W.gyroid_sigmoid(2048, 720)
+    elif name == "gyroid_fine":
+        w = W.gyroid_fine_sigmoid(2048, 64)
     else:
         raise ValueError(name)
     if views or res:
@@ -749,7 +758,7 @@ def bench_batched(args):
     flush = torch.empty(64 * 1024 * 1024, device=dev, dtype=torch.float32)
     march = args.march if args.march != "auto" else "trace"
     trace = _trace_mode(march)
-    b = X.Batch(items, ds=ds, autotune=True, trace=trace)
+    b = X.Batch(items, ds=ds, autotune=True, trace=trace, integration=args.integration)
     info = b.info()
     for _ in range(args.warmup):
         b.render(stream)
@@ -757,7 +766,8 @@ def bench_batched(args):
     # samples per step: each scene's counter pass on one view, scaled
     samples = 0.0
     for s, w in zip(scenes, ws):
-        _, n, _ = X.render(s, w.angles[:1], resolution=w.res, ds=ds, stats=True)
+        _, n, _ = X.render(s, w.angles[:1], resolution=w.res, ds=ds, stats=True,
+                           integration=args.integration)
         samples += n * len(w.angles)
     if world > 1:
         torch.distributed.barrier()
@@ -801,7 +811,7 @@ def bench_batched(args):
             t0 = time.perf_counter()
             sc2 = [X.Scene(o, d) for o, d in objs]
             with X.Batch([(s2, w.angles, w.res) for s2, w in zip(sc2, ws)], ds=ds, autotune=False,
-                         trace=trace) as b2:
+                         trace=trace, integration=args.integration) as b2:
                 b2.render()
                 for k, o in enumerate(outs):
                     XL.check(XL.load().xrp_batch_copy_item(b2._h, k, ctypes_ptr(o)), "xrp_batch_copy_item")
@@ -816,7 +826,7 @@ def bench_batched(args):
         "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 4)",
-        "config": batched_config(args.scenes, world),
+        "config": batched_config(args.scenes, world, args.integration),
         "batch": {"scenes": len(ws), "rays": rays, "tile": f'{info["tile_w"]}x{info["tile_h"]}',
                   "blocks_per_sm": info["blocks_per_sm"], "autotune_ms": info["tune_ms"],
                   "graph": "one CUDA graph replay per step",
@@ -836,7 +846,7 @@ def bench_batched(args):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_multi(ws[:8], args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline_multi(ws[:8], args.cpu_seconds, args.integration)
     if rank == 0:
         # error of the replayed batch against FP64: seeded rays of the first
         # eight items, from the items' images (copied back after the timing)
@@ -846,7 +856,7 @@ def bench_batched(args):
             rays = draw_rays(rng, len(w.angles), w.res, 2500)
             host = b.item(k)
             got = host[rays[:, 0], rays[:, 1], rays[:, 2]].astype(np.float64)
-            ref = oracle_rays(dataclasses.replace(w, ds=ds), w.angles, rays)
+            ref = oracle_rays(dataclasses.replace(w, ds=ds), w.angles, rays, integration=args.integration)
             d = np.abs(got - ref)
             worst_rel = max(worst_rel, float(np.max(d / ref)))
             worst_abs = max(worst_abs, float(np.max(d)))
@@ -929,18 +939,18 @@ def ctypes_ptr(t):
 BATCH_METRIC = "Mrays/s on 1 GB300 (64 uneven scenes, one persistent launch per step)"
 
 
-def batched_config(scenes, world):
+def batched_config(scenes, world, integration="simple"):
     return {"workload": f"batched_scenes_{scenes}", "scenes": scenes, "ds": 0.005,
-            "integrator": "simple", "R": 4.0, "fov": 40.0,
+            "integrator": integration, "R": 4.0, "fov": 40.0,
             "scene_definition": "collections of 1-200 seeded primitives, resolution 256/512/1024, "
                                 "8-128 views (seed 4)",
             "l2": "flushed before every timed step (256 MiB write); output > L2",
             "parallelism": f"scenes k mod {world}"}
 
 
-def cpu_baseline_multi(ws, seconds):
+def cpu_baseline_multi(ws, seconds, integration="simple"):
     """The oracle on seeded random rays spread over several scenes."""
-    parts = [cpu_baseline(w, seconds / len(ws))[0] for w in ws]
+    parts = [cpu_baseline(w, seconds / len(ws), integration=integration)[0] for w in ws]
     rays_s = len(ws) / sum(1.0 / p["value"] for p in parts)  # equal rays per scene
     out = dict(parts[0])
     out["value"] = rays_s

@@ -119,13 +119,15 @@ def test_greedy_sum_and_cancellation():
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-@pytest.mark.parametrize("name", ["gyroid", "lattice", "cube", "batched", "coll_defs", "coll_affine"])
+@pytest.mark.parametrize("name", ["gyroid", "gyroid_fine", "lattice", "cube", "batched", "coll_defs", "coll_affine"])
 def test_certificate_tracing(name, integration):
     """Certificate tracing (trace_pixel, the algorithm of k_trace and the
     tracing batch kernel), both integrators, against the FP64 oracle on the
     CPU build."""
     if name == "gyroid":
         w = W.reduced(W.gyroid_sigmoid(), 128, 4)
+    elif name == "gyroid_fine":
+        w = W.reduced(W.gyroid_fine_sigmoid(), 96, 2)
     elif name == "lattice":
         w = W.reduced(W.deformed_lattice(), 128, 3)
     elif name == "cube":
@@ -232,7 +234,7 @@ def _nested_lattice(depth):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
-@pytest.mark.parametrize("name", ["gyroid", "coll_defs", "lattice_gauss"])
+@pytest.mark.parametrize("name", ["gyroid", "gyroid_fine", "coll_defs", "lattice_gauss"])
 def test_curved_ray_tracing(name, integration):
     """Curved-ray certificates (CPU build) for non-affine chains: the traced
     renders match the oracle, with fewer evaluations than ball certificates
@@ -241,6 +243,8 @@ def test_curved_ray_tracing(name, integration):
              "centers": [0.0, 0.1, 0.0]}
     if name == "gyroid":
         w = W.reduced(W.gyroid_sigmoid(), 128, 4)
+    elif name == "gyroid_fine":
+        w = W.reduced(W.gyroid_fine_sigmoid(), 96, 2)
     elif name == "lattice_gauss":
         base = W.reduced(W.deformed_lattice(), 96, 3)
         w = W.Workload("lattice_gauss", base.obj, gauss, base.angles, base.res, base.ds)

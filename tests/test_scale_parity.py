@@ -57,6 +57,14 @@ def gyroid(X):
     s.close()
 
 
+@pytest.fixture(scope="module")
+def gyroid_fine(X):
+    w = W().gyroid_fine_sigmoid()
+    s = X.Scene(w.obj, w.deformation)
+    yield w, s
+    s.close()
+
+
 def _rays(nviews, res, n, seed):
     rng = np.random.default_rng(seed)
     return np.stack([rng.integers(0, nviews, n), rng.integers(0, res, n),
@@ -255,3 +263,33 @@ def test_launch_groups_overlap(X, lattice, march, integration, monkeypatch):
     ref = _oracle(w, angles, rays, integration)
     got = dev[rays[:, 0], rays[:, 1], rays[:, 2]].astype(np.float64)
     _check(got, ref, f"lattice {march} {integration}, overlapped groups")
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+@pytest.mark.parametrize("march", ["plain", "trace", "ball"])
+def test_gyroid_fine_every_march(X, gyroid_fine, march, integration):
+    """The example scene's gyroid (scale 0.1: a lattice of sheets) under the
+    sigmoid deformation, at the benchmarked 2048^2 and ds 0.001, on four of
+    its views: every march and both integrators against the oracle."""
+    w, s = gyroid_fine
+    angles = _subset(w, 4)
+    rays = _rays(len(angles), w.res, 20000, seed=41)
+    out, st = _render(X, s, w, angles, integration=integration, march=march)
+    err = _check(_pick(out, rays, w.res), _oracle(w, angles, rays, integration),
+                 f"fine gyroid {march} {integration}")
+    print(f"\nfine gyroid {march} {integration}: max rel {err:.2e}; counters {st}")
+
+
+def test_certificate_kind_probe(X, gyroid, gyroid_fine):
+    """Calls of at least 2^22 rays over a non-affine chain pick curve or ball
+    certificates from their evaluation counts on a small probe: curves for
+    the scale-8 gyroid (one smooth band), balls for the scale-0.1 one (a
+    lattice of sheets, where a curve evaluation's extra cost does not pay)."""
+    import torch
+    for (w, s), want_ball in ((gyroid, False), (gyroid_fine, True)):
+        angles = w.angles[:1]  # one 2048^2 view: 2^22 rays
+        out = torch.empty((1, w.res, w.res), device="cuda", dtype=torch.float32)
+        kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, out=out, stats=True)
+        _, auto = X.render_proposal(s, None, angles, trace=True, **kw)
+        _, ball = X.render_proposal(s, None, angles, trace="ball", **kw)
+        assert (auto["evaluations"] == ball["evaluations"]) == want_ball, (w.name, auto, ball)

@@ -31,6 +31,10 @@ struct BatchStage {
 // 4 (64 registers). Ray bounds on the 64-scene batch: 4116 Mrays/s with 2
 // blocks, 4591 with 3, 4809 with 4, 4841 with 5; ball certificates: 1678
 // with 3, 1911 with 4 (spills cost less than the lost warps).
+// XRP_BATCH_MERGE: tracing serves the warp's FP64 re-evaluations together.
+#ifndef XRP_BATCH_MERGE
+#define XRP_BATCH_MERGE 1
+#endif
 template <bool HIER, int DEPTH, bool DEFS, int TRACE>
 __global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 4 : XRP_SCENE_MIN_BLOCKS)
     k_batch(const SceneDev* __restrict__ scenes, const BatchItemDev* __restrict__ items, int nitems,
@@ -84,11 +88,14 @@ __global__ void __launch_bounds__(256, (TRACE && DEPTH < 3) ? 4 : XRP_SCENE_MIN_
         const int ty = tt / B.tiles_x, tx = tt - ty * B.tiles_x;
         const int i = ty * th + lane / tw;
         const int j = tx * tw + lane % tw;
+        const unsigned wm = __ballot_sync(0xffffffffu, i < res && j < res);
         if (i < res && j < res) {
             float val;
             if constexpr (TRACE != 0) {
+                // the warp's FP64 re-evaluations served together
                 unsigned ev = 0;
-                val = trace_pixel<HIER, DEPTH, DEFS, TRACE == 2, TRACE == 3>(sg.S, L, sg.P, sg.V, i, j, ev);
+                val = trace_pixel<HIER, DEPTH, DEFS, TRACE == 2, TRACE == 3, XRP_BATCH_MERGE != 0>(
+                    sg.S, L, sg.P, sg.V, i, j, ev, wm);
             } else {
                 RayStats st{0, 0};
                 val = render_pixel<HIER, false, DEPTH, DEFS>(sg.S, L, sg.P, sg.V, i, j, st);

@@ -1892,28 +1892,100 @@ XRP_HD float trace_sum_hier(const SceneDev& S, const Lattice& L, const Ray& ray,
     return acc.s - acc.c;
 }
 
+#if defined(__CUDA_ARCH__)
+// trace_sum with the warp's FP64 re-evaluations served together, as the
+// hierarchical march's MERGE does (XRP_MERGE_LANES, XRP_MERGE_WAIT): a lane
+// holds one undecided sample back and marches on, and a lane that meets a
+// second one waits until the held one is served.  The held value joins the
+// sum when served, so the terms are added in another order.  `wmask`: the
+// lanes calling.
+template <int DEPTH, bool DEFS, bool RAY, bool CURVE = false, int LM = kLeafAll, class Unc>
+__device__ __forceinline__ float trace_sum_merged(const SceneDev& S, const Lattice& L, const Ray& ray, int k0,
+                                                  int k1, Unc&& unc, unsigned& evals, unsigned wmask) {
+    KahanF acc;
+    const float step = L.ds32 * 1.00001f;
+    const float istep = (1.0f / step) * 0.999999f;
+    RayDir u;
+    if constexpr (RAY) u = ray_dir32(S, ray.d32);
+    int k = k0, held = -1, waited = 0;
+    bool stalled = false;
+    for (;;) {
+        const unsigned pm = __ballot_sync(wmask, held >= 0);
+        if (pm == 0u && !__any_sync(wmask, k <= k1)) break;
+        if (pm) {
+            const unsigned busy = __ballot_sync(wmask, k <= k1 && !stalled);
+            if (__popc(pm) >= XRP_MERGE_LANES || busy == 0u || ++waited >= XRP_MERGE_WAIT) {
+                waited = 0;
+                if (held >= 0) {
+                    acc.add(unc(held));  // every holding lane of the warp at once
+                    held = -1;
+                    stalled = false;
+                }
+            }
+        }
+        if (k > k1 || stalled) continue;
+        const float tk = lattice_t(L, k);
+        const float x = fmaf(ray.d32[0], tk, ray.pc[0]);
+        const float y = fmaf(ray.d32[1], tk, ray.pc[1]);
+        const float z = fmaf(ray.d32[2], tk, ray.pc[2]);
+        float m;
+        float rho;
+        if constexpr (RAY) rho = dens_ray32<DEPTH, DEFS>(S, x, y, z, u, (float)(k1 - k + 1) * step, m);
+        else if constexpr (CURVE) rho = dens_curve32<DEPTH, DEFS, LM>(S, x, y, z, ray.d32, m);
+        else rho = dens_margin32<DEPTH, DEFS>(S, x, y, z, m);
+        if (isunc(rho)) {
+            if (held < 0) {
+                held = k;
+                k++;
+                evals++;
+            } else {
+                stalled = true;  // evaluated again once the held sample is served
+            }
+            continue;
+        }
+        evals++;
+        const int jmp = (int)fminf(floorf(m * istep), (float)(k1 - k));
+        acc.add(rho * (float)(jmp + 1));
+        k += jmp + 1;
+    }
+    return acc.s - acc.c;
+}
+#endif
+
 // One pixel by certificate tracing, FP64 for undecided samples in place.
-template <bool HIER, int DEPTH, bool DEFS, bool RAY, bool CURVE = false>
+// MERGE (device): the warp's re-evaluations served together
+// (trace_sum_merged, trace_sum_hier's MERGE); `wmask`: the lanes calling.
+template <bool HIER, int DEPTH, bool DEFS, bool RAY, bool CURVE = false, bool MERGE = false>
 XRP_HD float trace_pixel(const SceneDev& S, const Lattice& L, const RenderParams& P, const ViewDev& V,
-                         int i, int j, unsigned& evals) {
+                         int i, int j, unsigned& evals, unsigned wmask = 0u) {
     Ray r;
     setup_ray_march(V, P, L, i, j, r);
     float t0, t1;
     clip_ray(S.sup_lo, S.sup_hi, r, t0, t1);
     int k0, k1;
     float acc = 0.0f;
-    if (sample_range(L, t0, t1, L.K, k0, k1)) {
+    const bool has = sample_range(L, t0, t1, L.K, k0, k1);
+    unsigned wm = 0u;
+#if defined(__CUDA_ARCH__)
+    if constexpr (MERGE) wm = __ballot_sync(wmask, has);
+#endif
+    (void)wmask;
+    (void)wm;
+    if (has) {
         if constexpr (HIER) {
-            acc = trace_sum_hier<DEPTH, DEFS, RAY, CURVE>(
+            acc = trace_sum_hier<DEPTH, DEFS, RAY, CURVE, kLeafAll, false, MERGE>(
                 S, L, r, k0, k1,
                 [&](int q, bool fine) {
                     return (float)sample64_pixel(S, V, P.xs, i, j, fine ? L.f64[q] : L.s64[q]);
                 },
-                evals);
+                evals, wm);
         } else {
-            acc = trace_sum<DEPTH, DEFS, RAY, CURVE>(
-                S, L, r, k0, k1,
-                [&](int k) { return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[k]); }, evals);
+            auto unc = [&](int k) { return (float)sample64_pixel(S, V, P.xs, i, j, L.s64[k]); };
+#if defined(__CUDA_ARCH__)
+            if constexpr (MERGE) acc = trace_sum_merged<DEPTH, DEFS, RAY, CURVE>(S, L, r, k0, k1, unc, evals, wm);
+            else
+#endif
+                acc = trace_sum<DEPTH, DEFS, RAY, CURVE>(S, L, r, k0, k1, unc, evals);
         }
     }
     float w = HIER ? P.density_multiplier : P.density_multiplier * L.ds32;

@@ -1821,6 +1821,56 @@ void xrp_proposal_destroy(xrp_proposal* p) {
     delete p;
 }
 
+// Curve certificates evaluate fewer samples than balls, but one curve
+// evaluation costs about 4.2 ball evaluations on GB300 (fitted on the two
+// gyroid scenes: scale 8, 7.4 against 44.7 evaluations per ray, curves
+// 2058 against balls 1516 Mrays/s; scale 0.1, 21.4 against 73.2, curves 701
+// against balls 892).  For a call of many rays over a non-affine chain the
+// simple integrator's tracing counts both kinds' evaluations on up to four
+// of the call's views at 64^2 and takes the cheaper: 2 (balls) or 1.
+static int probe_certificate_kind(Engine* E, xrp_scene* s, const std::vector<ViewDev>& v, const xrp_render_opts& o,
+                                  double fov_max, cudaStream_t st, int* kind) {
+    *kind = 1;
+    const int n = std::min<int>(4, (int)v.size());
+    std::vector<ViewDev> pv;
+    for (int q = 0; q < n; q++) pv.push_back(v[(size_t)q * v.size() / n]);
+    xrp_render_opts po = o;
+    po.resolution = 64;
+    PoolBuf img, sb;
+    cudaError_t e;
+    if ((e = img.alloc(E, (size_t)n * 64 * 64 * sizeof(float), st)) != cudaSuccess ||
+        (e = sb.alloc(E, 2 * kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
+        return cuda_fail(3, "certificate probe", e);
+    if ((e = cudaMemsetAsync(sb.p, 0, 2 * kStatCount * sizeof(unsigned long long), st)) != cudaSuccess)
+        return cuda_fail(7, "certificate probe", e);
+    for (int t = 1; t <= 2; t++) {
+        PropLaunch pl;
+        memset(&pl.Q, 0, sizeof(pl.Q));
+        pl.Q.trace = t;
+        pl.Q.mc = 64;
+        pl.Q.stats = (unsigned long long*)sb.p + (t - 1) * kStatCount;
+        PoolBuf fb, fbc;
+        int rc = alloc_fallback_list(E, pl, fb, fbc, st);
+        if (rc) return rc;
+        rc = render_views(E, s->hs, s->vdev, s->v64, pv, po, fov_max, (float*)img.p, false, st, st, false, 0, &pl);
+        if (rc) return rc;
+    }
+    unsigned long long h[2 * kStatCount];
+    if ((e = cudaMemcpyAsync(h, sb.p, sizeof(h), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return cuda_fail(7, "certificate probe", e);
+    const double curve = (double)h[kStatEvaluations], ball = (double)h[kStatCount + kStatEvaluations];
+    if (ball < 4.2 * curve) *kind = 2;
+    return 0;
+}
+
+// Whether the scene's deformation chain has a non-affine step.
+static bool chain_non_affine(const HostScene& hs) {
+    for (const HDef& d : hs.defs)
+        if (d.type != D_LINEAR && d.type != D_AFFINE && d.type != D_RIGID) return true;
+    return false;
+}
+
 static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, const xrp_camera* views,
                            int nviews, const xrp_render_opts* o, float* out, bool out_host, void* stream) {
     if (!s || !views || !o || !out) return fail(1, "null pointer");
@@ -1877,6 +1927,12 @@ static int render_proposal(xrp_scene* s, const xrp_proposal* prop, int segment, 
     int lrc = alloc_fallback_list(E, pl, fb, fbc, st, slots);
     if (lrc) return lrc;
     xrp_render_opts oo = *o;
+    if (pl.Q.trace == 1 && o->integration == XRP_INTEGRATE_SIMPLE && chain_non_affine(s->hs) &&
+        (long long)nviews * o->resolution * o->resolution >= (1LL << 22)) {
+        int kind = 1;
+        if ((lrc = probe_certificate_kind(E, s, v, *o, fov_max, st, &kind))) return lrc;
+        pl.Q.trace = kind;
+    }
     int rc = render_views(E, s->hs, s->vdev, s->v64, v, oo, fov_max, out, out_host, st,
                           out_host ? E->copy : st, false, 0, &pl);
     if (rc) return rc;

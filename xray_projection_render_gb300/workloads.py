@@ -162,6 +162,25 @@ def gyroid_sigmoid(res=2048, views=720) -> Workload:
     return Workload(f"gyroid_sigmoid_{views}x{res}^2", obj, deform, angles, res, 0.001)
 
 
+def gyroid_fine_sigmoid(res=2048, views=64) -> Workload:
+    """The gyroid of the reference's example scene (scale 0.1, thickness 0.2:
+    a period of about 0.63, a lattice of sheets, where scale 8 gives one
+    smooth band) tessellated with unit-cell bounds [-1,1]^3 and outer bounds
+    [-0.8,0.8]^3, under the sigmoid deformation of the scale-8 workload
+    (A 0.1, L 0.2, along z); `views` of its 720 cameras, evenly strided;
+    2048^2; ds 0.001."""
+    obj = {"type": "tessellated_obj_coll",
+           "uc": {"objects": {"type": "object_collection", "objects": [
+               {"type": "gyroid", "center": [0.0, 0.0, 0.0], "scale": 0.1, "thickness": 0.2,
+                "rho": 1.0}]},
+                  "xmin": -1.0, "xmax": 1.0, "ymin": -1.0, "ymax": 1.0, "zmin": -1.0, "zmax": 1.0},
+           "xmin": -0.8, "xmax": 0.8, "ymin": -0.8, "ymax": 0.8, "zmin": -0.8, "zmax": 0.8}
+    deform = {"type": "sigmoid", "amplitude": 0.1, "center": 0.0, "lengthscale": 0.2,
+              "direction": "z"}
+    angles = [(0.5 * k, 90.0) for k in range(0, 720, max(1, 720 // views))][:views]
+    return Workload(f"gyroid_fine_sigmoid_{views}x{res}^2", obj, deform, angles, res, 0.001)
+
+
 def reduced(w: Workload, res: int, views: int | None = None) -> Workload:
     """The same scene at another resolution and/or on an evenly strided
     subset of its views (parity tests, profiling).  The name says so: the
@@ -178,8 +197,9 @@ WORKLOADS = {
     "voxel_blobs": voxel_blobs,
     "deformed_lattice": deformed_lattice,
     "gyroid_sigmoid": gyroid_sigmoid,
+    "gyroid_fine_sigmoid": gyroid_fine_sigmoid,
 }
 
 __all__ = ["Workload", "cube_minus_sphere_cylinder", "gaussian_blob_volume", "voxel_blobs",
            "lattice_unit_cell", "deformed_lattice", "random_scene", "batched_scenes",
-           "gyroid_sigmoid", "reduced", "WORKLOADS", "math"]
+           "gyroid_sigmoid", "gyroid_fine_sigmoid", "reduced", "WORKLOADS", "math"]
