@@ -917,8 +917,11 @@ struct Flattener {
             // cells per axis ~1.6 cbrt(children); tracing a uniform
             // collection uses ~1.2 cbrt: inside a cell the tracer stops at the
             // cell's faces, and fewer, fuller cells cost it less (deformed
-            // lattice, 16 struts: 3 cells per axis 464 Mrays/s, 4 cells 424),
-            // while the plain march pays per candidate (4 cells: 140, 3: 121)
+            // lattice, 16 struts: 3 cells per axis 464 Mrays/s, 4 cells 424;
+            // with the FP64 pass overlapped, 3 cells 523, 2 cells 396, one
+            // 241: coarser cells cut the evaluations only 7-14 % while each
+            // evaluation reads more struts), while the plain march pays per
+            // candidate (4 cells: 140, 3: 121)
             const double gs = (tracing && uniform) ? 1.2 : 1.6;
             int G = (int)std::lround(std::cbrt((double)kids.size()) * gs);
             G = std::max(2, std::min(G, 16));
