@@ -1,7 +1,7 @@
 // xrp_kern_train.cu -- training of the proposal network: the training-row
 // generation march (k_propose with TRAIN), the forward/backward step on the
-// tcgen05 tensor cores (xrp_train_tc.cuh), Adam, and the logits of
-// validation rows.
+// tcgen05 tensor cores (xrp_train_tc.cuh, also the logits of validation
+// rows) and Adam.
 #define XRP_MLP_KERNELS
 #include "xrp_launch.h"
 #include "xrp_train_tc.cuh"
@@ -17,12 +17,7 @@ cudaError_t launch_prop_train(const Prepared& pr, int view0, int nviews, const P
 constexpr size_t kTcSmem = sizeof(TrainTcShared) + 1024;
 
 cudaError_t mlp_kernel_attrs() {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kTcSmem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mlp_logits, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(PropShared));
-    return e;
+    return cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
 }
 
 cudaError_t mlp_train_launch(cudaStream_t st, const float* params, const __nv_bfloat16* X,
@@ -48,13 +43,13 @@ cudaError_t mlp_adam_launch(cudaStream_t st, float* params, float* grad, float* 
     return cudaGetLastError();
 }
 
+// Logits of validation rows: the forward pass of the tcgen05 step.
 cudaError_t mlp_logits_launch(cudaStream_t st, const float* params, const __nv_bfloat16* X, int rows,
                               float* logits) {
-    int tiles = (rows + 31) / 32;
-    int blocks = (tiles + kPropWarps - 1) / kPropWarps;
-    if (blocks > 4096) blocks = 4096;
+    int blocks = (rows + kTcRows - 1) / kTcRows;
     if (blocks <= 0) return cudaSuccess;
-    k_mlp_logits<<<blocks, 32 * kPropWarps, sizeof(PropShared), st>>>(params, X, rows, logits);
+    k_mlp_train_tc<<<blocks, kTcRows, kTcSmem, st>>>(params, X, nullptr, nullptr, rows, 1.0f, 0.0f, nullptr,
+                                                     nullptr, logits);
     return cudaGetLastError();
 }
 

@@ -619,34 +619,7 @@ __global__ void k_prop_finish(float* __restrict__ T, long n) {
 }
 #endif  // XRP_PROP_RENDER_KERNELS
 
-#if defined(XRP_MLP_KERNELS)
-// Logits of `rows` feature rows (validation and tests), 32 rows per warp.
-__global__ void __launch_bounds__(32 * kPropWarps)
-    k_mlp_logits(const float* __restrict__ params, const __nv_bfloat16* __restrict__ X, int rows,
-                 float* __restrict__ logits) {
-    extern __shared__ __align__(16) unsigned char prop_smem[];
-    PropShared& sh = *reinterpret_cast<PropShared*>(prop_smem);
-    load_mlp_shared(params, sh.W);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __nv_bfloat16* xrow = sh.rows[warp];
-    const int tiles = (rows + 31) / 32;
-    for (int tile = blockIdx.x * kPropWarps + warp; tile < tiles; tile += gridDim.x * kPropWarps) {
-        const int r0 = tile * 32;
-        for (int q = lane; q < 32 * kMlpIn / 2; q += 32) {
-            int rr = q / (kMlpIn / 2), cc = q % (kMlpIn / 2);
-            uint32_t v = 0;
-            if (r0 + rr < rows) v = reinterpret_cast<const uint32_t*>(X + (size_t)(r0 + rr) * kMlpIn)[cc];
-            reinterpret_cast<uint32_t*>(xrow + rr * kMlpLd)[cc] = v;
-        }
-        __syncwarp();
-        float l = mlp_forward_warp(sh.W, xrow);
-        __syncwarp();
-        if (r0 + lane < rows) logits[r0 + lane] = l;
-    }
-}
 
-#endif  // XRP_MLP_KERNELS
 
 #endif  // __CUDACC__
 

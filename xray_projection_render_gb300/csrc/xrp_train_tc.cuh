@@ -167,7 +167,8 @@ __device__ unsigned g_mlp_tc_error;
 // X[idx[r]] or X[r]; labels y): adds the gradient of
 // inv_batch * sum_r w_r BCE(sigmoid(logit_r), y_r) (w_r = pos_weight for
 // positive rows, 1 otherwise) to `grad` and the loss to `loss`; optionally
-// writes the logits.
+// writes the logits.  With `grad` null only the forward pass runs (the
+// logits of validation rows; y and loss unused).
 __global__ void __launch_bounds__(kTcRows, 1)
     k_mlp_train_tc(const float* __restrict__ params, const __nv_bfloat16* __restrict__ X,
                    const float* __restrict__ y, const int* __restrict__ idx, int rows, float pos_weight,
@@ -281,6 +282,7 @@ __global__ void __launch_bounds__(kTcRows, 1)
         tc_store_col(S.z2t, t, acc);
         product(S.z2, 64 * 16, S.w[2], 64 * 16, 4);
     }
+    float dlog = 0.0f;  // d loss / d logit
     if (ok) {
         tc_load_row(tmem, acc);
         // head: z3 = relu(acc + b3) in FP32, logit, loss, dlogit
@@ -290,16 +292,18 @@ __global__ void __launch_bounds__(kTcRows, 1)
             acc[c] = fmaxf(acc[c] + S.b[2][c], 0.0f);
             logit = fmaf(acc[c], S.w4[c], logit);
         }
+        if (logits_out && valid) logits_out[row] = logit;
         float yy = 0.0f, ww = 0.0f;
-        if (valid) {
+        if (valid && grad) {
             yy = y[idx ? idx[row] : row];
             ww = yy > 0.5f ? pos_weight : 1.0f;
         }
         const float sp = fmaxf(logit, 0.0f) + log1pf(expf(-fabsf(logit)));
         const float sg = 1.0f / (1.0f + expf(-logit));
-        const float dlog = ww * (sg - yy) * inv_batch;
+        dlog = ww * (sg - yy) * inv_batch;
         atomicAdd(&S.loss, ww * (sp - yy * logit) * inv_batch);
-        if (logits_out && valid) logits_out[row] = logit;
+    }
+    if (ok && grad) {
         {
             float s = dlog;
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(kTcRows, 1)
     // dZ_{l-1} = (dZ_l W_l) relu'(Z_{l-1})
     const __nv_bfloat16* zprev[2] = {S.z2, S.z1};  // Z_{l-1} rows for l = 3, 2
     const __nv_bfloat16* zprevt[2] = {S.z1t, S.xt};
-    for (int l = 0; l < 2 && ok; l++) {
+    for (int l = 0; l < 2 && ok && grad; l++) {
         tc_load_row(tmem, acc);  // dW of layer 3 - l in lanes 0..63
         if (t < 64) {
             float* gw = grad + (l == 0 ? MlpLayout::W3 : MlpLayout::W2) + t * 64;
@@ -342,20 +346,20 @@ __global__ void __launch_bounds__(kTcRows, 1)
         tc_store_col(S.dzt, t, acc);
         product(S.dzt, kTcRows * 16, zprevt[l], kTcRows * 16, 8);  // dW of layer 2 - l
     }
-    if (ok) {
+    if (ok && grad) {
         tc_load_row(tmem, acc);  // dW1 in lanes 0..63
         if (t < 64) {
             float* gw = grad + MlpLayout::W1 + t * 64;
 #pragma unroll
             for (int c = 0; c < 64; c++) atomicAdd(&gw[c], acc[c]);
         }
-    } else if (t == 0) {
+    } else if (!ok && t == 0) {
         atomicOr(&g_mlp_tc_error, 1u);
         tc_wait(mbar, phase, kTcPolls);  // a product still in flight, if any
     }
     tc_fence_before();
     __syncthreads();
-    if (t == 0) atomicAdd(loss, S.loss);
+    if (t == 0 && loss) atomicAdd(loss, S.loss);
     if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
