@@ -64,6 +64,25 @@ def margin(obj, points, *, deformation=None, R=4.0, fov=40.0, ds=0.01, fused=Fal
     return (rho, m, rho2, m2) if fused else (rho, m)
 
 
+def density64(obj, points, *, deformation=None):
+    """The engine's FP64 densities at FP64 points [n,3]: (every primitive in
+    FP64, the FP64 pass's hybrid evaluator)."""
+    import ctypes as C
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    n = pts.shape[0]
+    a, b = np.zeros(n), np.zeros(n)
+    L = lib()
+    L.hs_density64.restype = C.c_int
+    L.hs_density64.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p,
+                               C.c_char_p, C.c_int]
+    err = C.create_string_buffer(512)
+    rc = L.hs_density64(json.dumps(obj).encode(), json.dumps(deformation).encode() if deformation else None,
+                        pts.ctypes.data, n, a.ctypes.data, b.ctypes.data, err, 512)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return a, b
+
+
 def ray_bound(obj, points, dirs, *, deformation=None, R=4.0, fov=40.0, ds=0.01):
     """Ray evaluator at points [n,3] along world directions [n,3]: (density,
     ray bound t, affine).  Every sample at parameter s in [0, t] must have

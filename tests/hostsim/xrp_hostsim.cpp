@@ -164,6 +164,39 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
     }
 }
 
+// The FP64 densities of the engine's two FP64 evaluators at FP64 points
+// (density64: every primitive in FP64; density_hyb: the FP64 pass's, FP32
+// decisions where they are certain), for the exactness test against the
+// oracle.
+extern "C" __attribute__((visibility("default"))) int hs_density64(
+    const char* obj_json, const char* def_json, const double* pts, long n, double* d64_out, double* hyb_out,
+    char* err, int errlen) {
+    try {
+        HostScene hs = load_scene(obj_json, def_json, {});
+        HostPrepared hp = prepare_host(hs, 8, 0, 0.01, 4.0, 0.0, 1.0, 40.0);
+        SceneDev S = hp.S;
+        S.nodes = hp.fs.nodes.data();
+        S.nodes64 = hp.fs.nodes64.data();
+        S.child = hp.fs.child.data();
+        S.cells = hp.fs.cells.data();
+        S.items = hp.fs.items.data();
+        S.clear = hp.fs.clear.data();
+        S.defs = hp.fs.defs.data();
+        S.vols = hp.vols.data();
+        for (long q = 0; q < n; q++) {
+            d64_out[q] = density64(S, pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+            hyb_out[q] = density_hyb(S, pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]);
+        }
+        return 0;
+    } catch (const std::exception& ex) {
+        if (err && errlen > 0) {
+            strncpy(err, ex.what(), errlen - 1);
+            err[errlen - 1] = 0;
+        }
+        return 2;
+    }
+}
+
 // FP32 march rays of the listed pixels by the two setups (double-float FP32
 // and FP64): out[q] = pc[3], d32[3] of each, for the equality test of the
 // double-float arithmetic.

@@ -274,3 +274,35 @@ def test_tracing_nested_tessellations(depth, integration):
         check(w, integration, nrays=1500, trace=True)
         if deform["type"] == "gaussian":
             check(w, integration, nrays=1500, trace="curve")
+
+
+def test_fp64_evaluators_exact_at_cylinder_surfaces():
+    """The FP64 evaluators (every primitive in FP64, and the FP64 pass's
+    hybrid, which decides primitives in FP32 where that is certain and tests
+    a cylinder's radius against a threshold precomputed on the host instead
+    of taking the square root) equal the oracle exactly at points within
+    1e-15 to 1e-6 of the deformed lattice's strut surfaces."""
+    w = W.deformed_lattice()
+    rng = np.random.default_rng(17)
+    cell = W.lattice_unit_cell()
+    struts = [o for o in cell["objects"]["objects"]] if "objects" in cell.get("objects", {}) else cell["objects"]
+    pts = []
+    for _ in range(3000):
+        c = struts[rng.integers(len(struts))]
+        p0, p1, r = np.array(c["p0"]), np.array(c["p1"]), c["radius"]
+        v = p1 - p0
+        t = rng.uniform(-0.05, 1.05)
+        nrm = np.cross(v, rng.normal(size=3))
+        nrm /= np.linalg.norm(nrm)
+        off = rng.choice([-1, 1]) * 10.0 ** rng.uniform(-15, -6)
+        q = p0 + t * v + (r + off) * nrm  # object space, near the strut's side
+        q += 0.2 * rng.integers(-5, 5, size=3)  # some tessellation cell
+        # back to world space through the linear strain (z scaled by 1.05)
+        pts.append([q[0], q[1], q[2] / 1.05])
+    pts = np.array(pts)
+    d64, hyb = hostsim.density64(w.obj, pts, deformation=w.deformation)
+    sc = O.Scene(w.obj, w.deformation)
+    ref = np.array([sc.density(*p) for p in pts])
+    assert np.array_equal(d64, ref)
+    assert np.array_equal(hyb, ref)
+    assert 0 < np.count_nonzero(ref) < len(ref)

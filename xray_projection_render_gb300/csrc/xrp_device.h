@@ -883,16 +883,18 @@ XRP_HD double ppd64(const double* d, double x, double y, double z) {
     return 0.0;
 }
 
+// Cylinder::Density (objects.go:334-350) in the reference's operation order.
+// The per-cylinder terms come from the host, formed by the same operations:
+// d[8..10] = p1 - p0, d[11] = |p1 - p0|^2, and d[12] = T with
+// sqrt(s) < r exactly when s < T, so the square root is not taken.
 XRP_HD double cyl64(const double* d, double x, double y, double z) {
-    double vx = dsub(d[3], d[0]), vy = dsub(d[4], d[1]), vz = dsub(d[5], d[2]);
+    const double vx = d[8], vy = d[9], vz = d[10];
     double wx = dsub(x, d[0]), wy = dsub(y, d[1]), wz = dsub(z, d[2]);
     double wv = dadd(dadd(dmul(wx, vx), dmul(wy, vy)), dmul(wz, vz));
-    double vv = dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz));
-    double c = ddiv(wv, vv);
+    double c = ddiv(wv, d[11]);
     if (c < 0.0 || c > 1.0) return 0.0;
     double dx = dsub(wx, dmul(vx, c)), dy = dsub(wy, dmul(vy, c)), dz = dsub(wz, dmul(vz, c));
-    double dd = dsqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)));
-    if (dd < d[6]) return d[7];
+    if (dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)) < d[12]) return d[7];
     return 0.0;
 }
 
@@ -1072,10 +1074,15 @@ XRP_HD double leaf_rho64(const SceneDev& S, int id) {
     }
 }
 
-XRP_HD double leaf_hyb(const SceneDev& S, int id, double x, double y, double z) {
-    float r = leaf32(S.nodes[id], (float)x, (float)y, (float)z);
+// (xf, yf, zf): the point rounded to FP32, formed once per collection.
+XRP_HD double leaf_hyb(const SceneDev& S, int id, double x, double y, double z, float xf, float yf, float zf) {
+    float r = leaf32(S.nodes[id], xf, yf, zf);
     if (!isunc(r)) return r != 0.0f ? leaf_rho64(S, id) : 0.0;
     return leaf64(S, id, x, y, z);
+}
+
+XRP_HD double leaf_hyb(const SceneDev& S, int id, double x, double y, double z) {
+    return leaf_hyb(S, id, x, y, z, (float)x, (float)y, (float)z);
 }
 
 template <int D>
@@ -1128,11 +1135,12 @@ XRP_HD double coll_hyb(const SceneDev& S, int id, double x, double y, double z) 
     const int32_t* kids = S.child + c.a;
     int cnt = c.b;
     const int32_t* list = nullptr;
+    const float xf = (float)x, yf = (float)y, zf = (float)z;
     if (c.flags & C_ACCEL) {
         int G = (c.flags >> 16) & 0xff;
-        int ix = (int)floorf(((float)x - c.f[0]) * c.f[3]);
-        int iy = (int)floorf(((float)y - c.f[1]) * c.f[4]);
-        int iz = (int)floorf(((float)z - c.f[2]) * c.f[5]);
+        int ix = (int)floorf((xf - c.f[0]) * c.f[3]);
+        int iy = (int)floorf((yf - c.f[1]) * c.f[4]);
+        int iz = (int)floorf((zf - c.f[2]) * c.f[5]);
         ix = ix < 0 ? 0 : (ix >= G ? G - 1 : ix);
         iy = iy < 0 ? 0 : (iy >= G ? G - 1 : iy);
         iz = iz < 0 ? 0 : (iz >= G ? G - 1 : iz);
@@ -1143,8 +1151,9 @@ XRP_HD double coll_hyb(const SceneDev& S, int id, double x, double y, double z) 
     const bool greedy = (c.flags & C_GREEDY) != 0;
     double density = 0.0;
     for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
-        double rho = item_hyb<D>(S, kids[slot], x, y, z);
+        const int kid = kids[list ? list[k] : k];
+        const double rho = S.nodes[kid].type <= N_GYROID ? leaf_hyb(S, kid, x, y, z, xf, yf, zf)
+                                                         : item_hyb<D>(S, kid, x, y, z);
         if (greedy && rho > 0.0) return rho;
         density = dadd(density, rho);
     }

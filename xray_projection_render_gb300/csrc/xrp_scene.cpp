@@ -11,6 +11,19 @@ namespace xrp {
 
 static const double kU = 5.9604644775390625e-08;  // 2^-24, FP32 unit roundoff
 static const double kSafety = 2.0;
+
+// T such that, for every double s, sqrt(s) < r exactly when s < T, with
+// sqrt correctly rounded (as the host's and the device's __dsqrt_rn are):
+// the smallest s whose square root rounds to r or above (sqrt is monotonic).
+static double sqrt_lt_threshold(double r) {
+    if (std::isnan(r) || std::isinf(r)) return r;
+    if (!(r > 0.0)) return 0.0;  // sqrt(s) < r never holds for s >= 0
+    double s = r * r;
+    if (std::isinf(s)) s = std::numeric_limits<double>::max();
+    while (s > 0.0 && std::sqrt(s) >= r) s = std::nextafter(s, 0.0);
+    while (std::sqrt(s) < r) s = std::nextafter(s, std::numeric_limits<double>::infinity());
+    return s;
+}
 static const double kInf = std::numeric_limits<double>::infinity();
 
 // ---------------------------------------------------------------------------
@@ -674,6 +687,12 @@ struct Flattener {
             }
             n.f[6] = (float)(1.0 / vv);
             n.f[7] = (float)(r * r);
+            // the FP64 test's per-cylinder terms, formed as the device would
+            // form them (same operations, no contraction): the axis, its
+            // squared length, and the threshold of its radius test
+            for (int a = 0; a < 3; a++) n64.d[8 + a] = d[3 + a] - d[a];
+            n64.d[11] = (n64.d[8] * n64.d[8] + n64.d[9] * n64.d[9]) + n64.d[10] * n64.d[10];
+            n64.d[12] = sqrt_lt_threshold(d[6]);
             n.f[8] = (float)r;   // certificate radii: radius and axis length
             n.f[9] = (float)vl;
             n.f[F_BAND2] = (float)(kSafety * band_c);
