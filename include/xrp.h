@@ -269,7 +269,8 @@ XRP_API int xrp_batch_render(xrp_batch* batch, void* stream);
  * xrp_batch_item_offset(batch, k) floats. */
 XRP_API const float* xrp_batch_output(const xrp_batch* batch);
 XRP_API long long xrp_batch_item_offset(const xrp_batch* batch, int k);
-/* Copies item k's images to host memory (synchronous). */
+/* Copies item k's images to host memory (synchronous; ordered after the
+ * last xrp_batch_render, whatever its stream). */
 XRP_API int xrp_batch_copy_item(const xrp_batch* batch, int k, float* out_host);
 XRP_API int xrp_batch_get_info(const xrp_batch* batch, xrp_batch_info* out);
 XRP_API void xrp_batch_destroy(xrp_batch* batch);

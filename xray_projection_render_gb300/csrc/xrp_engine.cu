@@ -1177,6 +1177,7 @@ struct xrp_batch {
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    cudaEvent_t rendered = nullptr;  // recorded after each replay, on its stream
     xrp_batch_info info;
 };
 
@@ -1192,6 +1193,7 @@ static void batch_free(xrp_batch* b) {
         else cudaFree(b->out);
     }
     if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->rendered) cudaEventDestroy(b->rendered);
     delete b;
 }
 
@@ -1347,7 +1349,8 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
         B->offset[order[q]] = out0[q];
         B->size[order[q]] = (long long)items[order[q]].num_views * items[order[q]].resolution * items[order[q]].resolution;
     }
-    if ((e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking)) != cudaSuccess)
+    if ((e = cudaStreamCreateWithFlags(&B->cap, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&B->rendered, cudaEventDisableTiming)) != cudaSuccess)
         return cuda_fail(3, "batch stream", e);
     // the images come from the engine's pool: memory released by an earlier
     // batch is reused already mapped (copies out of freshly mapped device
@@ -1463,6 +1466,7 @@ int xrp_batch_create(const xrp_batch_item* items, int n, const xrp_render_opts* 
 int xrp_batch_render(xrp_batch* b, void* stream) {
     if (!b) return fail(1, "null pointer");
     cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->rendered, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(7, "graph launch", e);
     return 0;
 }
@@ -1474,11 +1478,16 @@ long long xrp_batch_item_offset(const xrp_batch* b, int k) {
     return b->offset[k];
 }
 
+// A copy on the batch's own stream, ordered after the last replay by its
+// event (whatever stream the replay ran on), then a wait for that stream.
 int xrp_batch_copy_item(const xrp_batch* b, int k, float* out_host) {
     if (!b || !out_host) return fail(1, "null pointer");
     if (k < 0 || k >= (int)b->offset.size()) return fail(2, "item %d out of range", k);
-    cudaError_t e = cudaMemcpy(out_host, b->out + b->offset[k], (size_t)b->size[k] * sizeof(float),
-                               cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaStreamWaitEvent(b->cap, b->rendered, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out_host, b->out + b->offset[k], (size_t)b->size[k] * sizeof(float),
+                            cudaMemcpyDeviceToHost, b->cap);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->cap);
     if (e != cudaSuccess) return cuda_fail(8, "batch copy", e);
     return 0;
 }
