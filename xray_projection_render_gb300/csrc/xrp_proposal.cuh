@@ -475,7 +475,9 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 #ifndef XRP_PLAIN_MIN_BLOCKS
 #define XRP_PLAIN_MIN_BLOCKS 4
 #endif
-// Resident blocks per SM of the hierarchical integrator (depth < 3).
+// Resident blocks per SM of the hierarchical integrator (depth < 3; three
+// blocks measured slower: lattice 87 / plain 60 / gyroid 394 against
+// 92 / 66 / 418 Mrays/s).
 #ifndef XRP_HIER_MIN_BLOCKS
 #define XRP_HIER_MIN_BLOCKS 4
 #endif
