@@ -108,6 +108,29 @@ def test_plain_fp64_list_matches_inplace(X, name, integration):
     _compare(a, ref)
 
 
+@pytest.mark.parametrize("res", [97, 33])
+def test_merged_fp64_on_partial_warps(X, res):
+    """Odd image sizes leave lanes of the edge tiles outside the image: the
+    warp-merged FP64 re-evaluations (hierarchical tracing, the traced batch)
+    ballot over the lanes that march only.  Both match the oracle."""
+    w = W().reduced(W().deformed_lattice(), res, 2)
+    g = W().reduced(W().gyroid_sigmoid(), res, 2)
+    kw = dict(resolution=res, ds=w.ds, R=w.R, fov=w.fov)
+    with X.Scene(w.obj, w.deformation) as s, X.Scene(g.obj, g.deformation) as sg:
+        hier = X.render_proposal(s, None, w.angles, trace=True, integration="hierarchical", **kw)
+        hier_g = X.render_proposal(sg, None, g.angles, trace=True, integration="hierarchical",
+                                   resolution=res, ds=g.ds, R=g.R, fov=g.fov)
+        with X.Batch([(s, w.angles, res), (sg, g.angles, res)], ds=w.ds, trace=True) as b:
+            b.render()
+            batch_l, batch_g = b.item(0), b.item(1)
+    _compare(hier, O.render(O.Scene(w.obj, w.deformation), w.angles, res, w.ds, R=w.R, fov=w.fov,
+                            integration="hierarchical"))
+    _compare(hier_g, O.render(O.Scene(g.obj, g.deformation), g.angles, res, g.ds, R=g.R, fov=g.fov,
+                              integration="hierarchical"))
+    _compare(batch_l, O.render(O.Scene(w.obj, w.deformation), w.angles, res, w.ds, R=w.R, fov=w.fov))
+    _compare(batch_g, O.render(O.Scene(g.obj, g.deformation), g.angles, res, w.ds, R=g.R, fov=g.fov))
+
+
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 def test_fp64_list_overflow_paths(X, integration, monkeypatch):
     """A 16-entry FP64 list (the XRP_FALLBACK_LIST test hook) overflows on
