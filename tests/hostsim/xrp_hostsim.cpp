@@ -164,6 +164,11 @@ extern "C" __attribute__((visibility("default"))) int hs_margin(
     }
 }
 
+// sqrt_lt_threshold for each of n radii.
+extern "C" __attribute__((visibility("default"))) void hs_sqrt_threshold(const double* r, long n, double* out) {
+    for (long q = 0; q < n; q++) out[q] = sqrt_lt_threshold(r[q]);
+}
+
 // The FP64 densities of the engine's two FP64 evaluators at FP64 points
 // (density64: every primitive in FP64; density_hyb: the FP64 pass's, FP32
 // decisions where they are certain), for the exactness test against the

@@ -306,3 +306,27 @@ def test_fp64_evaluators_exact_at_cylinder_surfaces():
     assert np.array_equal(d64, ref)
     assert np.array_equal(hyb, ref)
     assert 0 < np.count_nonzero(ref) < len(ref)
+
+
+def test_sqrt_threshold_is_exact():
+    """The FP64 cylinder test compares the squared distance s with T instead
+    of sqrt(s) with the radius r: T is the smallest double whose correctly
+    rounded square root reaches r, so sqrt(s) < r exactly when s < T
+    (checked at T and its neighbours, for radii over many decades and the
+    special values)."""
+    import ctypes as C
+    rng = np.random.default_rng(5)
+    r = np.concatenate([10.0 ** rng.uniform(-6, 3, 20000), [0.03, 0.1, 1.0, 2.0, 0.0, -1.0, np.inf]])
+    T = np.zeros_like(r)
+    L = hostsim.lib()
+    L.hs_sqrt_threshold.restype = None
+    L.hs_sqrt_threshold.argtypes = [C.c_void_p, C.c_long, C.c_void_p]
+    L.hs_sqrt_threshold(r.ctypes.data, len(r), T.ctypes.data)
+    fin = np.isfinite(r) & (r > 0)
+    below = np.nextafter(T[fin], 0.0)
+    assert np.all(np.sqrt(T[fin]) >= r[fin])
+    assert np.all(np.sqrt(below) < r[fin])
+    assert np.all(T[~fin][:2] == 0.0) and T[-1] == np.inf
+    # and the equivalence on random squared distances near r^2
+    s = (r[fin] ** 2)[:, None] * (1.0 + rng.uniform(-1e-12, 1e-12, (fin.sum(), 8)))
+    assert np.array_equal(np.sqrt(s) < r[fin][:, None], s < T[fin][:, None])

@@ -12,10 +12,9 @@ namespace xrp {
 static const double kU = 5.9604644775390625e-08;  // 2^-24, FP32 unit roundoff
 static const double kSafety = 2.0;
 
-// T such that, for every double s, sqrt(s) < r exactly when s < T, with
-// sqrt correctly rounded (as the host's and the device's __dsqrt_rn are):
-// the smallest s whose square root rounds to r or above (sqrt is monotonic).
-static double sqrt_lt_threshold(double r) {
+// The smallest s whose correctly rounded square root reaches r (sqrt is
+// monotonic, so sqrt(s) < r exactly when s < it).
+double sqrt_lt_threshold(double r) {
     if (std::isnan(r) || std::isinf(r)) return r;
     if (!(r > 0.0)) return 0.0;  // sqrt(s) < r never holds for s >= 0
     double s = r * r;

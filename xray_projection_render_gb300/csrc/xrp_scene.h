@@ -61,6 +61,12 @@ HostScene volume_scene(const float* data_dev, int nx, int ny, int nz);
 // MinFeatureSize of the root object (the Object interface, objects.go:17).
 double min_feature_size(const HostScene& hs);
 
+// T such that, for every double s, sqrt(s) < r exactly when s < T, with
+// sqrt correctly rounded (as the host's std::sqrt and the device's
+// __dsqrt_rn are): the FP64 cylinder test compares with T instead of taking
+// the square root.
+double sqrt_lt_threshold(double r);
+
 // Inputs of the error analysis that are fixed per render call.
 struct RenderGeometry {
     double R = 4.0;        // camera distance
