@@ -471,6 +471,10 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 #ifndef XRP_TRACE_TILE_W
 #define XRP_TRACE_TILE_W 8
 #endif
+// The plain mode reads the node table from shared memory (1) or through L1.
+#ifndef XRP_PLAIN_SMEM_NODES
+#define XRP_PLAIN_SMEM_NODES 1
+#endif
 // Resident blocks per SM of the plain mode (depth < 3; three blocks ran
 // 151 against 159 Mrays/s on the lattice, five 161 against 168, gyroid
 // 106 against 112).
@@ -513,7 +517,7 @@ __global__ void __launch_bounds__(256, DEPTH >= 3 ? 2
     // FP64 re-evaluation keeps the global table
     extern __shared__ __align__(16) unsigned char trace_smem[];
     SceneDev Sl = S;
-    if (S.nnodes > 0) {
+    if (S.nnodes > 0 && (!PLAIN || XRP_PLAIN_SMEM_NODES)) {
         const int4* src = reinterpret_cast<const int4*>(S.nodes);
         int4* dst = reinterpret_cast<int4*>(trace_smem);
         for (int q = threadIdx.x; q < S.nnodes * (int)(sizeof(Node) / sizeof(int4)); q += blockDim.x)
