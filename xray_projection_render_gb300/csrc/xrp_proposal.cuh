@@ -471,7 +471,8 @@ __global__ void __launch_bounds__(32 * kPropWarps, 2)
 #ifndef XRP_TRACE_TILE_W
 #define XRP_TRACE_TILE_W 8
 #endif
-// The plain mode reads the node table from shared memory (1) or through L1.
+// The plain mode reads the node table from shared memory (1) or through L1
+// (0: lattice 164.6 against 167.8 Mrays/s, gyroid 109.3 against 111.8).
 #ifndef XRP_PLAIN_SMEM_NODES
 #define XRP_PLAIN_SMEM_NODES 1
 #endif
