@@ -763,7 +763,12 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     int max_views_per_launch = std::max(1, (int)(0x7fffffffL / tpv));
     if (pl) max_views_per_launch = std::max(1, std::min<int>(max_views_per_launch, (int)(pl->max_rays / (long long)img)));
     // two list slots: each launch group's FP64 pass beside the next march
+    // (the side stream and its events live for this call only)
     OverlapEvents ovl;
+    if (pl) {
+        pl->side = nullptr;
+        pl->groups = 0;
+    }
     if (pl && !pl->train && pl->fb_slot[1] && nviews > max_views_per_launch && overlap_enabled()) {
         pl->groups = 0;
         if ((e = ovl.create(*pl, E->side)) != cudaSuccess) return cuda_fail(7, "overlap events", e);
