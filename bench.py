@@ -458,19 +458,34 @@ def scene_step(X, scene, w, angles, march, out, stream, prop=None, volume_path="
                                      trace=trace, out=out, stream=stream, **kw)
 
 
-def launches_per_step(march, rays, voxel, integration="simple", plain_fp64="auto"):
+def non_affine(deformation):
+    """Whether a deformation map has a step that is not affine."""
+    if not deformation:
+        return False
+    steps = deformation.get("deformations", [deformation]) if deformation.get("type") == "composed" \
+        else [deformation]
+    return any(non_affine(d) if d.get("type") == "composed" else d.get("type") in ("gaussian", "sigmoid")
+               for d in steps)
+
+
+def launches_per_step(march, rays, voxel, integration="simple", plain_fp64="auto", probe=False):
     """Kernels one step launches: one render launch for a voxel-grid root
     and for the plain integrator re-evaluating in place (below 2^22 rays a
     call unless told otherwise); otherwise, per launch group of at most 8 M
     rays (2 M for the hierarchical integrator), the march, its FP64 pass and
     the exp pass, and for the plain integrator the re-march of rays that
-    found the FP64 list full."""
+    found the FP64 list full.  `probe`: tracing over a non-affine chain,
+    whose calls of 2^22 rays or more first render two small probes (three
+    launches each) to pick the certificate kind."""
     if voxel:
         return 1
     if march == "plain" and (plain_fp64 == "inplace" or (plain_fp64 == "auto" and rays < (1 << 22))):
         return 1
     group = 1 << (21 if integration == "hierarchical" else 23)
-    return (4 if march == "plain" else 3) * -(-rays // group)
+    n = (4 if march == "plain" else 3) * -(-rays // group)
+    if probe and march == "trace" and integration == "simple" and rays >= (1 << 22):
+        n += 6
+    return n
 
 
 def time_path(X, torch, scene, w, angles, march, stream, flush, steps, prop=None, err_rays=4000):
@@ -483,7 +498,8 @@ def time_path(X, torch, scene, w, angles, march, stream, flush, steps, prop=None
     t = _event_time(torch, step, steps, stream, flush)
     rec = {"value": len(angles) * w.res * w.res / t / 1e6, "unit": "Mrays/s", "views": len(angles),
            "res": w.res, "steps": steps, "ms_per_step": t * 1e3, "path": MARCH_PATHS[march],
-           "gpu_launches_per_step": launches_per_step(march, len(angles) * w.res * w.res, False)}
+           "gpu_launches_per_step": launches_per_step(march, len(angles) * w.res * w.res, False,
+                                                      probe=non_affine(w.deformation))}
     rng = np.random.default_rng(4321)
     rays = draw_rays(rng, len(angles), w.res, err_rays)
     wa = dataclasses.replace(w, angles=angles)
@@ -701,7 +717,7 @@ def bench_scene(args):
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(n_my * img * 4), "path": path},
         "gpu_launches": args.steps * launches_per_step(march, n_my * img, is_voxel, args.integration,
-                                                       args.plain_fp64),
+                                                       args.plain_fp64, non_affine(w.deformation)),
         "roofline": dict(roof, **{
             "traffic": traffic * n_my if traffic else None,
             "traffic_note": ("constant: DRAM bytes per view from an ncu capture of the same kernel "
