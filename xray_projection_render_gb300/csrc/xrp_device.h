@@ -39,6 +39,7 @@ XRP_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
 XRP_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
 XRP_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
 XRP_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+XRP_HD double drcp(double a) { return __drcp_rn(a); }  // 1.0 / a, correctly rounded as the division
 XRP_HD double dsqrt(double a) { return __dsqrt_rn(a); }
 XRP_HD float f_exp(float x) { return __expf(x); }
 XRP_HD float f_rcp(float x) { return __frcp_rn(x); }
@@ -47,6 +48,7 @@ XRP_HD double dadd(double a, double b) { return a + b; }
 XRP_HD double dsub(double a, double b) { return a - b; }
 XRP_HD double dmul(double a, double b) { return a * b; }
 XRP_HD double ddiv(double a, double b) { return a / b; }
+XRP_HD double drcp(double a) { return 1.0 / a; }
 XRP_HD double dsqrt(double a) { return sqrt(a); }
 XRP_HD float f_exp(float x) { return expf(x); }
 XRP_HD float f_rcp(float x) { return 1.0f / x; }
@@ -909,9 +911,10 @@ XRP_HD double gyroid64(const double* d, double x, double y, double z) {
 
 XRP_HD double voxel64(const Volume& V, double x, double y, double z) {
     if (x < -1 || x > 1 || y < -1 || y > 1 || z < -1 || z > 1) return 0.0;
-    x = ddiv(dadd(x, 1.0), 2.0);
-    y = ddiv(dadd(y, 1.0), 2.0);
-    z = ddiv(dadd(z, 1.0), 2.0);
+    // (v + 1) / 2: halving is exact, so the product by 0.5 is the quotient
+    x = dmul(dadd(x, 1.0), 0.5);
+    y = dmul(dadd(y, 1.0), 0.5);
+    z = dmul(dadd(z, 1.0), 0.5);
     x = dmul(x, (double)(V.nx - 1));
     y = dmul(y, (double)(V.ny - 1));
     z = dmul(z, (double)(V.nz - 1));
@@ -1205,12 +1208,12 @@ XRP_HD void setup_ray64(const ViewDev& V, const double* xs, int i, int j, Ray64&
     double iw = V.inv_w;
     if (V.general_w) {
         double t3 = dadd(dadd(dadd(dmul(m[3], v0), dmul(m[7], v1)), dmul(m[11], v2)), dmul(m[15], 1.0));
-        iw = ddiv(1.0, t3);
+        iw = drcp(t3);
     }
     double dx = dsub(dmul(t0, iw), V.eye[0]);
     double dy = dsub(dmul(t1, iw), V.eye[1]);
     double dz = dsub(dmul(t2, iw), V.eye[2]);
-    double l = ddiv(1.0, dsqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz))));
+    double l = drcp(dsqrt(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz))));
     r.d[0] = dmul(dx, l);
     r.d[1] = dmul(dy, l);
     r.d[2] = dmul(dz, l);
