@@ -223,9 +223,12 @@ def test_trained_proposal_is_exact_and_routes(X, gyroid_trained):
     for im in (img, ref_only, dense_only):
         assert np.max(np.abs(im - ref) / ref) <= REL_TOL
     assert st["mlp_rounds"] > 0 and st["routed_dense"] + st["subdivided"] > 0
-    # against integrating every uncertified segment densely, the proposal
-    # (network + refinement) evaluates fewer samples
-    assert _work(st) < _work(st_d)
+    # the network's routing against the two fixed policies: far less work
+    # than integrating every uncertified segment densely, and within 5 % of
+    # refining every one (which it does not beat: the certificates already
+    # settle what it could skip; measured 1.3 % above)
+    assert _work(st) < 0.5 * _work(st_d)
+    assert _work(st) <= 1.05 * _work(st_r)
     print(f"\nwork: proposal {_work(st)}, refinement only {_work(st_r)}, dense only {_work(st_d)}"
           f"\nproposal {st}\ninfo {info}")
 
