@@ -420,9 +420,8 @@ XRP_HD float coll_dc(const SceneDev& S, const Node& c, float x, float y, float z
     // bounds the curve (see coll_dr_uniform)
     const bool uniform = (c.flags & C_UNIFORM) != 0;
     for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
         float tk;
-        float r = item_dc<D, LM>(S, kids[slot], x, y, z, u, tk);
+        float r = item_dc<D, LM>(S, list ? list[k] : kids[k], x, y, z, u, tk);
         if (uniform && !unc && r > 0.0f) {
             t = tk;
             return r;

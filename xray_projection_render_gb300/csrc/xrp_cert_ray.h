@@ -409,9 +409,8 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
 XRP_HD float coll_dr_uniform(const SceneDev& S, const int32_t* kids, const int32_t* list, int cnt, float x,
                              float y, float z, const RayDir& u, float tcap, float& t) {
     for (int k = 0; k < cnt; k++) {
-        const int slot = list ? list[k] : k;
         float tk;
-        const float r = leaf_dr(S.nodes[kids[slot]], x, y, z, u, tcap, tk);
+        const float r = leaf_dr(S.nodes[list ? list[k] : kids[k]], x, y, z, u, tcap, tk);
         if (isunc(r)) {  // an undecided child before any certain one
             t = 0.0f;
             return r;
@@ -477,9 +476,8 @@ XRP_HD float coll_dr(const SceneDev& S, const Node& c, float x, float y, float z
     float sum = 0.0f, sabs = 0.0f;
     bool unc = false, done = false;
     for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
         float tk;
-        float r = item_dr<D>(S, kids[slot], x, y, z, u, fminf(t, tcap), tk);
+        float r = item_dr<D>(S, list ? list[k] : kids[k], x, y, z, u, fminf(t, tcap), tk);
         t = fminf(t, tk);
         if (done) continue;  // greedy value fixed; bounds of the rest still count
         if (isunc(r)) {

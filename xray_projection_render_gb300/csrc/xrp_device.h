@@ -150,7 +150,7 @@ struct SceneDev {
     const Node64* nodes64;
     const int32_t* child;   // child node ids of collections
     const int32_t* cells;   // accel: per collection, (G^3 + 1) offsets into items
-    const int32_t* items;   // accel: child slots (positions within the collection)
+    const int32_t* items;   // accel: node indices of each cell's listed children, in child order
     const float* clear;     // accel: per cell, distance to the nearest child not listed
     const Volume* vols;
     const DefStep* defs;
@@ -435,15 +435,15 @@ XRP_HD float coll32(const SceneDev& S, const Node& c, float x, float y, float z)
     float sum = 0.0f, sabs = 0.0f;
     const int homo = (c.flags >> 8) & 0xff;
     for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
-        const Node& n = S.nodes[kids[slot]];
+        const int kid = list ? list[k] : kids[k];
+        const Node& n = S.nodes[kid];
         float r;
         if (homo == N_CYL)
             r = cyl32(n.f, x, y, z);
         else if (homo == N_SPHERE)
             r = sphere32(n.f, x, y, z);
         else
-            r = item32<D>(S, kids[slot], x, y, z);
+            r = item32<D>(S, kid, x, y, z);
         if (isunc(r)) return r;
         if (greedy && r > 0.0f) return r;
         sum += r;
@@ -636,8 +636,7 @@ XRP_HD float collm32(const SceneDev& S, const Node& c, float x, float y, float z
         cnt = s1 - s0;
     }
     for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
-        m = fminf(m, itemm32<D>(S, kids[slot], x, y, z));
+        m = fminf(m, itemm32<D>(S, list ? list[k] : kids[k], x, y, z));
     }
     return m;
 }
@@ -806,9 +805,8 @@ XRP_HD float coll_dm(const SceneDev& S, const Node& c, float x, float y, float z
     float sum = 0.0f, sabs = 0.0f;
     bool unc = false, done = false;
     for (int k = 0; k < cnt; k++) {
-        int slot = list ? list[k] : k;
         float mk;
-        float r = item_dm<D>(S, kids[slot], x, y, z, mk);
+        float r = item_dm<D>(S, list ? list[k] : kids[k], x, y, z, mk);
         m = fminf(m, mk);
         if (done) continue;  // greedy value fixed; radii of the rest still count
         if (isunc(r)) {
@@ -1154,7 +1152,7 @@ XRP_HD double coll_hyb(const SceneDev& S, int id, double x, double y, double z) 
     const bool greedy = (c.flags & C_GREEDY) != 0;
     double density = 0.0;
     for (int k = 0; k < cnt; k++) {
-        const int kid = kids[list ? list[k] : k];
+        const int kid = list ? list[k] : kids[k];
         const double rho = S.nodes[kid].type <= N_GYROID ? leaf_hyb(S, kid, x, y, z, xf, yf, zf)
                                                          : item_hyb<D>(S, kid, x, y, z);
         if (greedy && rho > 0.0) return rho;

@@ -993,7 +993,7 @@ struct Flattener {
                                 d2 = g * g;
                             }
                             if (d2 == 0) {
-                                fs.items.push_back((int32_t)k);
+                                fs.items.push_back((int32_t)kids[k]);  // node index
                             } else {
                                 clear2 = std::min(clear2, d2);
                             }
