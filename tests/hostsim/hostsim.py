@@ -40,7 +40,7 @@ def lib():
         P, I, D, L_ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_long
         L.hs_render.restype = I
         L.hs_render.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, I, I, I, P, I, I, I, D, D, D,
-                                D, P, P, I, P, L_, I, I, ctypes.c_char_p, I]
+                                D, P, P, I, P, L_, I, I, I, ctypes.c_char_p, I]
         L.hs_margin.restype = I
         L.hs_margin.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, L_, D, D, D, P, P, P, P,
                                 P, P, P, P, ctypes.c_char_p, I]
@@ -106,10 +106,11 @@ def ray_bound(obj, points, dirs, *, deformation=None, R=4.0, fov=40.0, ds=0.01):
 
 def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integration="simple",
            flat_field=0.0, density_multiplier=1.0, rays=None, nthreads=None, force_general=False,
-           trace=False):
+           trace=False, fine_lists=False):
     """cams: array (n, 20) = eye(3), column-major camera(16), fov.  ``trace``:
     certificate tracing (stats[0] counts evaluations); "curve": curved-ray
-    certificates for non-affine chains."""
+    certificates for non-affine chains.  ``fine_lists``: the finer candidate-list
+    grids of large calls and batches."""
     cams = np.ascontiguousarray(cams, dtype=np.float64).reshape(-1, 20)
     n = cams.shape[0]
     vol = None
@@ -132,7 +133,7 @@ def render(obj, cams, res, ds, *, deformation=None, volume=None, R=4.0, integrat
                          nthreads or os.cpu_count() or 1,
                          rays.ctypes.data if rays is not None else None,
                          rays.shape[0] if rays is not None else 0, 1 if force_general else 0,
-                         2 if trace == "curve" else (1 if trace else 0), err, 512)
+                         2 if trace == "curve" else (1 if trace else 0), 1 if fine_lists else 0, err, 512)
     if rc != 0:
         raise ValueError(err.value.decode())
     return out, stats

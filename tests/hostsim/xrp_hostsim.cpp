@@ -15,7 +15,7 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
     const char* obj_json, const char* def_json, const float* vol, int nx, int ny, int nz,
     const double* cams, int ncams, int res, int integration, double ds, double R, double ff,
     double dm, float* out, unsigned long long* stats, int nthreads, const int* rays, long nrays,
-    int force_general, int trace, char* err, int errlen) {
+    int force_general, int trace, int fine_lists, char* err, int errlen) {
     try {
         std::vector<HVolume> ext;
         if (vol) {
@@ -34,7 +34,7 @@ extern "C" __attribute__((visibility("default"))) int hs_render(
             view_from_camera(p, p + 3, p[19], views[c]);
             fov_max = std::max(fov_max, std::fabs(p[19]));
         }
-        HostPrepared hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max, trace != 0);
+        HostPrepared hp = prepare_host(hs, res, integration, ds, R, ff, dm, fov_max, trace != 0, fine_lists != 0);
         for (size_t k = 0; k < hp.vols.size(); k++) {
             hp.vols[k].data = hs.vols[k].data.data();
             hp.vols[k].data64 = hs.vols[k].data64.empty() ? nullptr : hs.vols[k].data64.data();

@@ -55,6 +55,16 @@ def test_deformed_lattice(integration):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_fine_candidate_lists(integration):
+    # the finer list grids of large calls and batches: 12 cells per axis in
+    # the lattice's unit cell, up to 16 in the random scenes' collections
+    check(W.reduced(W.deformed_lattice(), 256, 6), integration, nrays=4000, fine_lists=True)
+    for w in W.batched_scenes(6):
+        check(W.reduced(w, 128, 3), integration, nrays=600, fine_lists=True)
+        check(W.reduced(w, 128, 3), integration, nrays=600, fine_lists=True, trace=True)
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 def test_gyroid_sigmoid(integration):
     check(W.reduced(W.gyroid_sigmoid(), 256, 6), integration)
 

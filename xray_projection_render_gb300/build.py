@@ -26,8 +26,9 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # extra nvcc options, e.g. the occupancy knobs of xrp_launch.h
-# (XRP_NVCC_FLAGS="-DXRP_CURVE_MIN_BLOCKS=3"); they take part in the
-# staleness check through the flags file below
+# (XRP_NVCC_FLAGS="-DXRP_CURVE_MIN_BLOCKS=3"; its -D options reach the host
+# scene code too); they take part in the staleness check through the flags
+# file below
 EXTRA = os.environ.get("XRP_NVCC_FLAGS", "").split()
 
 
@@ -85,7 +86,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     nvcc = _nvcc()
     common_host = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fvisibility=hidden"]
     o_scene = os.path.join(BUILD, "xrp_scene.o")
-    cmds = [["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, "-c",
+    cmds = [["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, *[e for e in EXTRA if e.startswith("-D")], "-c",
              os.path.join(CSRC, "xrp_scene.cpp"), "-o", o_scene]]
     objs = [o_scene]
     for unit in CUDA_UNITS:

@@ -7,6 +7,20 @@
 #include <cstring>
 #include <limits>
 
+// cells per axis of candidate lists, per cube root of the children (build
+// knobs): XRP_LIST_GRID by default, XRP_LIST_GRID_FINE where the caller asks
+// for fine lists, XRP_LIST_GRID_TRACE for uniform collections rendered by
+// certificate tracing
+#ifndef XRP_LIST_GRID
+#define XRP_LIST_GRID 1.6
+#endif
+#ifndef XRP_LIST_GRID_FINE
+#define XRP_LIST_GRID_FINE 4.8
+#endif
+#ifndef XRP_LIST_GRID_TRACE
+#define XRP_LIST_GRID_TRACE 1.2
+#endif
+
 namespace xrp {
 
 static const double kU = 5.9604644775390625e-08;  // 2^-24, FP32 unit roundoff
@@ -529,6 +543,7 @@ struct Flattener {
     FlatScene& fs;
     bool hier;
     bool tracing;  // certificate tracing renders this scene
+    bool fine;     // fine candidate lists (flattening time traded for march time)
     std::vector<int> map;  // host node -> flat node
 
     static int32_t i_of_f(float f) {
@@ -932,15 +947,20 @@ struct Flattener {
                       kn.f[F_RHO] > 0.0f;
         }
         if (kids.size() >= 6 && bounded && !all.empty()) {
-            // cells per axis ~1.6 cbrt(children); tracing a uniform
-            // collection uses ~1.2 cbrt: inside a cell the tracer stops at the
-            // cell's faces, and fewer, fuller cells cost it less (deformed
-            // lattice, 16 struts: 3 cells per axis 464 Mrays/s, 4 cells 424;
-            // with the FP64 pass overlapped, 3 cells 523, 2 cells 396, one
-            // 241: coarser cells cut the evaluations only 7-14 % while each
-            // evaluation reads more struts), while the plain march pays per
-            // candidate (4 cells: 140, 3: 121)
-            const double gs = (tracing && uniform) ? 1.2 : 1.6;
+            // cells per axis ~1.6 cbrt(children), ~4.8 cbrt with fine lists
+            // (at most 16); tracing a uniform collection uses ~1.2 cbrt:
+            // inside a cell the tracer stops at the cell's faces, and fewer,
+            // fuller cells cost it less (deformed lattice, 16 struts: 3 cells
+            // per axis 464 Mrays/s, 4 cells 424; with the FP64 pass
+            // overlapped, 3 cells 523, 2 cells 396, one 241: coarser cells
+            // cut the evaluations only 7-14 % while each evaluation reads
+            // more struts), while the plain march pays per candidate (lattice,
+            // 4 cells per axis 171 Mrays/s, 8: 176, 10: 184, 12: 194; 64
+            // random scenes in one batch, plain 809 -> 1155, traced 4974 ->
+            // 5237) and flattening pays per cell (the lattice 0.2 ms at 4
+            // cells per axis, 7.5 ms at 12)
+            const double gs = (tracing && uniform) ? XRP_LIST_GRID_TRACE
+                                                   : (fine ? XRP_LIST_GRID_FINE : XRP_LIST_GRID);
             int G = (int)std::lround(std::cbrt((double)kids.size()) * gs);
             G = std::max(2, std::min(G, 16));
             double ext = 0;
@@ -1171,7 +1191,8 @@ Box3 def_preimage(const HDef& d, const Box3& b) {
 
 }  // namespace
 
-FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical, bool tracing) {
+FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical, bool tracing,
+                  bool fine_lists) {
     FlatScene fs;
     // position error of the FP32 sample points (per axis), see xrp_device.h
     double half = std::tan(g.fov_deg * 0.5 * M_PI / 180.0);
@@ -1258,7 +1279,7 @@ FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchica
         }
         fs.curve_acc = acc * 1.01 + 1e-12;
     }
-    Flattener F{hs, fs, hierarchical, tracing, {}};
+    Flattener F{hs, fs, hierarchical, tracing, fine_lists, {}};
     Flattener::Info info;
     fs.root = F.node(hs.root, E, P, 0, info);
     // support box: where density may be non-zero
@@ -1500,13 +1521,14 @@ HostLattice build_lattice(double R, double ds, bool hierarchical) {
 }
 
 HostPrepared prepare_host(const HostScene& hs, int res, int integration, double ds, double R,
-                          double flat_field, double density_multiplier, double fov_max, bool tracing) {
+                          double flat_field, double density_multiplier, double fov_max, bool tracing,
+                          bool fine_lists) {
     HostPrepared hp;
     bool hier = integration == 1;
     RenderGeometry g;
     g.R = R;
     g.fov_deg = fov_max;
-    hp.fs = flatten(hs, g, hier, tracing);
+    hp.fs = flatten(hs, g, hier, tracing, fine_lists);
     hp.hl = build_lattice(R, ds, hier);
     if (hp.hl.s64.empty()) {  // keep the tables non-empty; K = 0 means "no samples"
         hp.hl.s64.push_back(0.0);

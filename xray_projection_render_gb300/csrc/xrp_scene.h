@@ -98,8 +98,12 @@ struct FlatScene {
 };
 
 // `tracing`: the scene is rendered by certificate tracing (coarser candidate
-// lists for uniform collections, see Flattener::coll).
-FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical, bool tracing = false);
+// lists for uniform collections, see Flattener::coll).  `fine_lists`: finer
+// candidate-list grids, which shorten the lists the march reads per sample
+// but take longer to build (for large calls and for batches, which flatten
+// once and replay).
+FlatScene flatten(const HostScene& hs, const RenderGeometry& g, bool hierarchical, bool tracing = false,
+                  bool fine_lists = false);
 
 // mathgl restatement for the host-side camera (main.go:226-239).
 void camera_from_angles(double az_deg, double polar_deg, double R, double eye[3], double m[16]);
@@ -132,6 +136,7 @@ struct HostPrepared {
     bool volume_fast = false;
 };
 HostPrepared prepare_host(const HostScene& hs, int res, int integration, double ds, double R,
-                          double flat_field, double density_multiplier, double fov_max, bool tracing = false);
+                          double flat_field, double density_multiplier, double fov_max, bool tracing = false,
+                          bool fine_lists = false);
 
 }  // namespace xrp
