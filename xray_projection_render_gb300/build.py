@@ -86,7 +86,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     nvcc = _nvcc()
     common_host = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fvisibility=hidden"]
     o_scene = os.path.join(BUILD, "xrp_scene.o")
-    cmds = [["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, *[e for e in EXTRA if e.startswith("-D")], "-c",
+    defines = [e for e in EXTRA if e.startswith("-D")]
+    cmds = [["g++", "-std=c++17", *common_host, "-Wall", "-I", INCLUDE, *defines, "-c",
              os.path.join(CSRC, "xrp_scene.cpp"), "-o", o_scene]]
     objs = [o_scene]
     for unit in CUDA_UNITS:
