@@ -59,6 +59,14 @@ def test_fine_candidate_lists(integration):
     # the finer list grids of large calls and batches: 12 cells per axis in
     # the lattice's unit cell, up to 16 in the random scenes' collections
     check(W.reduced(W.deformed_lattice(), 256, 6), integration, nrays=4000, fine_lists=True)
+    # a child left out of a cell's list has density 0 there, so the plain
+    # march reads the same values with either grid: identical images
+    w = W.reduced(W.deformed_lattice(), 96, 3)
+    a, _ = hostsim.render(w.obj, cams_of(w), w.res, w.ds, deformation=w.deformation, R=w.R,
+                          integration=integration)
+    b, _ = hostsim.render(w.obj, cams_of(w), w.res, w.ds, deformation=w.deformation, R=w.R,
+                          integration=integration, fine_lists=True)
+    assert np.array_equal(a, b)
     for w in W.batched_scenes(6):
         check(W.reduced(w, 128, 3), integration, nrays=600, fine_lists=True)
         check(W.reduced(w, 128, 3), integration, nrays=600, fine_lists=True, trace=True)
