@@ -386,14 +386,20 @@ XRP_HD float item_dr(const SceneDev& S, int id, float x, float y, float z, const
             float fx = fmaf(-f12.z, nx, x), fy = fmaf(-f12.w, ny, y), fz = fmaf(-f16.x, nz, z);
             float mu = fminf(fminf(fminf(fx - ub[0], ub[1] - fx), fminf(fy - ub[2], ub[3] - fy)),
                              fminf(fz - ub[4], ub[5] - fz));
-            const float tu = bounds_ray(ub, fx, fy, fz, mu, u.eps + f12.y, u);
-            if (mu < -f12.y) { t = fminf(tt, tu); return 0.0f; }  // outside the unit-cell bounds
+            if (mu < -f12.y) {  // outside the unit-cell bounds: zero up to them
+                t = fminf(tt, bounds_ray(ub, fx, fy, fz, mu, u.eps + f12.y, u));
+                return 0.0f;
+            }
             if (!(mu > f12.y)) { t = 0.0f; return xnan(); }
+            // Inside, the unit-cell bounds need no ray bound of their own: the
+            // fold's period and origin are the unit cell's extent and lower
+            // bounds (objects.go:574-579), so up to tc every sample folds into
+            // this cell at least the fold band away from its faces, where the
+            // inclusive unit-cell test (objects.go:460) holds.
             float tk;
-            const float tm = fminf(fminf(tt, tu), tcap);
             // unit cells are where uniform greedy collections occur (lattices)
-            float r = coll_dr<D - 1, true>(S, S.nodes[n.a], fx, fy, fz, u, tm, tk);
-            t = fminf(fminf(tt, tu), tk);
+            float r = coll_dr<D - 1, true>(S, S.nodes[n.a], fx, fy, fz, u, fminf(tt, tcap), tk);
+            t = fminf(tt, tk);
             return r;
         }
     }
