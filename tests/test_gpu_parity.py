@@ -56,6 +56,21 @@ def _render_both(X, w, integration="simple", stats=False, **kw):
 
 
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
+def test_offset_unit_cell_traced(X, integration):
+    """A tessellated unit cell away from the origin with non-dyadic extents:
+    ray certificates bound the fold cell only (it is the unit cell's box)."""
+    w = W().offset_unit_cell()
+    kw = dict(resolution=w.res, ds=w.ds, R=w.R, fov=w.fov, integration=integration)
+    with X.Scene(w.obj, w.deformation) as s:
+        traced = X.render_proposal(s, None, w.angles, trace=True, **kw)
+        plain = X.render(s, w.angles, **kw)
+    ref = O.render(O.Scene(w.obj, w.deformation), w.angles, w.res, w.ds, R=w.R, fov=w.fov,
+                   integration=integration)
+    _compare(traced, ref)
+    _compare(plain, ref)
+
+
+@pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 def test_cube_minus_sphere_cylinder_full_size(X, integration):
     w = W().cube_minus_sphere_cylinder(512)
     (got, ns, nf), ref = _render_both(X, w, integration, stats=True)

@@ -75,24 +75,10 @@ def test_fine_candidate_lists(integration):
 @pytest.mark.parametrize("integration", ["simple", "hierarchical"])
 @pytest.mark.parametrize("trace", [False, True])
 def test_offset_unit_cell(integration, trace):
-    # a unit cell whose box does not start at the origin and whose extents
-    # are not dyadic, struts reaching its faces, under an affine chain: the
-    # ray certificates bound the fold cell and not the unit-cell box (the
-    # fold cell is that box), which must leave the results exact
-    lo, hi = [0.05, -0.13, 0.2], [0.31, 0.11, 0.37]
-    c = [(l + h) / 2 for l, h in zip(lo, hi)]
-    objs = [{"type": "sphere", "center": c, "radius": 0.06, "rho": 1.0},
-            {"type": "cylinder", "p0": [lo[0], c[1], c[2]], "p1": [hi[0], c[1], c[2]],
-             "radius": 0.025, "rho": 1.0},
-            {"type": "cylinder", "p0": lo, "p1": hi, "radius": 0.02, "rho": 1.0}]
-    uc = {"objects": {"type": "object_collection", "objects": objs},
-          "xmin": lo[0], "xmax": hi[0], "ymin": lo[1], "ymax": hi[1], "zmin": lo[2], "zmax": hi[2]}
-    obj = {"type": "tessellated_obj_coll", "uc": uc,
-           "xmin": -0.9, "xmax": 0.85, "ymin": -0.8, "ymax": 0.95, "zmin": -0.7, "zmax": 0.9}
-    w = W.Workload("offset_unit_cell", obj, {"type": "affine", "matrix": [[1.02, 0.03, 0.0],
-                                                                          [0.0, 0.97, 0.04],
-                                                                          [0.02, 0.0, 1.05]]},
-                   [(17.0, 70.0), (133.0, 95.0), (251.0, 120.0)], 256, 0.003)
+    # the ray certificates bound the fold cell and not the unit-cell box (the
+    # fold cell is that box), which must leave the results exact for a box
+    # away from the origin with non-dyadic extents
+    w = W.offset_unit_cell()
     check(w, integration, nrays=6000, seed=5, trace=trace)
 
 

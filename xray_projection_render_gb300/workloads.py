@@ -89,6 +89,25 @@ def lattice_unit_cell(a=0.2, r=0.03):
             "xmin": 0.0, "xmax": a, "ymin": 0.0, "ymax": a, "zmin": 0.0, "zmax": a}
 
 
+def offset_unit_cell(res=256) -> Workload:
+    """Tessellation of a unit cell whose box does not start at the origin and
+    whose extents are not dyadic (a sphere, an axial and a diagonal strut
+    reaching its faces), under an affine chain; three views, ds 0.003."""
+    lo, hi = [0.05, -0.13, 0.2], [0.31, 0.11, 0.37]
+    c = [(a + b) / 2 for a, b in zip(lo, hi)]
+    objs = [{"type": "sphere", "center": c, "radius": 0.06, "rho": 1.0},
+            {"type": "cylinder", "p0": [lo[0], c[1], c[2]], "p1": [hi[0], c[1], c[2]],
+             "radius": 0.025, "rho": 1.0},
+            {"type": "cylinder", "p0": lo, "p1": hi, "radius": 0.02, "rho": 1.0}]
+    uc = {"objects": {"type": "object_collection", "objects": objs},
+          "xmin": lo[0], "xmax": hi[0], "ymin": lo[1], "ymax": hi[1], "zmin": lo[2], "zmax": hi[2]}
+    obj = {"type": "tessellated_obj_coll", "uc": uc,
+           "xmin": -0.9, "xmax": 0.85, "ymin": -0.8, "ymax": 0.95, "zmin": -0.7, "zmax": 0.9}
+    deform = {"type": "affine", "matrix": [[1.02, 0.03, 0.0], [0.0, 0.97, 0.04], [0.02, 0.0, 1.05]]}
+    return Workload(f"offset_unit_cell_3x{res}^2", obj, deform,
+                    [(17.0, 70.0), (133.0, 95.0), (251.0, 120.0)], res, 0.003)
+
+
 def deformed_lattice(res=1024, views=360, seed=3) -> Workload:
     """Deformed lattice: 16-cylinder cell tessellated 10x10x10 over [-1,1]^3 with 5 %
     axial (zz) strain; seeded random azimuth U[0,360) and polar U[30,150]."""
