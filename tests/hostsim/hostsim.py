@@ -16,27 +16,33 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CSRC = os.path.join(ROOT, "xray_projection_render_gb300", "csrc")
 LIB = os.path.join(HERE, "_build", "libxrp_hostsim.so")
+# AddressSanitizer + UndefinedBehaviorSanitizer build (a process that loads it
+# needs the ASan runtime preloaded); XRP_HOSTSIM_SANITIZED=1 selects it
+LIB_SAN = os.path.join(HERE, "_build", "libxrp_hostsim_san.so")
+SAN_FLAGS = ["-O1", "-g", "-fno-omit-frame-pointer", "-fsanitize=address,undefined",
+             "-fno-sanitize-recover=undefined"]
 _lib = None
 
 
-def build():
+def build(sanitize=False):
+    out = LIB_SAN if sanitize else LIB
     srcs = [os.path.join(HERE, "xrp_hostsim.cpp"), os.path.join(CSRC, "xrp_scene.cpp")]
-    deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
-    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
-        return LIB
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    tmp = LIB + f".tmp{os.getpid()}"
-    subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-                    "-fno-fast-math", "-pthread", "-I", os.path.join(ROOT, "include"), *srcs,
-                    "-o", tmp], check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")] + [__file__]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    tmp = out + f".tmp{os.getpid()}"
+    subprocess.run(["g++", "-std=c++17", *(SAN_FLAGS if sanitize else ["-O2"]), "-fPIC", "-shared",
+                    "-ffp-contract=off", "-fno-fast-math", "-pthread", "-I", os.path.join(ROOT, "include"),
+                    *srcs, "-o", tmp], check=True)
+    os.replace(tmp, out)
+    return out
 
 
 def lib():
     global _lib
     if _lib is None:
-        L = ctypes.CDLL(build())
+        L = ctypes.CDLL(build(sanitize=os.environ.get("XRP_HOSTSIM_SANITIZED") == "1"))
         P, I, D, L_ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_long
         L.hs_render.restype = I
         L.hs_render.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, I, I, I, P, I, I, I, D, D, D,
