@@ -32,16 +32,48 @@ cases = [
     (W.reduced(W.voxel_blobs(n=24), 64, 2), {}),
 ]
 cases += [(W.reduced(w, 64, 2), {"trace": True}) for w in W.batched_scenes(4)]
+# edge cases: nested tessellation, empty and degenerate children, a
+# collection at the list-grid cap, a negative density
+inner = {"type": "tessellated_obj_coll",
+         "uc": {"objects": {"type": "object_collection", "objects": [
+             {"type": "sphere", "center": [0.1, 0.1, 0.1], "radius": 0.08, "rho": 1.0}]},
+                "xmin": 0, "xmax": 0.2, "ymin": 0, "ymax": 0.2, "zmin": 0, "zmax": 0.2},
+         "xmin": 0, "xmax": 0.4, "ymin": 0, "ymax": 0.4, "zmin": 0, "zmax": 0.4}
+nested = {"type": "tessellated_obj_coll",
+          "uc": {"objects": {"type": "object_collection", "objects": [inner]},
+                 "xmin": 0, "xmax": 0.5, "ymin": 0, "ymax": 0.5, "zmin": 0, "zmax": 0.5},
+          "xmin": -1, "xmax": 1, "ymin": -1, "ymax": 1, "zmin": -1, "zmax": 1}
+many = {"type": "object_collection", "objects": [
+    {"type": "sphere", "center": [-0.9 + 0.12 * (k % 15), -0.9 + 0.12 * ((k // 15) % 15), -0.5 + 0.05 * (k // 225)],
+     "radius": 0.05, "rho": 0.3} for k in range(300)]}
+empty = {"type": "object_collection", "objects": []}
+edge = {"type": "object_collection", "objects": [
+    {"type": "cylinder", "p0": [0.1, 0.2, 0.3], "p1": [0.1, 0.2, 0.3], "radius": 0.2, "rho": 1.0},
+    {"type": "sphere", "center": [0.0, 0.0, 0.0], "radius": 0.0, "rho": 1.0},
+    {"type": "cube", "center": [0.2, -0.1, 0.0], "side": 0.5, "rho": 0.7},
+    {"type": "sphere", "center": [0.2, -0.1, 0.0], "radius": 0.2, "rho": -0.4}]}
+for name, obj in (("nested", nested), ("many", many), ("edge", edge), ("empty", empty)):
+    w = W.Workload(name, obj, None, [(30.0, 75.0), (200.0, 110.0)], 64, 0.005)
+    cases += [(w, {}), (w, {"trace": True}), (w, {"fine_lists": True, "trace": True})]
 for w, kw in cases:
     for integration in ("simple", "hierarchical"):
-        check(w, integration, nrays=300, seed=1, nthreads=2, **kw)
+        check(w, integration, nrays=1500, seed=1, nthreads=4, **kw)
+import hostsim
+for bad in ({"type": "sphere", "center": [0, 0]}, {"type": "no_such_object"},
+            {"type": "object_collection", "objects": [{"type": "cylinder"}]}):
+    try:
+        hostsim.render(bad, check.__globals__["cams_of"](cases[0][0]), 16, 0.05)
+    except ValueError:
+        pass
+    else:
+        raise AssertionError("schema error not reported")
 print("sanitized renders ok", len(cases))
 """
 
 
-def _asan_runtime():
+def _runtime(name):
     try:
-        p = subprocess.run(["g++", "-print-file-name=libasan.so"], capture_output=True, text=True,
+        p = subprocess.run(["g++", f"-print-file-name={name}"], capture_output=True, text=True,
                            timeout=30)
     except (OSError, subprocess.TimeoutExpired):
         return None
@@ -50,13 +82,15 @@ def _asan_runtime():
 
 
 def test_per_pixel_code_under_sanitizers():
-    asan = _asan_runtime()
-    if asan is None:
+    asan, cxx = _runtime("libasan.so"), _runtime("libstdc++.so")
+    if asan is None or cxx is None:
         pytest.skip("no AddressSanitizer runtime")
     sys.path.insert(0, os.path.join(HERE, "hostsim"))
     import hostsim
     hostsim.build(sanitize=True)
-    env = dict(os.environ, XRP_HOSTSIM_SANITIZED="1", LD_PRELOAD=asan,
+    # the C++ runtime is preloaded too, so that ASan finds the real
+    # __cxa_throw when the scene loader reports a schema error
+    env = dict(os.environ, XRP_HOSTSIM_SANITIZED="1", LD_PRELOAD=f"{asan} {cxx}",
                ASAN_OPTIONS="detect_leaks=0:abort_on_error=0:exitcode=23",
                UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1:exitcode=24")
     p = subprocess.run([sys.executable, "-c", CHILD, ROOT], capture_output=True, text=True, env=env,
