@@ -714,7 +714,7 @@ static int render_views(Engine* E, const HostScene& hs, const std::vector<const 
     Prepared pr;
     // fine candidate lists from 2^25 rays: the march saves more than the
     // longer flattening costs (deformed lattice, plain: 171 -> 194 Mrays/s
-    // for 0.2 -> 7.5 ms of host time per call)
+    // for 0.1 -> 3.9 ms of host time per call)
     const bool fine = (long long)nviews * res * res >= (1LL << 25);
     int rc = prepare(E, hs, vdev, v64, views, res, o.integration, o.ds, o.R, o.flat_field,
                      o.density_multiplier, fov_max, st, tab, pr,

@@ -957,8 +957,8 @@ struct Flattener {
             // more struts), while the plain march pays per candidate (lattice,
             // 4 cells per axis 171 Mrays/s, 8: 176, 10: 184, 12: 194; 64
             // random scenes in one batch, plain 809 -> 1155, traced 4974 ->
-            // 5237) and flattening pays per cell (the lattice 0.2 ms at 4
-            // cells per axis, 7.5 ms at 12)
+            // 5237) and flattening pays per cell (the lattice 0.1 ms at 4
+            // cells per axis, 3.9 ms at 12)
             const double gs = (tracing && uniform) ? XRP_LIST_GRID_TRACE
                                                    : (fine ? XRP_LIST_GRID_FINE : XRP_LIST_GRID);
             int G = (int)std::lround(std::cbrt((double)kids.size()) * gs);
@@ -978,33 +978,42 @@ struct Flattener {
             double margin = 4 * E + 16 * kU * (P + all.maxabs() + ext) * (G + 1) + 1e-12;
             int cell_base = (int)fs.cells.size();
             c.f[6] = f_of_i(cell_base);
+            // (dilated) cell bounds along each axis; the first/last cells also
+            // hold points beyond the grid
+            auto cell_lo = [&](int a, int i) { return i == 0 ? -kInf : all.lo[a] + i * h3[a] - margin; };
+            auto cell_hi = [&](int a, int i) { return i == G - 1 ? kInf : all.lo[a] + (i + 1) * h3[a] + margin; };
+            // squared gap of every child's box to each slab of cells, per axis
+            // (0 where they overlap); a cell's squared box distance adds its
+            // three slabs' terms in the order x, y, z
+            const size_t nk = kids.size();
+            std::vector<double> sq[3];
+            for (int a = 0; a < 3; a++) {
+                sq[a].assign((size_t)G * nk, 0.0);
+                for (int i = 0; i < G; i++) {
+                    const double l = cell_lo(a, i), u = cell_hi(a, i);
+                    for (size_t k = 0; k < nk; k++) {
+                        const Box3& b = infos[k].box;
+                        if (b.empty()) continue;
+                        double gap = std::max(b.lo[a] - u, l - b.hi[a]);
+                        if (gap > 0) sq[a][(size_t)i * nk + k] = gap * gap;
+                    }
+                }
+            }
             for (int iz = 0; iz < G; iz++)
                 for (int iy = 0; iy < G; iy++)
                     for (int ix = 0; ix < G; ix++) {
                         fs.cells.push_back((int32_t)fs.items.size());
-                        double lo[3] = {all.lo[0] + ix * h3[0] - margin, all.lo[1] + iy * h3[1] - margin,
-                                        all.lo[2] + iz * h3[2] - margin};
-                        double hi[3] = {all.lo[0] + (ix + 1) * h3[0] + margin,
-                                        all.lo[1] + (iy + 1) * h3[1] + margin,
-                                        all.lo[2] + (iz + 1) * h3[2] + margin};
-                        // the first/last cells also hold points beyond the grid
-                        if (ix == 0) lo[0] = -kInf;
-                        if (iy == 0) lo[1] = -kInf;
-                        if (iz == 0) lo[2] = -kInf;
-                        if (ix == G - 1) hi[0] = kInf;
-                        if (iy == G - 1) hi[1] = kInf;
-                        if (iz == G - 1) hi[2] = kInf;
+                        const double lo[3] = {cell_lo(0, ix), cell_lo(1, iy), cell_lo(2, iz)};
+                        const double hi[3] = {cell_hi(0, ix), cell_hi(1, iy), cell_hi(2, iz)};
+                        const double* sx = sq[0].data() + (size_t)ix * nk;
+                        const double* sy = sq[1].data() + (size_t)iy * nk;
+                        const double* sz = sq[2].data() + (size_t)iz * nk;
                         // clearance: distance from the (dilated) cell to the
                         // nearest child that is not listed (certificate radii)
                         double clear2 = kInf;
-                        for (size_t k = 0; k < kids.size(); k++) {
-                            const Box3& b = infos[k].box;
-                            if (b.empty()) continue;
-                            double d2 = 0;
-                            for (int a = 0; a < 3; a++) {
-                                double gap = std::max(b.lo[a] - hi[a], lo[a] - b.hi[a]);
-                                if (gap > 0) d2 += gap * gap;
-                            }
+                        for (size_t k = 0; k < nk; k++) {
+                            if (infos[k].box.empty()) continue;
+                            double d2 = (sx[k] + sy[k]) + sz[k];
                             // spheres and cylinders: the distance to the capsule
                             // (a box hit may still miss the capsule, e.g. a
                             // diagonal strut and a corner cell)
